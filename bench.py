@@ -1,0 +1,282 @@
+"""Benchmark of the path-tracing hot path on one GB300.
+
+Workload (one step = one frame): the Cornell box with mixture-pdf light
+sampling - 555-unit room, 130x105 light at emission 15, 165x330x165 box
+rotated +15 deg, glass sphere r=90 - rendered at 600x600, 1024 samples per
+pixel, max depth 50, reference semantics (black background), FP32 radiance.
+Metric: Msamples/s = 600*600*1024 camera samples / frame time.
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+
+value:  frames rendered from the scene already resident in HBM, image left in
+        HBM, timed with CUDA events on the library's stream; L2 (129 MB) is
+        flushed by writing a 256 MB buffer between timed steps.
+e2e:    the same frame through the C ABI with host buffers: scene-arena upload
+        (H2D), render, image download (D2H) inside the timed region.
+cpu_baseline / --impl reference: the reference algorithm on the host cores
+        (oracle/_ref linked from the reference sources when it was built here,
+        else the CPU oracle port), on a bounded band of image rows.
+Multi-GPU: N independent replicas (one frame each per step), scaling "weak".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "tiny-path-tracer_gb300")
+ORACLE = os.path.join(ROOT, "oracle")
+for _p in (PKG, ORACLE):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+W, H, SPP, DEPTH = 600, 600, 1024, 50
+METRIC = "Msamples/s (Cornell box 600x600, 1024 spp, depth 50, 1 GPU)"
+WORKLOAD = "cornell_box_600x600_1024spp_depth50"
+# wavefront traffic floor per ray segment: ray 32 B written + read, hit 16 B
+# written + read, path state 48 B read + written (the dominant kernel pair)
+BYTES_PER_SEGMENT = 192
+TRAVERSE_BYTES_PER_SEGMENT = 64 + 16  # traverse reads the path record, writes the hit
+
+
+def _peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_leg(text: str, rows: tuple[int, int], spp: int, prefer_ref: bool = True) -> dict:
+    """The reference algorithm on host cores over image rows [rows)."""
+    import pyoracle
+
+    n_samples = (rows[1] - rows[0]) * W * spp
+    cores = os.cpu_count() or 1
+    if prefer_ref and pyoracle.ref_available():
+        rs = pyoracle.RefScene(text)
+        t0 = time.perf_counter()
+        _, secs = rs.render(W, H, spp, DEPTH, lean=1, rows=rows)
+        el = time.perf_counter() - t0
+        kind, threads = "reference", pyoracle.ref_lib().ref_hardware_concurrency()
+        note = "reference sources (oracle/_ref), one std::async task per row as main.cpp:157-159"
+    else:
+        os_ = pyoracle.Scene(text)
+        t0 = time.perf_counter()
+        os_.render(W, H, spp, DEPTH, semantics=0, background=0, seed=9, nthreads=cores, rows=rows)
+        el = time.perf_counter() - t0
+        kind, threads = "port", cores
+        note = "CPU oracle port of the reference algorithm, all host cores"
+    return {"value": n_samples / el / 1e6, "unit": "Msamples/s", "cores": threads, "kind": kind,
+            "sample": f"rows {rows[0]}..{rows[1]} of 600x600 at {spp} spp ({n_samples} samples), {note}",
+            "seconds": el}
+
+
+def reference_arm(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from tpt import scenes
+
+    text = scenes.cornell().text()
+    vals = []
+    leg = None
+    for _ in range(args.warmup):
+        cpu_leg(text, (280, 320), 8)
+    for _ in range(args.steps):
+        leg = cpu_leg(text, (0, 600), 32)
+        vals.append(leg["value"])
+    v = float(np.mean(vals))
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Msamples/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": {"workload": WORKLOAD},
+           "cpu_baseline": {"value": v, "unit": "Msamples/s", "cores": leg["cores"], "kind": leg["kind"],
+                            "sample": leg["sample"]},
+           "e2e": {"value": v, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--engine", type=int, default=0)
+    ap.add_argument("--wave", type=int, default=0)
+    ap.add_argument("--block", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import tpt
+    from tpt import scenes
+
+    text = scenes.cornell().text()
+    ctx = tpt.Context(local)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)  # library work and the timing events share this stream
+    scene = tpt.Scene(text)
+    slot = ctx.upload(scene)
+    arena_bytes = scene.info()["arena_bytes"]
+    img = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    kw = dict(max_depth=DEPTH, engine=args.engine, wave=args.wave, block=args.block, seed=1)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for w in range(args.warmup):
+        ctx.render(slot, W, H, SPP, out=img.data_ptr(), **kw)
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    times, launches, tr_ms, tr_n, segs = [], 0, 0.0, 0, 0
+    for k in range(args.steps):
+        flush.fill_(k & 0xff)  # evict L2 between timed steps (outside the events)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _, st = ctx.render(slot, W, H, SPP, out=img.data_ptr(), profile=True, seed=100 + k, **{
+            x: y for x, y in kw.items() if x != "seed"})
+        e1.record(stream)
+        barrier()
+        times.append(e0.elapsed_time(e1))
+        launches += st["kernel_launches"]
+        tr_ms += st["traverse_ms"]
+        tr_n += st["traverse_launches"]
+        segs += st["segments"]
+    clk = clocks.stop()
+    ms = float(np.sum(times))
+    t_max = ms
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    samples = W * H * SPP * args.steps * world
+    value = samples / (t_max / 1e3) / 1e6
+
+    # e2e through the C ABI with host buffers
+    host_img = np.zeros((H, W, 3), np.float32)
+    e2e_times = []
+    for k in range(max(1, min(args.steps, 3))):
+        barrier()
+        t0 = time.perf_counter()
+        sc = tpt.Scene(text)
+        s2 = ctx.upload(sc)
+        host_img, _ = ctx.render(s2, W, H, SPP, seed=200 + k, **{x: y for x, y in kw.items() if x != "seed"})
+        ctx.release(s2)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_value = W * H * SPP / float(np.mean(e2e_times)) / 1e6
+
+    peaks = _peaks()
+    roof = None
+    if tr_n > 0 and tr_ms > 0:
+        seg_per_launch = segs / tr_n
+        algo_bytes = seg_per_launch * TRAVERSE_BYTES_PER_SEGMENT
+        achieved = algo_bytes / (tr_ms / tr_n / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                "kernel": "k_wf_traverse" if args.engine != 2 else "k_persistent",
+                "peak_source": peaks["source"], "launch_ms": tr_ms / tr_n,
+                "segments_per_launch": seg_per_launch, "bytes_per_segment": TRAVERSE_BYTES_PER_SEGMENT,
+                "traverse_share": tr_ms / ms}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_leg(text, (0, 600), 32)
+        cpu.pop("seconds", None)
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": SPP, "max_depth": DEPTH,
+                          "semantics": "reference", "engine": ["auto", "wavefront", "persistent"][args.engine],
+                          "l2": "flushed between timed steps (256 MB write)",
+                          "segments_per_step": segs / args.steps},
+               "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": int(arena_bytes),
+                       "d2h_bytes_per_step": int(W * H * 3 * 4)},
+               "gpu_launches": int(launches), "clocks": clk, "roofline": roof, "cpu_baseline": cpu}
+        print(json.dumps(out))
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,214 @@
+/*
+ * tpt.h - C ABI of the GB300 (sm_103a) path tracer: the drop-in boundary for
+ * the hot path of BlurryLight/tiny-path-tracer (camera rays -> BVH closest
+ * hit -> material scatter -> mixture-pdf light sampling -> per-pixel
+ * accumulation).
+ *
+ * The reference exposes no FFI: its boundary is the C++ virtual object model
+ * (hitable / material / texture / camera, the free function color()) and the
+ * config.ini keys.  This header maps each of those onto plain C entry points:
+ *
+ *   - scene construction mirrors the reference constructors one to one
+ *     (tpt_sphere <-> sphere::sphere, tpt_bvh_node <-> bvh_node::bvh_node ...)
+ *     and returns integer handles instead of raw pointers;
+ *   - tpt_trace_closest replaces world->hit(r, 0.001, FLT_MAX, rec) for a
+ *     batch of rays;
+ *   - tpt_render replaces the per-row sample loop of main.cpp:109-159 with
+ *     color() (utils.cc:58-94) inside it;
+ *   - tpt_render_params carries the config.ini keys (main.cpp:42-56).
+ *
+ * Conventions: every entry point returns a tpt_status (0 = TPT_OK) or, for
+ * constructors, a non-negative handle / a negative tpt_status.  Buffers are
+ * caller-owned; nothing is retained after a call returns unless stated.  No
+ * entry point exits the process or throws across the ABI.  One tpt_context
+ * per host thread.  There is no CPU fallback: device entry points return
+ * TPT_ERR_NO_DEVICE when no CUDA device is usable.
+ */
+#ifndef TPT_H
+#define TPT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t tpt_status;
+enum {
+  TPT_OK = 0,
+  TPT_ERR_INVALID_ARGUMENT = 1,
+  TPT_ERR_PARSE = 2,
+  TPT_ERR_UNSUPPORTED = 3,      /* scene shape the device layout cannot express */
+  TPT_ERR_NO_BOUNDING_BOX = 4,  /* reference: exit(-1) in box_axis_compare (hitable.cc:20-23) */
+  TPT_ERR_CUDA = 5,
+  TPT_ERR_OUT_OF_MEMORY = 6,
+  TPT_ERR_DEVICE_TIMEOUT = 7,   /* a device loop hit its iteration limit */
+  TPT_ERR_STACK_OVERFLOW = 8,   /* traversal stack deeper than the device stack */
+  TPT_ERR_NO_DEVICE = 9,
+  TPT_ERR_BAD_HANDLE = 10
+};
+
+/* Human-readable name of a status code (static storage). */
+const char *tpt_status_string(tpt_status s);
+/* Library version, e.g. "tpt-gb300 0.1". */
+const char *tpt_version(void);
+/* Detail of the last failing CUDA call on this host thread ("" if none). */
+const char *tpt_last_error(void);
+
+/* ------------------------------------------------------------------------
+ * Scene construction.  A builder holds a scene graph made of the reference's
+ * classes.  Handles are per-kind integers (textures, materials, hitables).
+ * ---------------------------------------------------------------------- */
+typedef struct tpt_builder tpt_builder;
+
+tpt_status tpt_builder_create(tpt_builder **out);
+void tpt_builder_destroy(tpt_builder *b);
+
+/* Textures: headers/texture.h:15-51. */
+int32_t tpt_constant_texture(tpt_builder *b, float r, float g, float bl);          /* texture.h:15-24 */
+int32_t tpt_checker_texture(tpt_builder *b, int32_t odd, int32_t even);           /* texture.cc:4-16 */
+int32_t tpt_perlin_noise_texture(tpt_builder *b, float scale);                    /* texture.cc:18-25 */
+/* Shared perlin tables (perlin_noise.h:13-16): 256 gradients (x,y,z) and the
+ * x, y, z permutations of 0..255.  Without this call the builder fills them
+ * from its drand_r stream like perlin_noise.cc:3-21 (the permutation shuffle
+ * uses a fixed-seed engine instead of the reference's clock seed). */
+tpt_status tpt_perlin_tables(tpt_builder *b, const float *gradients768, const int32_t *perm768);
+/* image_texture (texture.cc:27-42): RGB8, width*height*3 bytes, copied. */
+int32_t tpt_image_texture(tpt_builder *b, const uint8_t *rgb, int32_t width, int32_t height);
+
+/* Materials: headers/material.h:27-79. */
+int32_t tpt_lambertian(tpt_builder *b, int32_t albedo_tex);                       /* material.cc:3-17 */
+int32_t tpt_metal(tpt_builder *b, float r, float g, float bl, float fuzz);        /* material.h:39-50 */
+int32_t tpt_dielectric(tpt_builder *b, float ref_idx);                            /* material.cc:19-70 */
+int32_t tpt_diffuse_light(tpt_builder *b, int32_t emit_tex);                      /* material.cc:79-86 */
+int32_t tpt_isotropic(tpt_builder *b, int32_t albedo_tex);                        /* material.h:72-79 */
+
+/* Hitables: headers/sphere.h, rect_box.h, hitable.h, hitable_list.h. */
+int32_t tpt_sphere(tpt_builder *b, float cx, float cy, float cz, float radius, int32_t mat);   /* sphere.h:6-21 */
+int32_t tpt_moving_sphere(tpt_builder *b, float c0x, float c0y, float c0z, float c1x, float c1y, float c1z,
+                          float t0, float t1, float radius, int32_t mat);                      /* sphere.h:23-40 */
+int32_t tpt_xy_rect(tpt_builder *b, float x0, float x1, float y0, float y1, float k, int32_t mat); /* rect_box.h:5-15 */
+int32_t tpt_xz_rect(tpt_builder *b, float x0, float x1, float z0, float z1, float k, int32_t mat); /* rect_box.h:17-30 */
+int32_t tpt_yz_rect(tpt_builder *b, float y0, float y1, float z0, float z1, float k, int32_t mat); /* rect_box.h:32-42 */
+int32_t tpt_flip_normal(tpt_builder *b, int32_t child);                                       /* rect_box.h:44-60 */
+int32_t tpt_box(tpt_builder *b, float x0, float y0, float z0, float x1, float y1, float z1, int32_t mat); /* rect_box.h:62-74 */
+int32_t tpt_translate(tpt_builder *b, int32_t child, float ox, float oy, float oz);           /* rect_box.h:77-99 */
+int32_t tpt_rotate_y(tpt_builder *b, int32_t child, float angle_degrees);                     /* rect_box.h:101-116 */
+int32_t tpt_constant_medium(tpt_builder *b, int32_t boundary, float density, int32_t tex);   /* hitable.h:58-69 */
+int32_t tpt_hitable_list(tpt_builder *b, const int32_t *items, int32_t n);                   /* hitable_list.h:4-19 */
+/* bvh_node (hitable.cc:32-56): built immediately, drawing its split axes from
+ * the builder's drand_r stream (std::mt19937 in its default state when the
+ * builder is created), so topology matches the reference bit for bit.
+ * Returns TPT_ERR_NO_BOUNDING_BOX (negated) where the reference would exit. */
+int32_t tpt_bvh_node(tpt_builder *b, const int32_t *items, int32_t n, float t0, float t1);
+
+tpt_status tpt_builder_set_world(tpt_builder *b, int32_t world);
+/* light_shape argument of color() (utils.h:26-27); -1 = none (pure cosine). */
+tpt_status tpt_builder_set_light_shape(tpt_builder *b, int32_t light_shape);
+/* camera_with_blur constructor (camera.cc:2-21). */
+tpt_status tpt_builder_set_camera(tpt_builder *b, const float lookfrom[3], const float lookat[3], const float vup[3],
+                                  float vfov, float aspect, float aperture, float focus_dist, float t0, float t1);
+
+/* ------------------------------------------------------------------------
+ * Compiled scenes: the builder graph flattened into the device layout
+ * (BVH nodes as 32-byte {min.xyz,left}{max.xyz,right} SoA records, leaf and
+ * material tables).  Host memory; immutable.
+ * ---------------------------------------------------------------------- */
+typedef struct tpt_scene tpt_scene;
+
+tpt_status tpt_scene_compile(const tpt_builder *b, tpt_scene **out);
+/* Parse scene-description text (the statement format documented in
+ * docs of the package loader) into a builder and compile it. */
+tpt_status tpt_scene_from_text(const char *sd_text, tpt_scene **out, char *err, size_t errlen);
+void tpt_scene_destroy(tpt_scene *s);
+
+typedef struct {
+  int32_t n_nodes, n_leaves, n_items, n_blas;
+  int32_t n_materials, n_textures, n_lights, max_stack;
+  int64_t arena_bytes;
+} tpt_scene_info;
+tpt_status tpt_scene_get_info(const tpt_scene *s, tpt_scene_info *out);
+
+/* Pre-order dump of the BVH built for builder hitable `handle` (a
+ * tpt_bvh_node).  Per node: box (6 floats) and (left, right), a child >= 0
+ * being a pre-order node index and a child < 0 being -(1 + hitable handle of
+ * the leaf).  Returns the node count (call with cap 0 to size), or < 0. */
+int32_t tpt_scene_bvh_dump(const tpt_scene *s, int32_t handle, float *boxes, int32_t *kids, int32_t cap);
+
+/* ------------------------------------------------------------------------
+ * Device context.
+ * ---------------------------------------------------------------------- */
+typedef struct tpt_context tpt_context;
+
+tpt_status tpt_context_create(int32_t device, tpt_context **out);
+void tpt_context_destroy(tpt_context *ctx);
+/* Use this cudaStream_t (passed as void*) for all later work; NULL = the
+ * context's own stream. */
+tpt_status tpt_context_set_stream(tpt_context *ctx, void *stream);
+/* Copy a compiled scene into device memory; returns a slot id. */
+tpt_status tpt_scene_upload(tpt_context *ctx, const tpt_scene *s, int32_t *slot);
+tpt_status tpt_scene_release(tpt_context *ctx, int32_t slot);
+
+/* Memory location flags for caller buffers. */
+enum { TPT_MEM_HOST = 0, TPT_MEM_DEVICE = 1 };
+
+/* Batched world->hit(r, 0.001, FLT_MAX, rec) (hitable.h:30-39).
+ * rays: n x 7 floats (ox,oy,oz,dx,dy,dz,time).  hit_f: n x 9 floats
+ * (t,u,v,px,py,pz,nx,ny,nz); hit_i: n x 2 int32 (hit flag, hitable handle of
+ * the primitive hit, -1 on a miss).  The free-flight uniform of a
+ * constant_medium is Philox-4x32-10 of (ray index, medium handle) keyed by
+ * `seed`.  mem = TPT_MEM_HOST or TPT_MEM_DEVICE for all three buffers. */
+tpt_status tpt_trace_closest(tpt_context *ctx, int32_t slot, const float *rays, int64_t n, uint64_t seed,
+                             float *hit_f, int32_t *hit_i, int32_t mem);
+
+/* Render parameters: the config.ini keys (main.cpp:42-56) plus the
+ * integrator switches. */
+enum { TPT_SEMANTICS_REFERENCE = 0, TPT_SEMANTICS_PHYSICAL = 1 };
+enum { TPT_BACKGROUND_BLACK = 0, TPT_BACKGROUND_SKY = 1 };
+enum { TPT_ENGINE_AUTO = 0, TPT_ENGINE_WAVEFRONT = 1, TPT_ENGINE_PERSISTENT = 2 };
+typedef struct {
+  int32_t width, height;    /* [DEFAULT] width, height */
+  int32_t spp;              /* [DEFAULT] sample */
+  int32_t max_depth;        /* [DEFAULT] recur_depth */
+  int32_t semantics;        /* TPT_SEMANTICS_* */
+  int32_t background;       /* TPT_BACKGROUND_* */
+  float sky_scale;          /* sky gradient scale (utils.cc:87-90 uses 0.1) */
+  uint64_t seed;            /* RNG key */
+  int32_t engine;           /* TPT_ENGINE_* */
+  int32_t block;            /* threads per block, 0 = tuned */
+  int32_t wave;             /* wavefront path slots, 0 = tuned */
+  int32_t accumulate_fp64;  /* 1: also accumulate in double (out_rgb is the FP64 mean) */
+  int32_t profile;          /* 1: time each traverse/shade launch with CUDA events */
+} tpt_render_params;
+
+typedef struct {
+  int64_t samples;          /* camera samples traced */
+  int64_t segments;         /* rays traced (all bounces) */
+  int32_t iterations;       /* wavefront iterations / persistent launches */
+  int32_t kernel_launches;  /* kernels this library launched */
+  double device_ms;         /* device time of the render, CUDA events */
+  double traverse_ms;       /* profile=1: summed device time of the traversal launches */
+  double shade_ms;          /* profile=1: summed device time of the shading launches */
+  int32_t traverse_launches;
+  int32_t shade_launches;
+} tpt_render_stats;
+
+void tpt_render_params_default(tpt_render_params *p);
+
+/* Render the scene in `slot`.  out_rgb: width*height*3 floats, row 0 = top
+ * image row, each the mean of de_nan(color()) over spp samples (linear, before
+ * the gamma of main.cpp:136).  mem = TPT_MEM_HOST or TPT_MEM_DEVICE.
+ * stats may be NULL. */
+tpt_status tpt_render(tpt_context *ctx, int32_t slot, const tpt_render_params *p, float *out_rgb, int32_t mem,
+                      tpt_render_stats *stats);
+
+/* Host helpers: reference output quantisation (main.cpp:135-142,176-182) and
+ * the PPM P3 writer of main.cpp:69,183-189. */
+void tpt_quantize(const float *mean_rgb, int64_t n_pixels, uint8_t *rgb8);
+tpt_status tpt_write_ppm(const char *path, const uint8_t *rgb8, int32_t width, int32_t height);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TPT_H */

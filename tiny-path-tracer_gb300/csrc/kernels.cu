@@ -1,0 +1,718 @@
+// kernels.cu - sm_103a kernels of the hot path and the device half of the
+// C ABI (context, scene upload, batched closest hit, render).
+//
+// Render engines (same device functions, different schedulers):
+//   wavefront   generate -> [traverse -> shade]* with path regeneration:
+//               SoA path state in two ping-pong buffers, paths that survive a
+//               bounce or that replace a finished path are compacted into the
+//               other buffer with __ballot_sync + one atomic per warp; the
+//               iteration pair is replayed from a CUDA graph.
+//   persistent  one launch of SM-count x occupancy blocks; each warp claims
+//               camera samples from a global counter (one atomic per warp)
+//               and carries its paths to termination in registers.
+// Both accumulate into a float4 image buffer (optionally also double) with
+// vector atomics; `resolve` divides by spp.  No kernel waits on another and
+// every loop is bounded by the sample count and max_depth.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "../../include/tpt.h"
+#include "arena.h"
+#include "device.cuh"
+#include "scene_internal.h"
+
+namespace tpt {
+
+// ------------------------------------------------------------ counters ----
+struct WfCounters {
+  unsigned int count[2];        // live paths in each ping-pong buffer
+  unsigned long long issued;    // camera samples handed out
+  unsigned long long segments;  // rays traced
+  int err;
+  int pad;
+};
+
+// SoA path state (64 bytes per path).
+struct PathBuf {
+  float4 *o_time;   // origin, ray time
+  float4 *d_depth;  // direction, bounce depth (int bits)
+  float4 *thr_pix;  // throughput, pixel (int bits)
+  float4 *rad_smp;  // radiance so far, sample index (int bits)
+};
+
+__device__ __forceinline__ void warp_claim(bool want, unsigned long long *counter, unsigned long long &base,
+                                           int &rank) {
+  const unsigned mask = __ballot_sync(0xffffffffu, want);
+  const int lane = threadIdx.x & 31;
+  rank = __popc(mask & ((1u << lane) - 1u));
+  unsigned long long b = 0;
+  const int leader = mask ? __ffs(mask) - 1 : 0;
+  if (want && lane == leader) b = atomicAdd(counter, (unsigned long long)__popc(mask));
+  base = __shfl_sync(0xffffffffu, b, leader);
+}
+
+__device__ __forceinline__ unsigned warp_append(bool want, unsigned int *counter) {
+  const unsigned mask = __ballot_sync(0xffffffffu, want);
+  const int lane = threadIdx.x & 31;
+  const int rank = __popc(mask & ((1u << lane) - 1u));
+  unsigned b = 0;
+  const int leader = mask ? __ffs(mask) - 1 : 0;
+  if (want && lane == leader) b = atomicAdd(counter, (unsigned)__popc(mask));
+  b = __shfl_sync(0xffffffffu, b, leader);
+  return b + rank;
+}
+
+struct FrameDesc {
+  int nx, ny, spp;
+  unsigned long long total;  // nx*ny*spp
+  float4 *accum;             // per pixel sum (xyz)
+  double *accum64;           // optional per pixel double sum (3 per pixel)
+};
+
+// sample index s -> (pixel, sample number): pixel-major within a pass so a
+// warp's camera rays are neighbours.
+__device__ __forceinline__ void sample_coords(const FrameDesc &F, unsigned long long s, uint32_t &pixel,
+                                              uint32_t &sample, int &i, int &j) {
+  const unsigned long long npix = (unsigned long long)F.nx * F.ny;
+  sample = (uint32_t)(s / npix);
+  pixel = (uint32_t)(s - (unsigned long long)sample * npix);
+  const int row = (int)(pixel / (uint32_t)F.nx);  // 0 = top row
+  i = (int)(pixel - (uint32_t)row * F.nx);
+  j = F.ny - 1 - row;
+}
+
+__device__ __forceinline__ void accumulate(const FrameDesc &F, uint32_t pixel, float3 L) {
+  L = de_nan(L);
+  atomicAdd(F.accum + pixel, make_float4(L.x, L.y, L.z, 0.f));
+  if (F.accum64) {
+    atomicAdd(F.accum64 + 3 * (size_t)pixel, (double)L.x);
+    atomicAdd(F.accum64 + 3 * (size_t)pixel + 1, (double)L.y);
+    atomicAdd(F.accum64 + 3 * (size_t)pixel + 2, (double)L.z);
+  }
+}
+
+__device__ __forceinline__ void write_path(const PathBuf &B, unsigned idx, const Ray &r, int depth, float3 T,
+                                           float3 L, uint32_t pixel, uint32_t sample) {
+  B.o_time[idx] = make_float4(r.o.x, r.o.y, r.o.z, r.time);
+  B.d_depth[idx] = make_float4(r.d.x, r.d.y, r.d.z, __int_as_float(depth));
+  B.thr_pix[idx] = make_float4(T.x, T.y, T.z, __int_as_float((int)pixel));
+  B.rad_smp[idx] = make_float4(L.x, L.y, L.z, __int_as_float((int)sample));
+}
+
+// ---------------------------------------------------------------- kernels -
+
+// Batched world->hit for the parity boundary (tpt_trace_closest).
+__global__ void k_trace_closest(DevScene S, const float *__restrict__ rays, long long n, uint2 key,
+                                float *__restrict__ hit_f, int *__restrict__ hit_i, int *err) {
+  extern __shared__ int2 stack_smem[];
+  int2 *stk = stack_smem + threadIdx.x;
+  int e = 0;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const float *q = rays + 7 * k;
+    Ray r{v3(q[0], q[1], q[2]), v3(q[3], q[4], q[5]), q[6]};
+    MediumRng m{make_uint4((uint32_t)k, (uint32_t)(k >> 32), 0u, 0x4d454449u), key, 0};
+    HitRef h;
+    float *o = hit_f + 9 * k;
+    if (trace_closest(S, r, 0.001f, stk, blockDim.x, m, h, e)) {
+      Surface sf;
+      finalize(S, r, h, sf);
+      o[0] = h.t; o[1] = sf.u; o[2] = sf.v;
+      o[3] = sf.p.x; o[4] = sf.p.y; o[5] = sf.p.z;
+      o[6] = sf.n.x; o[7] = sf.n.y; o[8] = sf.n.z;
+      hit_i[2 * k] = 1;
+      hit_i[2 * k + 1] = S.leaf_user[h.leaf];
+    } else {
+      for (int c = 0; c < 9; c++) o[c] = 0.f;
+      hit_i[2 * k] = 0;
+      hit_i[2 * k + 1] = -1;
+    }
+  }
+  if (e) atomicExch(err, e);
+}
+
+// Fills slots [0, count) of a path buffer with camera samples first..first+count.
+__global__ void k_wf_generate(DevScene S, FrameDesc F, PathBuf out, unsigned long long first, unsigned count,
+                              uint2 key) {
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+    uint32_t pixel, sample;
+    int i, j;
+    sample_coords(F, first + k, pixel, sample, i, j);
+    const Ray r = camera_ray(S.cam, i, j, F.nx, F.ny, pixel, sample, key);
+    write_path(out, k, r, 0, v3(1.f, 1.f, 1.f), v3(0.f, 0.f, 0.f), pixel, sample);
+  }
+}
+
+// Closest hit for every live path of buffer `cur`; also clears the append
+// counter of the other buffer for the following shade pass.
+__global__ void k_wf_traverse(DevScene S, PathBuf in, int cur, WfCounters *C, int4 *__restrict__ hits, uint2 key) {
+  extern __shared__ int2 stack_smem[];
+  int2 *stk = stack_smem + threadIdx.x;
+  const unsigned n = C->count[cur];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    C->count[cur ^ 1] = 0;
+    C->segments += n;
+  }
+  int e = 0;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const float4 ot = in.o_time[k], dd = in.d_depth[k];
+    const float4 tp = in.thr_pix[k], rs = in.rad_smp[k];
+    const Ray r{v3(ot.x, ot.y, ot.z), v3(dd.x, dd.y, dd.z), ot.w};
+    MediumRng m{make_uint4((uint32_t)__float_as_int(tp.w), (uint32_t)__float_as_int(rs.w),
+                           (uint32_t)__float_as_int(dd.w), 0u), key, 1};
+    HitRef h;
+    if (trace_closest(S, r, 0.001f, stk, blockDim.x, m, h, e))
+      hits[k] = make_int4(__float_as_int(h.t), h.leaf, h.inst, h.face);
+    else
+      hits[k] = make_int4(0, -1, -1, -1);
+  }
+  if (e) atomicExch(&C->err, e);
+}
+
+// Shades every live path of buffer `cur`; survivors and regenerated camera
+// paths are appended (compacted) to buffer cur^1; finished paths are
+// accumulated.
+__global__ void k_wf_shade(DevScene S, RenderCfg cfg, FrameDesc F, PathBuf in, PathBuf out, int cur, WfCounters *C,
+                           const int4 *__restrict__ hits) {
+  const unsigned n = C->count[cur];
+  const unsigned stride = gridDim.x * blockDim.x;
+  // whole warps iterate together (ballots need converged lanes)
+  const unsigned n_round = (n + 31u) & ~31u;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n_round; k += stride) {
+    const bool live = k < n;
+    bool cont = false;
+    Ray r{};
+    int depth = 0;
+    float3 T = v3(0.f, 0.f, 0.f), L = v3(0.f, 0.f, 0.f);
+    uint32_t pixel = 0, sample = 0;
+    if (live) {
+      const float4 ot = in.o_time[k], dd = in.d_depth[k];
+      const float4 tp = in.thr_pix[k], rs = in.rad_smp[k];
+      r = Ray{v3(ot.x, ot.y, ot.z), v3(dd.x, dd.y, dd.z), ot.w};
+      depth = __float_as_int(dd.w);
+      T = v3(tp.x, tp.y, tp.z);
+      L = v3(rs.x, rs.y, rs.z);
+      pixel = (uint32_t)__float_as_int(tp.w);
+      sample = (uint32_t)__float_as_int(rs.w);
+      const int4 hv = hits[k];
+      const HitRef h{__int_as_float(hv.x), hv.y, hv.z, hv.w};
+      cont = shade_vertex(S, cfg, r, hv.y >= 0, h, T, L, depth, pixel, sample);
+      if (cont) {
+        depth++;
+      } else {
+        accumulate(F, pixel, L);
+      }
+    }
+    // regenerate finished paths from the global sample counter
+    const bool want = live && !cont;
+    unsigned long long base;
+    int rank;
+    warp_claim(want, &C->issued, base, rank);
+    bool fresh = false;
+    if (want) {
+      const unsigned long long s = base + (unsigned long long)rank;
+      if (s < F.total) {
+        int i, j;
+        sample_coords(F, s, pixel, sample, i, j);
+        r = camera_ray(S.cam, i, j, F.nx, F.ny, pixel, sample, cfg.key);
+        depth = 0;
+        T = v3(1.f, 1.f, 1.f);
+        L = v3(0.f, 0.f, 0.f);
+        fresh = true;
+      }
+    }
+    const bool emit = cont || fresh;
+    const unsigned slot = warp_append(emit, &C->count[cur ^ 1]);
+    if (emit) write_path(out, slot, r, depth, T, L, pixel, sample);
+  }
+}
+
+// Persistent engine: warps claim camera samples until all are issued and
+// trace each path to termination.
+__global__ void k_persistent(DevScene S, RenderCfg cfg, FrameDesc F, WfCounters *C) {
+  extern __shared__ int2 stack_smem[];
+  int2 *stk = stack_smem + threadIdx.x;
+  int e = 0;
+  unsigned long long segs = 0;
+  for (;;) {
+    unsigned long long base;
+    int rank;
+    warp_claim(true, &C->issued, base, rank);
+    const unsigned long long s = base + (unsigned long long)rank;
+    if (base >= F.total) break;  // warp-uniform
+    if (s < F.total) {
+      uint32_t pixel, sample;
+      int i, j;
+      sample_coords(F, s, pixel, sample, i, j);
+      Ray r = camera_ray(S.cam, i, j, F.nx, F.ny, pixel, sample, cfg.key);
+      float3 T = v3(1.f, 1.f, 1.f), L = v3(0.f, 0.f, 0.f);
+      for (int depth = 0;; depth++) {
+        MediumRng m{make_uint4(pixel, sample, (uint32_t)depth, 0u), cfg.key, 1};
+        HitRef h;
+        const bool hit = trace_closest(S, r, 0.001f, stk, blockDim.x, m, h, e);
+        segs++;
+        if (!shade_vertex(S, cfg, r, hit, h, T, L, depth, pixel, sample)) break;
+      }
+      accumulate(F, pixel, L);
+    }
+  }
+  if (segs) atomicAdd(&C->segments, segs);
+  if (e) atomicExch(&C->err, e);
+}
+
+// mean = sum / spp, image order (row 0 = top).
+__global__ void k_resolve(FrameDesc F, float *__restrict__ out) {
+  const long long npix = (long long)F.nx * F.ny;
+  const float inv = 1.0f / (float)F.spp;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix; p += (long long)gridDim.x * blockDim.x) {
+    if (F.accum64) {
+      const double d = (double)F.spp;
+      out[3 * p] = (float)(F.accum64[3 * p] / d);
+      out[3 * p + 1] = (float)(F.accum64[3 * p + 1] / d);
+      out[3 * p + 2] = (float)(F.accum64[3 * p + 2] / d);
+    } else {
+      const float4 a = F.accum[p];
+      out[3 * p] = a.x * inv;
+      out[3 * p + 1] = a.y * inv;
+      out[3 * p + 2] = a.z * inv;
+    }
+  }
+}
+
+}  // namespace tpt
+
+using namespace tpt;
+
+// ============================================================== context ===
+namespace {
+
+struct Slot {
+  void *arena = nullptr;
+  size_t bytes = 0;
+  DevScene ds{};
+  bool live = false;
+};
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct tpt_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own = nullptr;
+  int sm_count = 0;
+  std::vector<Slot> slots;
+  DevBuf path[2], hits, accum, accum64, staging, rays, hitf, hiti;
+  WfCounters *counters = nullptr;       // device
+  WfCounters *counters_host = nullptr;  // pinned
+  int *err = nullptr;                   // device error flag for trace
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t prof_ev[24] = {};  // per-launch timing of one graph (8 iterations x 3)
+  // cached wavefront graph
+  cudaGraphExec_t graph = nullptr;
+  size_t graph_key = 0;
+};
+
+static thread_local char g_last_error[256] = "";
+
+static tpt_status cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return TPT_OK;
+  std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
+  if (e == cudaErrorMemoryAllocation) return TPT_ERR_OUT_OF_MEMORY;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return TPT_ERR_NO_DEVICE;
+  return TPT_ERR_CUDA;
+}
+#define TPT_CUDA(x)                              \
+  do {                                           \
+    cudaError_t e_ = (x);                        \
+    if (e_ != cudaSuccess) return cuda_status(e_); \
+  } while (0)
+
+static tpt_status ensure(DevBuf &b, size_t bytes) {
+  if (b.bytes >= bytes) return TPT_OK;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  TPT_CUDA(cudaMalloc(&b.p, bytes));
+  b.bytes = bytes;
+  return TPT_OK;
+}
+
+static int stack_smem(int block) { return block * TRAVERSAL_STACK * (int)sizeof(int2); }
+
+template <class K>
+static int grid_for(const tpt_context *ctx, K kernel, int block, int smem) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
+  if (per_sm < 1) per_sm = 1;
+  return ctx->sm_count * per_sm;
+}
+
+extern "C" {
+
+const char *tpt_last_error(void) { return g_last_error; }
+
+tpt_status tpt_context_create(int32_t device, tpt_context **out) {
+  if (!out) return TPT_ERR_INVALID_ARGUMENT;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return TPT_ERR_NO_DEVICE;
+  if (device < 0 || device >= n) return TPT_ERR_INVALID_ARGUMENT;
+  TPT_CUDA(cudaSetDevice(device));
+  auto *c = new (std::nothrow) tpt_context();
+  if (!c) return TPT_ERR_OUT_OF_MEMORY;
+  c->device = device;
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  cudaError_t e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&c->counters, sizeof(WfCounters));
+  if (e == cudaSuccess) e = cudaMallocHost(&c->counters_host, sizeof(WfCounters));
+  if (e == cudaSuccess) e = cudaMalloc(&c->err, sizeof(int));
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+  if (e != cudaSuccess) {
+    tpt_context_destroy(c);
+    return cuda_status(e);
+  }
+  c->stream = c->own;
+  *out = c;
+  return TPT_OK;
+}
+
+void tpt_context_destroy(tpt_context *c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto &s : c->slots)
+    if (s.arena) cudaFree(s.arena);
+  DevBuf *bufs[] = {&c->path[0], &c->path[1], &c->hits, &c->accum, &c->accum64,
+                    &c->staging, &c->rays, &c->hitf, &c->hiti};
+  for (DevBuf *b : bufs)
+    if (b->p) cudaFree(b->p);
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  if (c->counters) cudaFree(c->counters);
+  if (c->counters_host) cudaFreeHost(c->counters_host);
+  if (c->err) cudaFree(c->err);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  for (auto &ev : c->prof_ev)
+    if (ev) cudaEventDestroy(ev);
+  if (c->own) cudaStreamDestroy(c->own);
+  delete c;
+}
+
+tpt_status tpt_context_set_stream(tpt_context *c, void *stream) {
+  if (!c) return TPT_ERR_INVALID_ARGUMENT;
+  c->stream = stream ? (cudaStream_t)stream : c->own;
+  if (c->graph) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+  }
+  return TPT_OK;
+}
+
+tpt_status tpt_scene_upload(tpt_context *c, const tpt_scene *sc, int32_t *slot) {
+  if (!c || !sc || !slot) return TPT_ERR_INVALID_ARGUMENT;
+  const HostScene &S = *host_scene(sc);
+  TPT_CUDA(cudaSetDevice(c->device));
+  const ArenaLayout L = arena_layout(S);
+  std::vector<uint8_t> host(L.total, 0);
+  const void *src[15] = {S.node_lo.data(),   S.node_hi.data(), S.leaf_hdr.data(), S.leaf_user.data(),
+                         S.leaf_data.data(), S.items.data(),   S.mat_i.data(),    S.mat_f.data(),
+                         S.tex_i.data(),     S.tex_f.data(),   S.images.data(),   S.perlin_grad.data(),
+                         S.perlin_perm.data(), S.light_i.data(), S.light_f.data()};
+  const size_t len[15] = {S.node_lo.size() * sizeof(f4),   S.node_hi.size() * sizeof(f4),
+                          S.leaf_hdr.size() * sizeof(i4),  S.leaf_user.size() * sizeof(int32_t),
+                          S.leaf_data.size() * sizeof(f4), S.items.size() * sizeof(i2),
+                          S.mat_i.size() * sizeof(i4),     S.mat_f.size() * sizeof(f4),
+                          S.tex_i.size() * sizeof(i4),     S.tex_f.size() * sizeof(f4),
+                          S.images.size(),                 S.perlin_grad.size() * sizeof(f4),
+                          S.perlin_perm.size() * sizeof(int32_t), S.light_i.size() * sizeof(i4),
+                          S.light_f.size() * sizeof(f4)};
+  for (int i = 0; i < 15; i++)
+    if (len[i]) std::memcpy(host.data() + L.off[i], src[i], len[i]);
+  Slot s;
+  TPT_CUDA(cudaMalloc(&s.arena, L.total));
+  cudaError_t e = cudaMemcpyAsync(s.arena, host.data(), L.total, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    cudaFree(s.arena);
+    return cuda_status(e);
+  }
+  s.bytes = L.total;
+  uint8_t *base = (uint8_t *)s.arena;
+  DevScene &d = s.ds;
+  d.node_lo = (const f4 *)(base + L.off[0]);
+  d.node_hi = (const f4 *)(base + L.off[1]);
+  d.leaf_hdr = (const i4 *)(base + L.off[2]);
+  d.leaf_user = (const int32_t *)(base + L.off[3]);
+  d.leaf_data = (const f4 *)(base + L.off[4]);
+  d.items = (const i2 *)(base + L.off[5]);
+  d.mat_i = (const i4 *)(base + L.off[6]);
+  d.mat_f = (const f4 *)(base + L.off[7]);
+  d.tex_i = (const i4 *)(base + L.off[8]);
+  d.tex_f = (const f4 *)(base + L.off[9]);
+  d.images = base + L.off[10];
+  d.perlin_grad = (const f4 *)(base + L.off[11]);
+  d.perlin_perm = (const int32_t *)(base + L.off[12]);
+  d.light_i = (const i4 *)(base + L.off[13]);
+  d.light_f = (const f4 *)(base + L.off[14]);
+  d.n_nodes = (int32_t)S.node_lo.size();
+  d.n_leaves = (int32_t)S.leaf_hdr.size();
+  d.n_items = (int32_t)S.items.size();
+  d.n_mats = (int32_t)S.mat_i.size();
+  d.n_texs = (int32_t)S.tex_i.size();
+  d.n_lights = (int32_t)S.light_i.size();
+  d.light_is_list = S.light_is_list;
+  d.has_lights = S.has_lights;
+  d.cam = S.cam;
+  s.live = true;
+  for (size_t i = 0; i < c->slots.size(); i++)
+    if (!c->slots[i].live) {
+      c->slots[i] = s;
+      *slot = (int32_t)i;
+      return TPT_OK;
+    }
+  c->slots.push_back(s);
+  *slot = (int32_t)c->slots.size() - 1;
+  return TPT_OK;
+}
+
+tpt_status tpt_scene_release(tpt_context *c, int32_t slot) {
+  if (!c || slot < 0 || slot >= (int32_t)c->slots.size() || !c->slots[slot].live) return TPT_ERR_BAD_HANDLE;
+  cudaStreamSynchronize(c->stream);
+  cudaFree(c->slots[slot].arena);
+  c->slots[slot] = Slot{};
+  return TPT_OK;
+}
+
+tpt_status tpt_trace_closest(tpt_context *c, int32_t slot, const float *rays, int64_t n, uint64_t seed, float *hit_f,
+                             int32_t *hit_i, int32_t mem) {
+  if (!c || n < 0 || (n > 0 && (!rays || !hit_f || !hit_i))) return TPT_ERR_INVALID_ARGUMENT;
+  if (slot < 0 || slot >= (int32_t)c->slots.size() || !c->slots[slot].live) return TPT_ERR_BAD_HANDLE;
+  if (n == 0) return TPT_OK;
+  TPT_CUDA(cudaSetDevice(c->device));
+  const float *d_rays = rays;
+  float *d_f = hit_f;
+  int *d_i = hit_i;
+  if (mem == TPT_MEM_HOST) {
+    tpt_status st;
+    if ((st = ensure(c->rays, (size_t)n * 7 * sizeof(float))) != TPT_OK) return st;
+    if ((st = ensure(c->hitf, (size_t)n * 9 * sizeof(float))) != TPT_OK) return st;
+    if ((st = ensure(c->hiti, (size_t)n * 2 * sizeof(int))) != TPT_OK) return st;
+    TPT_CUDA(cudaMemcpyAsync(c->rays.p, rays, (size_t)n * 7 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    d_rays = (const float *)c->rays.p;
+    d_f = (float *)c->hitf.p;
+    d_i = (int *)c->hiti.p;
+  }
+  TPT_CUDA(cudaMemsetAsync(c->err, 0, sizeof(int), c->stream));
+  const int block = 128, smem = stack_smem(block);
+  int grid = grid_for(c, k_trace_closest, block, smem);
+  const long long need = (n + block - 1) / block;
+  if (grid > need) grid = (int)need;
+  k_trace_closest<<<grid, block, smem, c->stream>>>(c->slots[slot].ds, d_rays, n,
+                                                   make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)), d_f, d_i,
+                                                   c->err);
+  TPT_CUDA(cudaGetLastError());
+  int herr = 0;
+  TPT_CUDA(cudaMemcpyAsync(&herr, c->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  if (mem == TPT_MEM_HOST) {
+    TPT_CUDA(cudaMemcpyAsync(hit_f, d_f, (size_t)n * 9 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    TPT_CUDA(cudaMemcpyAsync(hit_i, d_i, (size_t)n * 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  }
+  TPT_CUDA(cudaStreamSynchronize(c->stream));
+  return herr ? (tpt_status)herr : TPT_OK;
+}
+
+void tpt_render_params_default(tpt_render_params *p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->width = 400;   // main.cpp:31-40 defaults
+  p->height = 200;
+  p->spp = 10;
+  p->max_depth = 50;
+  p->semantics = TPT_SEMANTICS_REFERENCE;
+  p->background = TPT_BACKGROUND_BLACK;
+  p->sky_scale = 1.0f;
+  p->seed = 1;
+}
+
+}  // extern "C"
+
+static PathBuf path_view(DevBuf &b, size_t wave) {
+  float4 *base = (float4 *)b.p;
+  return PathBuf{base, base + wave, base + 2 * wave, base + 3 * wave};
+}
+
+// Wavefront render; returns after all samples are accumulated.
+static tpt_status run_wavefront(tpt_context *c, const DevScene &S, const RenderCfg &cfg, const FrameDesc &F, int block,
+                                size_t wave, bool profile, tpt_render_stats *stats) {
+  tpt_status st;
+  if ((st = ensure(c->path[0], wave * 4 * sizeof(float4))) != TPT_OK) return st;
+  if ((st = ensure(c->path[1], wave * 4 * sizeof(float4))) != TPT_OK) return st;
+  if ((st = ensure(c->hits, wave * sizeof(int4))) != TPT_OK) return st;
+  PathBuf P[2] = {path_view(c->path[0], wave), path_view(c->path[1], wave)};
+  const unsigned first = (unsigned)std::min<unsigned long long>(wave, F.total);
+  WfCounters init{};
+  init.count[0] = first;
+  init.issued = first;
+  std::memcpy(c->counters_host, &init, sizeof(init));
+  TPT_CUDA(cudaMemcpyAsync(c->counters, c->counters_host, sizeof(WfCounters), cudaMemcpyHostToDevice, c->stream));
+  const int smem = stack_smem(block);
+  const int g_gen = std::max(1, std::min<int>((int)((first + block - 1) / block), c->sm_count * 8));
+  k_wf_generate<<<g_gen, block, 0, c->stream>>>(S, F, P[0], 0ull, first, cfg.key);
+  TPT_CUDA(cudaGetLastError());
+  int launches = 1;
+  const int g_tr = grid_for(c, k_wf_traverse, block, smem);
+  const int g_sh = grid_for(c, k_wf_shade, block, 0);
+  // iteration bound: every sample lives at most max_depth+1 segments
+  const unsigned long long max_iters = (F.total * (unsigned long long)(cfg.max_depth + 1)) / wave + 64;
+  // capture an even number of iterations (buffer parity returns) as a graph;
+  // with profiling, event-record nodes bracket every launch
+  const int kIters = 8;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  if (profile && !c->prof_ev[0]) {
+    for (auto &ev : c->prof_ev)
+      if (cudaEventCreate(&ev) != cudaSuccess) return TPT_ERR_CUDA;
+  }
+  TPT_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  for (int it = 0; it < kIters; it++) {
+    const int cur = it & 1;
+    if (profile) cudaEventRecordWithFlags(c->prof_ev[3 * it], c->stream, cudaEventRecordExternal);
+    k_wf_traverse<<<g_tr, block, smem, c->stream>>>(S, P[cur], cur, c->counters, (int4 *)c->hits.p, cfg.key);
+    if (profile) cudaEventRecordWithFlags(c->prof_ev[3 * it + 1], c->stream, cudaEventRecordExternal);
+    k_wf_shade<<<g_sh, block, 0, c->stream>>>(S, cfg, F, P[cur], P[cur ^ 1], cur, c->counters,
+                                              (const int4 *)c->hits.p);
+    if (profile) cudaEventRecordWithFlags(c->prof_ev[3 * it + 2], c->stream, cudaEventRecordExternal);
+  }
+  cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_status(e);
+  unsigned long long iters = 0;
+  tpt_status result = TPT_OK;
+  for (;;) {
+    e = cudaGraphLaunch(exec, c->stream);
+    if (e != cudaSuccess) { result = cuda_status(e); break; }
+    launches += 2 * kIters;
+    iters += kIters;
+    e = cudaMemcpyAsync(c->counters_host, c->counters, sizeof(WfCounters), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) { result = cuda_status(e); break; }
+    const WfCounters &h = *c->counters_host;
+    if (profile && stats) {
+      for (int it = 0; it < kIters; it++) {
+        float a = 0.f, b = 0.f;
+        cudaEventElapsedTime(&a, c->prof_ev[3 * it], c->prof_ev[3 * it + 1]);
+        cudaEventElapsedTime(&b, c->prof_ev[3 * it + 1], c->prof_ev[3 * it + 2]);
+        stats->traverse_ms += a;
+        stats->shade_ms += b;
+      }
+      stats->traverse_launches += kIters;
+      stats->shade_launches += kIters;
+    }
+    if (h.err) { result = h.err; break; }
+    if (h.count[0] == 0 && h.issued >= F.total) break;
+    if (iters > max_iters) { result = TPT_ERR_DEVICE_TIMEOUT; break; }
+  }
+  cudaGraphExecDestroy(exec);
+  if (stats) {
+    stats->iterations = (int32_t)iters;
+    stats->kernel_launches += launches;
+    stats->segments = (int64_t)c->counters_host->segments;
+  }
+  return result;
+}
+
+static tpt_status run_persistent(tpt_context *c, const DevScene &S, const RenderCfg &cfg, const FrameDesc &F, int block,
+                                 bool profile, tpt_render_stats *stats) {
+  WfCounters init{};
+  std::memcpy(c->counters_host, &init, sizeof(init));
+  TPT_CUDA(cudaMemcpyAsync(c->counters, c->counters_host, sizeof(WfCounters), cudaMemcpyHostToDevice, c->stream));
+  const int smem = stack_smem(block);
+  const int grid = grid_for(c, k_persistent, block, smem);
+  if (profile && !c->prof_ev[0]) {
+    for (auto &ev : c->prof_ev)
+      if (cudaEventCreate(&ev) != cudaSuccess) return TPT_ERR_CUDA;
+  }
+  if (profile) cudaEventRecord(c->prof_ev[0], c->stream);
+  k_persistent<<<grid, block, smem, c->stream>>>(S, cfg, F, c->counters);
+  TPT_CUDA(cudaGetLastError());
+  if (profile) cudaEventRecord(c->prof_ev[1], c->stream);
+  TPT_CUDA(cudaMemcpyAsync(c->counters_host, c->counters, sizeof(WfCounters), cudaMemcpyDeviceToHost, c->stream));
+  TPT_CUDA(cudaStreamSynchronize(c->stream));
+  if (stats) {
+    stats->iterations = 1;
+    stats->kernel_launches += 1;
+    stats->segments = (int64_t)c->counters_host->segments;
+    if (profile) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, c->prof_ev[0], c->prof_ev[1]);
+      stats->traverse_ms = ms;  // traversal and shading are fused in this engine
+      stats->traverse_launches = 1;
+    }
+  }
+  return c->counters_host->err ? (tpt_status)c->counters_host->err : TPT_OK;
+}
+
+extern "C" tpt_status tpt_render(tpt_context *c, int32_t slot, const tpt_render_params *p, float *out_rgb,
+                                 int32_t mem, tpt_render_stats *stats) {
+  if (!c || !p || !out_rgb) return TPT_ERR_INVALID_ARGUMENT;
+  if (slot < 0 || slot >= (int32_t)c->slots.size() || !c->slots[slot].live) return TPT_ERR_BAD_HANDLE;
+  if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->max_depth < 0) return TPT_ERR_INVALID_ARGUMENT;
+  const unsigned long long npix = (unsigned long long)p->width * p->height;
+  const unsigned long long total = npix * (unsigned long long)p->spp;
+  if (npix > 0x7fffffffull || (unsigned long long)p->spp > 0x7fffffffull) return TPT_ERR_INVALID_ARGUMENT;
+  TPT_CUDA(cudaSetDevice(c->device));
+  tpt_status st;
+  if ((st = ensure(c->accum, npix * sizeof(float4))) != TPT_OK) return st;
+  if (p->accumulate_fp64 && (st = ensure(c->accum64, npix * 3 * sizeof(double))) != TPT_OK) return st;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  FrameDesc F{p->width, p->height, p->spp, total, (float4 *)c->accum.p,
+              p->accumulate_fp64 ? (double *)c->accum64.p : nullptr};
+  RenderCfg cfg{p->max_depth, p->semantics, p->background, p->sky_scale,
+                make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32))};
+  const int block = p->block > 0 ? p->block : 128;
+  if (block % 32 || block > 1024) return TPT_ERR_INVALID_ARGUMENT;
+  size_t wave = p->wave > 0 ? (size_t)p->wave : (size_t)1 << 20;
+  if (wave > total) wave = (size_t)std::max<unsigned long long>(total, 32ull);
+  TPT_CUDA(cudaEventRecord(c->ev0, c->stream));
+  TPT_CUDA(cudaMemsetAsync(c->accum.p, 0, npix * sizeof(float4), c->stream));
+  if (F.accum64) TPT_CUDA(cudaMemsetAsync(c->accum64.p, 0, npix * 3 * sizeof(double), c->stream));
+  const DevScene &S = c->slots[slot].ds;
+  const int engine = p->engine == TPT_ENGINE_AUTO ? TPT_ENGINE_WAVEFRONT : p->engine;
+  if (engine == TPT_ENGINE_PERSISTENT)
+    st = run_persistent(c, S, cfg, F, block, p->profile != 0, stats);
+  else
+    st = run_wavefront(c, S, cfg, F, block, wave, p->profile != 0, stats);
+  if (st != TPT_OK) return st;
+  float *dst = out_rgb;
+  if (mem == TPT_MEM_HOST) {
+    if ((st = ensure(c->staging, npix * 3 * sizeof(float))) != TPT_OK) return st;
+    dst = (float *)c->staging.p;
+  }
+  const int rblock = 256;
+  const int rgrid = (int)std::min<unsigned long long>((npix + rblock - 1) / rblock, (unsigned long long)c->sm_count * 16);
+  k_resolve<<<rgrid, rblock, 0, c->stream>>>(F, dst);
+  TPT_CUDA(cudaGetLastError());
+  TPT_CUDA(cudaEventRecord(c->ev1, c->stream));
+  if (mem == TPT_MEM_HOST)
+    TPT_CUDA(cudaMemcpyAsync(out_rgb, dst, npix * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  TPT_CUDA(cudaStreamSynchronize(c->stream));
+  if (stats) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    stats->device_ms = ms;
+    stats->samples = (int64_t)total;
+    stats->kernel_launches += 1;
+  }
+  return TPT_OK;
+}

@@ -1,0 +1,264 @@
+"""Python binding of the tiny-path-tracer GB300 library (libtpt.so) over its
+C ABI (include/tpt.h), via ctypes.
+
+This is a thin host-side mirror of the reference's entry points: a scene is
+built from scene-description text (tpt.scenes generates the workloads), a
+Context owns a GPU, `trace_closest` is the batched `world->hit`, `render` the
+per-pixel sample loop with color().  There is no CPU fallback: loading raises
+if the compiled library is missing, and device calls raise TptError when no
+GPU is usable.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "_build", "libtpt.so")
+
+TPT_MEM_HOST = 0
+TPT_MEM_DEVICE = 1
+SEMANTICS_REFERENCE = 0
+SEMANTICS_PHYSICAL = 1
+BACKGROUND_BLACK = 0
+BACKGROUND_SKY = 1
+ENGINE_AUTO = 0
+ENGINE_WAVEFRONT = 1
+ENGINE_PERSISTENT = 2
+
+STATUS = {0: "TPT_OK", 1: "TPT_ERR_INVALID_ARGUMENT", 2: "TPT_ERR_PARSE", 3: "TPT_ERR_UNSUPPORTED",
+          4: "TPT_ERR_NO_BOUNDING_BOX", 5: "TPT_ERR_CUDA", 6: "TPT_ERR_OUT_OF_MEMORY",
+          7: "TPT_ERR_DEVICE_TIMEOUT", 8: "TPT_ERR_STACK_OVERFLOW", 9: "TPT_ERR_NO_DEVICE",
+          10: "TPT_ERR_BAD_HANDLE"}
+
+
+class TptError(RuntimeError):
+    def __init__(self, status: int, msg: str = ""):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}{': ' + msg if msg else ''}")
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("max_depth", C.c_int32),
+                ("semantics", C.c_int32), ("background", C.c_int32), ("sky_scale", C.c_float),
+                ("seed", C.c_uint64), ("engine", C.c_int32), ("block", C.c_int32), ("wave", C.c_int32),
+                ("accumulate_fp64", C.c_int32), ("profile", C.c_int32)]
+
+
+class RenderStats(C.Structure):
+    _fields_ = [("samples", C.c_int64), ("segments", C.c_int64), ("iterations", C.c_int32),
+                ("kernel_launches", C.c_int32), ("device_ms", C.c_double), ("traverse_ms", C.c_double),
+                ("shade_ms", C.c_double), ("traverse_launches", C.c_int32), ("shade_launches", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("n_nodes", "n_leaves", "n_items", "n_blas", "n_materials",
+                                         "n_textures", "n_lights", "max_stack")] + [("arena_bytes", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+# Every symbol include/tpt.h declares, with its ctypes signature.
+_SIGS = {
+    "tpt_status_string": (C.c_char_p, [C.c_int32]),
+    "tpt_version": (C.c_char_p, []),
+    "tpt_last_error": (C.c_char_p, []),
+    "tpt_builder_create": (C.c_int32, [C.c_void_p]),
+    "tpt_builder_destroy": (None, [C.c_void_p]),
+    "tpt_constant_texture": (C.c_int32, [C.c_void_p, C.c_float, C.c_float, C.c_float]),
+    "tpt_checker_texture": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32]),
+    "tpt_perlin_noise_texture": (C.c_int32, [C.c_void_p, C.c_float]),
+    "tpt_perlin_tables": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "tpt_image_texture": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32]),
+    "tpt_lambertian": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "tpt_metal": (C.c_int32, [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float]),
+    "tpt_dielectric": (C.c_int32, [C.c_void_p, C.c_float]),
+    "tpt_diffuse_light": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "tpt_isotropic": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "tpt_sphere": (C.c_int32, [C.c_void_p] + [C.c_float] * 4 + [C.c_int32]),
+    "tpt_moving_sphere": (C.c_int32, [C.c_void_p] + [C.c_float] * 9 + [C.c_int32]),
+    "tpt_xy_rect": (C.c_int32, [C.c_void_p] + [C.c_float] * 5 + [C.c_int32]),
+    "tpt_xz_rect": (C.c_int32, [C.c_void_p] + [C.c_float] * 5 + [C.c_int32]),
+    "tpt_yz_rect": (C.c_int32, [C.c_void_p] + [C.c_float] * 5 + [C.c_int32]),
+    "tpt_flip_normal": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "tpt_box": (C.c_int32, [C.c_void_p] + [C.c_float] * 6 + [C.c_int32]),
+    "tpt_translate": (C.c_int32, [C.c_void_p, C.c_int32, C.c_float, C.c_float, C.c_float]),
+    "tpt_rotate_y": (C.c_int32, [C.c_void_p, C.c_int32, C.c_float]),
+    "tpt_constant_medium": (C.c_int32, [C.c_void_p, C.c_int32, C.c_float, C.c_int32]),
+    "tpt_hitable_list": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32]),
+    "tpt_bvh_node": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.c_float]),
+    "tpt_builder_set_world": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "tpt_builder_set_light_shape": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "tpt_builder_set_camera": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p] + [C.c_float] * 6),
+    "tpt_scene_compile": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "tpt_scene_from_text": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_char_p, C.c_size_t]),
+    "tpt_scene_destroy": (None, [C.c_void_p]),
+    "tpt_scene_get_info": (C.c_int32, [C.c_void_p, C.POINTER(SceneInfo)]),
+    "tpt_scene_bvh_dump": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]),
+    "tpt_context_create": (C.c_int32, [C.c_int32, C.c_void_p]),
+    "tpt_context_destroy": (None, [C.c_void_p]),
+    "tpt_context_set_stream": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "tpt_scene_upload": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int32)]),
+    "tpt_scene_release": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "tpt_trace_closest": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_uint64, C.c_void_p,
+                                      C.c_void_p, C.c_int32]),
+    "tpt_render_params_default": (None, [C.POINTER(RenderParams)]),
+    "tpt_render": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.c_void_p, C.c_int32,
+                               C.POINTER(RenderStats)]),
+    "tpt_quantize": (None, [C.c_void_p, C.c_int64, C.c_void_p]),
+    "tpt_write_ppm": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int32, C.c_int32]),
+}
+
+_lib = None
+
+
+def lib():
+    """Loads libtpt.so; raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libtpt.so not built at {LIB_PATH}: run tiny-path-tracer_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(st: int, what: str = "") -> None:
+    if st != 0:
+        detail = lib().tpt_last_error().decode() if st == 5 else ""
+        raise TptError(st, what + (f" ({detail})" if detail else ""))
+
+
+def _ptr(a):
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data_as(C.c_void_p)
+    return C.c_void_p(int(a))  # raw device pointer
+
+
+class Scene:
+    """A compiled scene (host arena) built from scene-description text."""
+
+    def __init__(self, sd_text: str):
+        h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        st = lib().tpt_scene_from_text(sd_text.encode(), C.byref(h), err, 512)
+        if st != 0:
+            raise TptError(st, err.value.decode())
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self) -> dict:
+        i = SceneInfo()
+        check(lib().tpt_scene_get_info(self._h, C.byref(i)))
+        return i.as_dict()
+
+    def bvh_dump(self, user_id: int):
+        n = lib().tpt_scene_bvh_dump(self._h, user_id, None, None, 0)
+        if n < 0:
+            raise TptError(-n, f"bvh_dump({user_id})")
+        boxes = np.zeros((n, 6), np.float32)
+        kids = np.zeros((n, 2), np.int32)
+        lib().tpt_scene_bvh_dump(self._h, user_id, _ptr(boxes), _ptr(kids), n)
+        return boxes, kids
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.tpt_scene_destroy(self._h)
+            self._h = None
+
+
+class Context:
+    """One GPU: uploaded scenes, scratch buffers, a stream."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(lib().tpt_context_create(device, C.byref(h)), "context_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tpt_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        if _lib is not None:
+            self.close()
+
+    def set_stream(self, stream_ptr: int | None):
+        check(lib().tpt_context_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
+
+    def upload(self, scene: Scene) -> int:
+        slot = C.c_int32()
+        check(lib().tpt_scene_upload(self._h, scene.handle, C.byref(slot)), "scene_upload")
+        return slot.value
+
+    def release(self, slot: int) -> None:
+        check(lib().tpt_scene_release(self._h, slot))
+
+    def trace_closest(self, slot: int, rays: np.ndarray, seed: int = 0):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        f = np.zeros((n, 9), np.float32)
+        i = np.zeros((n, 2), np.int32)
+        check(lib().tpt_trace_closest(self._h, slot, _ptr(rays), n, seed, _ptr(f), _ptr(i), TPT_MEM_HOST),
+              "trace_closest")
+        return f, i
+
+    def trace_closest_device(self, slot: int, rays_ptr: int, n: int, seed: int, hit_f_ptr: int, hit_i_ptr: int):
+        check(lib().tpt_trace_closest(self._h, slot, C.c_void_p(rays_ptr), n, seed, C.c_void_p(hit_f_ptr),
+                                      C.c_void_p(hit_i_ptr), TPT_MEM_DEVICE), "trace_closest")
+
+    def render(self, slot: int, width: int, height: int, spp: int, max_depth: int = 50,
+               semantics: int = SEMANTICS_REFERENCE, background: int = BACKGROUND_BLACK, sky_scale: float = 1.0,
+               seed: int = 1, engine: int = ENGINE_AUTO, block: int = 0, wave: int = 0, fp64: bool = False,
+               profile: bool = False, out=None):
+        p = make_params(width, height, spp, max_depth, semantics, background, sky_scale, seed, engine, block,
+                        wave, fp64, profile)
+        st = RenderStats()
+        if out is None:
+            img = np.zeros((height, width, 3), np.float32)
+            check(lib().tpt_render(self._h, slot, C.byref(p), _ptr(img), TPT_MEM_HOST, C.byref(st)), "render")
+            return img, st.as_dict()
+        check(lib().tpt_render(self._h, slot, C.byref(p), C.c_void_p(int(out)), TPT_MEM_DEVICE, C.byref(st)),
+              "render")
+        return None, st.as_dict()
+
+
+def make_params(width, height, spp, max_depth=50, semantics=0, background=0, sky_scale=1.0, seed=1, engine=0,
+                block=0, wave=0, fp64=False, profile=False) -> RenderParams:
+    p = RenderParams()
+    lib().tpt_render_params_default(C.byref(p))
+    p.width, p.height, p.spp, p.max_depth = width, height, spp, max_depth
+    p.semantics, p.background, p.sky_scale, p.seed = semantics, background, sky_scale, seed
+    p.engine, p.block, p.wave, p.accumulate_fp64 = engine, block, wave, int(bool(fp64))
+    p.profile = int(bool(profile))
+    return p
+
+
+def quantize(mean_rgb: np.ndarray) -> np.ndarray:
+    m = np.ascontiguousarray(mean_rgb, np.float32)
+    out = np.zeros(m.shape, np.uint8)
+    lib().tpt_quantize(_ptr(m), m.size // 3, _ptr(out))
+    return out
+
+
+def write_ppm(path: str, rgb8: np.ndarray) -> None:
+    h, w, _ = rgb8.shape
+    check(lib().tpt_write_ppm(path.encode(), _ptr(np.ascontiguousarray(rgb8)), w, h), "write_ppm")
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGS)
