@@ -150,6 +150,14 @@ tpt_status tpt_context_set_stream(tpt_context *ctx, void *stream);
 tpt_status tpt_scene_upload(tpt_context *ctx, const tpt_scene *s, int32_t *slot);
 tpt_status tpt_scene_release(tpt_context *ctx, int32_t slot);
 
+/* Context options (tpt_context_set_option). */
+enum {
+  TPT_OPT_FLAT_NODES = 1  /* BVHs of at most this many nodes use the stackless walk
+                             (default 48); applies to tpt_trace_closest and to renders
+                             whose flat_nodes parameter is 0 */
+};
+tpt_status tpt_context_set_option(tpt_context *ctx, int32_t option, int64_t value);
+
 /* Memory location flags for caller buffers. */
 enum { TPT_MEM_HOST = 0, TPT_MEM_DEVICE = 1 };
 
@@ -166,6 +174,7 @@ tpt_status tpt_trace_closest(tpt_context *ctx, int32_t slot, const float *rays, 
  * integrator switches. */
 enum { TPT_SEMANTICS_REFERENCE = 0, TPT_SEMANTICS_PHYSICAL = 1 };
 enum { TPT_BACKGROUND_BLACK = 0, TPT_BACKGROUND_SKY = 1 };
+/* AUTO = PERSISTENT: measured fastest on the Cornell workload. */
 enum { TPT_ENGINE_AUTO = 0, TPT_ENGINE_WAVEFRONT = 1, TPT_ENGINE_PERSISTENT = 2 };
 typedef struct {
   int32_t width, height;    /* [DEFAULT] width, height */
@@ -176,10 +185,12 @@ typedef struct {
   float sky_scale;          /* sky gradient scale (utils.cc:87-90 uses 0.1) */
   uint64_t seed;            /* RNG key */
   int32_t engine;           /* TPT_ENGINE_* */
-  int32_t block;            /* threads per block, 0 = tuned */
-  int32_t wave;             /* wavefront path slots, 0 = tuned */
+  int32_t block;            /* threads per block, 0 = tuned (persistent engine: <= 128) */
+  int32_t wave;             /* wavefront: path slots (0 = 1M); persistent: register
+                               variant, minimum resident blocks 4 (default), 6 or 8 */
   int32_t accumulate_fp64;  /* 1: also accumulate in double (out_rgb is the FP64 mean) */
   int32_t profile;          /* 1: time each traverse/shade launch with CUDA events */
+  int32_t flat_nodes;       /* stackless-walk size limit; 0 = the context option */
 } tpt_render_params;
 
 typedef struct {

@@ -4,8 +4,9 @@ host scene compiler + C ABI), compiled in-tree into tiny-path-tracer_gb300/_buil
     python tiny-path-tracer_gb300/build.py
 
 The two translation units compile in parallel: kernels.cu with nvcc
-(-gencode arch=compute_103a,code=sm_103a, -fmad=false so hit arithmetic keeps
-the reference's rounding), scene.cc with g++ (-ffp-contract=off).
+(-gencode arch=compute_103a,code=sm_103a; hit arithmetic is written with
+unfused round-to-nearest intrinsics, so FMA contraction stays on for the
+rest), scene.cc with g++ (-ffp-contract=off).
 """
 from __future__ import annotations
 
@@ -51,7 +52,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cuda = _cuda_home(nvcc)
     k_obj = os.path.join(OUT, "kernels.o")
     s_obj = os.path.join(OUT, "scene.o")
-    nv = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-fmad=false", "-std=c++17",
+    nv = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
           "-Xcompiler", "-fPIC", "-c", os.path.join(CSRC, "kernels.cu"), "-o", k_obj]
     gx = ["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fPIC", "-Wall", f"-I{cuda}/include", "-c",
           os.path.join(CSRC, "scene.cc"), "-o", s_obj]

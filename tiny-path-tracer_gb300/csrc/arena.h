@@ -3,6 +3,8 @@
 //
 // HBM layout (one contiguous allocation per uploaded scene, 256-byte aligned
 // sections):
+//   node_skip[n]             pre-order index just past the node's subtree
+//                            (stackless walk: on a box miss jump there)
 //   node_lo[n], node_hi[n]   BVH2 nodes as two SoA float4 arrays:
 //                            {min.x,min.y,min.z,left}, {max.x,max.y,max.z,right}
 //                            (children stored as int bits; >= 0 internal node,
@@ -69,6 +71,7 @@ enum { TRAVERSAL_STACK = 32 };
 struct DevScene {
   const f4 *node_lo;
   const f4 *node_hi;
+  const int32_t *node_skip;
   const i4 *leaf_hdr;
   const int32_t *leaf_user;
   const f4 *leaf_data;
@@ -85,8 +88,12 @@ struct DevScene {
   int32_t n_nodes, n_leaves, n_items, n_mats, n_texs, n_lights;
   int32_t light_is_list;  // 0: single light_shape hitable; 1: hitable_list
   int32_t has_lights;
+  int32_t flat_max;  // BVH items of at most this many nodes use the stackless walk
   Camera cam;
 };
+
+// Default size limit of the stackless pre-order walk (tuned per render).
+enum { DEFAULT_FLAT_MAX = 48 };
 
 }  // namespace tpt
 #endif

@@ -3,11 +3,13 @@
 // finalisation, textures, materials, mixture-pdf light sampling and the
 // per-vertex shading step shared by the wavefront and persistent engines.
 //
-// Exactness: the file is compiled with -fmad=false so that no a*b+c is fused
-// behind our back; hit arithmetic follows the reference's float operation
-// order, and the sphere root - which the reference evaluates in double
-// (sphere.cc:23,32: unqualified sqrt on float promotes) - is reproduced with
-// a float-float evaluation instead of slow FP64.
+// Exactness: every operation of the hit path is an explicit round-to-nearest
+// intrinsic (x* helpers below), which the compiler never contracts into an
+// FMA, in the reference's float operation order; the sphere root - which the
+// reference evaluates in double (sphere.cc:23,32: unqualified sqrt on float
+// promotes) - is reproduced with a float-float evaluation instead of slow
+// FP64.  Shading, which is compared statistically, uses ordinary (fusable)
+// arithmetic and fast intrinsics.
 #ifndef TPT_DEVICE_CUH
 #define TPT_DEVICE_CUH
 
@@ -34,7 +36,7 @@ __device__ __forceinline__ float3 cross3(float3 a, float3 b) {
   return v3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
 }
 __device__ __forceinline__ float length3(float3 a) { return sqrtf(dot3(a, a)); }
-__device__ __forceinline__ float3 unit3(float3 a) { return a / length3(a); }
+__device__ __forceinline__ float3 unit3(float3 a) { return a * rsqrtf(dot3(a, a)); }  // shading only
 __device__ __forceinline__ float comp(float3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
 __device__ __forceinline__ float3 f3(const f4 &a) { return v3(a.x, a.y, a.z); }
 __device__ __forceinline__ f4 ldg4(const f4 *p) {
@@ -46,11 +48,36 @@ __device__ __forceinline__ i4 ldg4(const i4 *p) {
   return i4{q.x, q.y, q.z, q.w};
 }
 
+// Unfused IEEE round-to-nearest operations for the hit path.
+__device__ __forceinline__ float xm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float xa(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float xs(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float xd(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float3 xadd3(float3 a, float3 b) { return v3(xa(a.x, b.x), xa(a.y, b.y), xa(a.z, b.z)); }
+__device__ __forceinline__ float3 xsub3(float3 a, float3 b) { return v3(xs(a.x, b.x), xs(a.y, b.y), xs(a.z, b.z)); }
+__device__ __forceinline__ float3 xscl3(float3 a, float t) { return v3(xm(a.x, t), xm(a.y, t), xm(a.z, t)); }
+__device__ __forceinline__ float3 xdiv3(float3 a, float t) { return v3(xd(a.x, t), xd(a.y, t), xd(a.z, t)); }
+__device__ __forceinline__ float xdot3(float3 a, float3 b) {  // vec3.h:77-79 order
+  return xa(xa(xm(a.x, b.x), xm(a.y, b.y)), xm(a.z, b.z));
+}
+// n / d correctly rounded, given y = RN(1/d): q = RN(n*y) is within an ulp
+// and the FMA remainder step of Markstein (IBM J. R&D 34(1), 1990) rounds
+// it correctly.  Outside that theorem's range (d = 0 or tiny, overflow,
+// subnormal or zero quotients) the IEEE division is used.
+__device__ __forceinline__ float xdiv_rcp(float n, float d, float y) {
+  const float q = xm(n, y);
+  const float r = __fmaf_rn(-q, d, n);
+  const float q2 = __fmaf_rn(r, y, q);
+  const float a = fabsf(q2);
+  if (!(a <= 1.0e37f) || a < 1.0e-36f || !(fabsf(y) <= 1.0e36f)) return xd(n, d);
+  return q2;
+}
+
 struct Ray {
   float3 o, d;
   float time;
 };
-__device__ __forceinline__ float3 at(const Ray &r, float t) { return r.o + t * r.d; }  // ray.h:13
+__device__ __forceinline__ float3 at(const Ray &r, float t) { return xadd3(r.o, xscl3(r.d, t)); }  // ray.h:13
 
 // -------------------------------------------------------------- Philox ---
 // Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): counter-based, so every
@@ -103,7 +130,7 @@ struct RayPre {
 __device__ __forceinline__ RayPre precompute(const Ray &r) {
   RayPre p;
   p.o = r.o;
-  p.inv = v3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
+  p.inv = v3(__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z));  // == 1.0f / d, IEEE
   p.nx = p.inv.x < 0.0f;
   p.ny = p.inv.y < 0.0f;
   p.nz = p.inv.z < 0.0f;
@@ -129,12 +156,12 @@ __device__ __forceinline__ float prune_key(const RayPre &r, const f4 &lo, const 
 // so the final emptiness test equals the reference's early-exit result.
 __device__ __forceinline__ bool slab(const RayPre &r, const f4 &lo, const f4 &hi, float tmin, float tmax,
                                      float &entry) {
-  float n0 = ((r.nx ? hi.x : lo.x) - r.o.x) * r.inv.x;
-  float f0 = ((r.nx ? lo.x : hi.x) - r.o.x) * r.inv.x;
-  float n1 = ((r.ny ? hi.y : lo.y) - r.o.y) * r.inv.y;
-  float f1 = ((r.ny ? lo.y : hi.y) - r.o.y) * r.inv.y;
-  float n2 = ((r.nz ? hi.z : lo.z) - r.o.z) * r.inv.z;
-  float f2 = ((r.nz ? lo.z : hi.z) - r.o.z) * r.inv.z;
+  float n0 = xm(xs(r.nx ? hi.x : lo.x, r.o.x), r.inv.x);
+  float f0 = xm(xs(r.nx ? lo.x : hi.x, r.o.x), r.inv.x);
+  float n1 = xm(xs(r.ny ? hi.y : lo.y, r.o.y), r.inv.y);
+  float f1 = xm(xs(r.ny ? lo.y : hi.y, r.o.y), r.inv.y);
+  float n2 = xm(xs(r.nz ? hi.z : lo.z, r.o.z), r.inv.z);
+  float f2 = xm(xs(r.nz ? lo.z : hi.z, r.o.z), r.inv.z);
   tmin = fmaxf(fmaxf(fmaxf(n0, tmin), n1), n2);
   tmax = fminf(fminf(fminf(f0, tmax), f1), f2);
   entry = tmin;
@@ -151,7 +178,7 @@ __device__ __forceinline__ bool slab(const RayPre &r, const f4 &lo, const f4 &hi
 __device__ __forceinline__ float ref_root(float b, float disc, float a2, bool far_root) {
   float sh = __fsqrt_rn(disc);
   float e = __fmaf_rn(-sh, sh, disc);
-  float sl = __fdividef(e, 2.0f * sh);
+  float sl = __fdividef(e, xm(2.0f, sh));
   float x = -b;
   float y = far_root ? sh : -sh;
   float yl = far_root ? sl : -sl;
@@ -170,13 +197,13 @@ __device__ __forceinline__ float ref_root(float b, float disc, float a2, bool fa
 // sphere::hit candidate (sphere.cc:13-43): near root if it lies in
 // (tmin, tmax), else the far root.
 __device__ __forceinline__ bool sphere_t(float3 c, float radius, const Ray &r, float tmin, float tmax, float &t) {
-  float3 oc = r.o - c;
-  float a = dot3(r.d, r.d);
-  float b = 2.0f * dot3(r.d, oc);
-  float cc = dot3(oc, oc) - radius * radius;
-  float disc = b * b - 4.0f * a * cc;
+  float3 oc = xsub3(r.o, c);
+  float a = xdot3(r.d, r.d);
+  float b = xm(2.0f, xdot3(r.d, oc));
+  float cc = xs(xdot3(oc, oc), xm(radius, radius));
+  float disc = xs(xm(b, b), xm(xm(4.0f, a), cc));
   if (!(disc > 0.0f)) return false;
-  float a2 = 2.0f * a;
+  float a2 = xm(2.0f, a);
   float tn = ref_root(b, disc, a2, false);
   if (tn < tmax && tn > tmin) {
     t = tn;
@@ -192,43 +219,44 @@ __device__ __forceinline__ bool sphere_t(float3 c, float radius, const Ray &r, f
 
 __device__ __forceinline__ float3 msphere_center(const f4 &d0, const f4 &d1, const f4 &d2, float time) {
   // sphere.h:29-32
-  return f3(d0) + ((time - d1.w) / (d2.x - d1.w)) * (f3(d1) - f3(d0));
+  return xadd3(f3(d0), xscl3(xsub3(f3(d1), f3(d0)), xd(xs(time, d1.w), xs(d2.x, d1.w))));
 }
 
 // Axis-aligned rectangle (rect_box.cc:8-24,51-68,75-91): plane axis ax,
 // in-plane axes (ia, ib); closed interval [tmin, tmax].
 template <int AX>
-__device__ __forceinline__ bool rect_t(float a0, float a1, float b0, float b1, float k, const Ray &r, float tmin,
-                                       float tmax, float &t) {
+__device__ __forceinline__ bool rect_t(float a0, float a1, float b0, float b1, float k, const Ray &r, float y,
+                                       float tmin, float tmax, float &t) {
   constexpr int IA = AX == 0 ? 1 : 0;
   constexpr int IB = AX == 2 ? 1 : 2;
-  float tt = (k - comp(r.o, AX)) / comp(r.d, AX);
+  float tt = xdiv_rcp(xs(k, comp(r.o, AX)), comp(r.d, AX), y);
   if (tt > tmax || tt < tmin) return false;
-  float a = comp(r.o, IA) + tt * comp(r.d, IA);
-  float b = comp(r.o, IB) + tt * comp(r.d, IB);
+  float a = xa(comp(r.o, IA), xm(tt, comp(r.d, IA)));
+  float b = xa(comp(r.o, IB), xm(tt, comp(r.d, IB)));
   if (a < a0 || a > a1 || b < b0 || b > b1) return false;
   t = tt;
   return true;
 }
-__device__ __forceinline__ bool rect_any(int ax, float4 ab, float k, const Ray &r, float tmin, float tmax, float &t) {
-  if (ax == 0) return rect_t<0>(ab.x, ab.y, ab.z, ab.w, k, r, tmin, tmax, t);
-  if (ax == 1) return rect_t<1>(ab.x, ab.y, ab.z, ab.w, k, r, tmin, tmax, t);
-  return rect_t<2>(ab.x, ab.y, ab.z, ab.w, k, r, tmin, tmax, t);
+__device__ __forceinline__ bool rect_any(int ax, float4 ab, float k, const Ray &r, float3 inv, float tmin, float tmax,
+                                         float &t) {
+  if (ax == 0) return rect_t<0>(ab.x, ab.y, ab.z, ab.w, k, r, inv.x, tmin, tmax, t);
+  if (ax == 1) return rect_t<1>(ab.x, ab.y, ab.z, ab.w, k, r, inv.y, tmin, tmax, t);
+  return rect_t<2>(ab.x, ab.y, ab.z, ab.w, k, r, inv.z, tmin, tmax, t);
 }
 
 // box (rect_box.cc:93-119): a hitable_list of six faces, sequential with the
 // shrinking closest_so_far; a face is accepted when t <= closest, so a tie
 // goes to the later face.
-__device__ __forceinline__ bool box_t(float3 p0, float3 p1, const Ray &r, float tmin, float tmax, float &t,
-                                      int &face) {
+__device__ __forceinline__ bool box_t(float3 p0, float3 p1, const Ray &r, float3 inv, float tmin, float tmax,
+                                      float &t, int &face) {
   bool any = false;
   float closest = tmax, tt;
-  if (rect_t<2>(p0.x, p1.x, p0.y, p1.y, p1.z, r, tmin, closest, tt)) { closest = tt; face = 0; any = true; }
-  if (rect_t<2>(p0.x, p1.x, p0.y, p1.y, p0.z, r, tmin, closest, tt)) { closest = tt; face = 1; any = true; }
-  if (rect_t<1>(p0.x, p1.x, p0.z, p1.z, p1.y, r, tmin, closest, tt)) { closest = tt; face = 2; any = true; }
-  if (rect_t<1>(p0.x, p1.x, p0.z, p1.z, p0.y, r, tmin, closest, tt)) { closest = tt; face = 3; any = true; }
-  if (rect_t<0>(p0.y, p1.y, p0.z, p1.z, p1.x, r, tmin, closest, tt)) { closest = tt; face = 4; any = true; }
-  if (rect_t<0>(p0.y, p1.y, p0.z, p1.z, p0.x, r, tmin, closest, tt)) { closest = tt; face = 5; any = true; }
+  if (rect_t<2>(p0.x, p1.x, p0.y, p1.y, p1.z, r, inv.z, tmin, closest, tt)) { closest = tt; face = 0; any = true; }
+  if (rect_t<2>(p0.x, p1.x, p0.y, p1.y, p0.z, r, inv.z, tmin, closest, tt)) { closest = tt; face = 1; any = true; }
+  if (rect_t<1>(p0.x, p1.x, p0.z, p1.z, p1.y, r, inv.y, tmin, closest, tt)) { closest = tt; face = 2; any = true; }
+  if (rect_t<1>(p0.x, p1.x, p0.z, p1.z, p0.y, r, inv.y, tmin, closest, tt)) { closest = tt; face = 3; any = true; }
+  if (rect_t<0>(p0.y, p1.y, p0.z, p1.z, p1.x, r, inv.x, tmin, closest, tt)) { closest = tt; face = 4; any = true; }
+  if (rect_t<0>(p0.y, p1.y, p0.z, p1.z, p0.x, r, inv.x, tmin, closest, tt)) { closest = tt; face = 5; any = true; }
   t = closest;
   return any;
 }
@@ -239,12 +267,12 @@ __device__ __forceinline__ Ray to_object(const f4 *data, int nops, Ray r) {
   for (int i = 0; i < nops; i++) {
     f4 op = ldg4(data + 1 + i);
     if (op.x == (float)OP_TRANSLATE) {
-      r.o = r.o - v3(op.y, op.z, op.w);
+      r.o = xsub3(r.o, v3(op.y, op.z, op.w));
     } else {
       float sn = op.y, cs = op.z;
       float3 o = r.o, d = r.d;
-      r.o = v3(cs * o.x - sn * o.z, o.y, sn * o.x + cs * o.z);
-      r.d = v3(cs * d.x - sn * d.z, d.y, sn * d.x + cs * d.z);
+      r.o = v3(xs(xm(cs, o.x), xm(sn, o.z)), o.y, xa(xm(sn, o.x), xm(cs, o.z)));
+      r.d = v3(xs(xm(cs, d.x), xm(sn, d.z)), d.y, xa(xm(sn, d.x), xm(cs, d.z)));
     }
   }
   return r;
@@ -254,19 +282,19 @@ __device__ __forceinline__ void to_world(const f4 *data, int nops, float3 &p, fl
   for (int i = nops - 1; i >= 0; i--) {
     f4 op = ldg4(data + 1 + i);
     if (op.x == (float)OP_TRANSLATE) {
-      p = p + v3(op.y, op.z, op.w);
+      p = xadd3(p, v3(op.y, op.z, op.w));
     } else {
       float sn = op.y, cs = op.z;
-      p = v3(cs * p.x + sn * p.z, p.y, -sn * p.x + cs * p.z);
-      n = v3(cs * n.x + sn * n.z, n.y, -sn * n.x + cs * n.z);
+      p = v3(xa(xm(cs, p.x), xm(sn, p.z)), p.y, xa(xm(-sn, p.x), xm(cs, p.z)));
+      n = v3(xa(xm(cs, n.x), xm(sn, n.z)), n.y, xa(xm(-sn, n.x), xm(cs, n.z)));
     }
   }
 }
 
 // Candidate of a geometric primitive leaf (sphere, moving sphere, rect,
 // box).  face: box face or -1.
-__device__ __forceinline__ bool prim_t(const DevScene &S, const i4 &h, const Ray &r, float tmin, float tmax, float &t,
-                                       int &face) {
+__device__ __forceinline__ bool prim_t(const DevScene &S, const i4 &h, const Ray &r, float3 inv, float tmin,
+                                       float tmax, float &t, int &face) {
   const f4 *d = S.leaf_data + h.y;
   int type = h.x & LEAF_TYPE_MASK;
   face = -1;
@@ -276,11 +304,11 @@ __device__ __forceinline__ bool prim_t(const DevScene &S, const i4 &h, const Ray
   }
   if (type == LT_RECT) {
     f4 ab = ldg4(d), k = ldg4(d + 1);
-    return rect_any((h.x >> LEAF_AXIS_SHIFT) & 3, make_float4(ab.x, ab.y, ab.z, ab.w), k.x, r, tmin, tmax, t);
+    return rect_any((h.x >> LEAF_AXIS_SHIFT) & 3, make_float4(ab.x, ab.y, ab.z, ab.w), k.x, r, inv, tmin, tmax, t);
   }
   if (type == LT_BOX) {
     f4 p0 = ldg4(d), p1 = ldg4(d + 1);
-    return box_t(f3(p0), f3(p1), r, tmin, tmax, t, face);
+    return box_t(f3(p0), f3(p1), r, inv, tmin, tmax, t, face);
   }
   if (type == LT_MSPHERE) {
     f4 d0 = ldg4(d), d1 = ldg4(d + 1), d2 = ldg4(d + 2);
@@ -290,16 +318,18 @@ __device__ __forceinline__ bool prim_t(const DevScene &S, const i4 &h, const Ray
 }
 
 // A primitive or a transformed primitive (medium boundaries).
-__device__ __forceinline__ bool simple_t(const DevScene &S, int leaf, const Ray &r, float tmin, float tmax, float &t) {
+__device__ __forceinline__ float3 recip3(float3 d) { return v3(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z)); }
+
+__device__ __noinline__ bool simple_t(const DevScene &S, int leaf, const Ray &r, float tmin, float tmax, float &t) {
   i4 h = ldg4(S.leaf_hdr + leaf);
   int face;
   if ((h.x & LEAF_TYPE_MASK) == LT_INSTANCE) {
     const f4 *d = S.leaf_data + h.y;
     Ray o = to_object(d, (int)ldg4(d).x, r);
     i4 ch = ldg4(S.leaf_hdr + ~h.w);
-    return prim_t(S, ch, o, tmin, tmax, t, face);
+    return prim_t(S, ch, o, recip3(o.d), tmin, tmax, t, face);
   }
-  return prim_t(S, h, r, tmin, tmax, t, face);
+  return prim_t(S, h, r, recip3(r.d), tmin, tmax, t, face);
 }
 
 // constant_medium::hit (hitable.cc:98-128) with the free-flight uniform u.
@@ -311,12 +341,12 @@ __device__ __forceinline__ bool medium_t(const DevScene &S, const i4 &h, const R
   if (t1 < tmin) t1 = tmin;
   if (t2 > tmax) t2 = tmax;
   if (t1 >= t2) return false;
-  float dl = length3(r.d);
-  float inside = (t2 - t1) * dl;
+  float dl = __fsqrt_rn(xdot3(r.d, r.d));
+  float inside = xm(xs(t2, t1), dl);
   float density = ldg4(S.leaf_data + h.y).x;
-  float dist = (-1.0f / density) * logf(u);
+  float dist = xm(xd(-1.0f, density), logf(u));
   if (dist < inside) {
-    t = t1 + dist / dl;
+    t = xa(t1, xd(dist, dl));
     return true;
   }
   return false;
@@ -336,25 +366,30 @@ __device__ __forceinline__ bool beats(float t, int outer, int inner, float bt, i
   return t < bt || (t == bt && (outer > bouter || (outer == bouter && inner > binner)));
 }
 
-// Stack entries: node >= 0 (box already passed), STK_RESTORE (leave object
-// space), or -2 - leaf (enter an instanced BVH: switch to its object-space
-// ray when popped).
+// Stack entries {what, prune key}: what >= 0 an internal node whose box
+// passed; STK_RESTORE leave object space; what <= -2 the leaf -2-what (an
+// instanced BVH is entered when its leaf is popped).  Leaves go through the
+// stack too, so the primitive tests have a single call site.
 enum { STK_RESTORE = -1 };
 
 // Closest hit of the world for ray wr over [tmin, FLT_MAX] with the exact
 // semantics of hitable_list::hit across the top-level items (sequential,
 // shrinking t_max) and bvh_node::hit within an item (every child tested with
-// the same interval, ties to the right).  Within an item the search runs
-// near-first with pruning, which cannot change the result: the winner is the
-// minimum of (t, -leaf order), and a subtree is skipped only when the lower
-// bound prune_key() on any t its primitives can report exceeds the best t.
-// stk: this thread's stack slots, `stride` entries apart (shared memory).
-// err receives TPT_ERR_STACK_OVERFLOW if the stack would overflow.
+// the same interval, ties to the right).  The candidate set is the
+// reference's: a leaf is tested iff every ancestor box passes.  Small BVHs
+// are walked stacklessly in pre-order (a box miss jumps to the node's skip
+// index), which keeps a warp's lanes on the same node sequence; large ones
+// near-first with a shared-memory stack and pruning, which cannot change the
+// result: the winner is the minimum of (t, -leaf order), and a subtree is
+// skipped only when the lower bound prune_key() on any t its primitives can
+// report exceeds the best t.  stk: this thread's stack slots, `stride`
+// entries apart.  err receives TPT_ERR_STACK_OVERFLOW on overflow.
 __device__ bool trace_closest(const DevScene &S, const Ray &wr, float tmin, int2 *stk, int stride,
                               const MediumRng &mrng, HitRef &res, int &err) {
   const RayPre W = precompute(wr);
   float closest = 3.402823466e38f;  // std::numeric_limits<float>::max()
   bool found = false;
+  const int never_pruned = __float_as_int(-CUDART_INF_F);
   for (int it = 0; it < S.n_items; it++) {
     const int2 item = *reinterpret_cast<const int2 *>(S.items + it);
     const float tmax = closest;
@@ -366,115 +401,124 @@ __device__ bool trace_closest(const DevScene &S, const Ray &wr, float tmin, int2
     RayPre curp = W;
     int cur_inst = -1;
 
-    auto visit_leaf = [&](int leaf) {
-      const i4 h = ldg4(S.leaf_hdr + leaf);
-      const int type = h.x & LEAF_TYPE_MASK;
-      float t;
-      int face = -1;
-      if (type == LT_INSTANCE) {
-        const f4 *d = S.leaf_data + h.y;
-        const Ray o = to_object(d, (int)ldg4(d).x, cur);
-        if (h.w < 0) {  // one transformed primitive
-          const int cl = ~h.w;
-          if (prim_t(S, ldg4(S.leaf_hdr + cl), o, tmin, tmax, t, face) && beats(t, leaf, cl, bt, bo, bn)) {
-            bt = t; bl = cl; bi = leaf; bf = face; bo = leaf; bn = cl;
-          }
-        } else {  // instanced BVH: test its root box in object space
-          float en;
-          const RayPre op = precompute(o);
-          const f4 rlo = ldg4(S.node_lo + h.w), rhi = ldg4(S.node_hi + h.w);
-          if (slab(op, rlo, rhi, tmin, tmax, en)) {
-            if (sp >= TRAVERSAL_STACK) {
-              overflow = true;
-            } else {
-              stk[sp * stride] = make_int2(-2 - leaf, __float_as_int(prune_key(op, rlo, rhi, en)));
-              sp++;
+    auto push = [&](int what, int key) {
+      if (sp >= TRAVERSAL_STACK) {
+        overflow = true;
+      } else {
+        stk[sp * stride] = make_int2(what, key);
+        sp++;
+      }
+    };
+
+    auto run_stack = [&]() {
+      while (sp > 0 && !overflow) {
+        --sp;
+        const int2 e = stk[sp * stride];
+        if (e.x == STK_RESTORE) {
+          cur = wr;
+          curp = W;
+          cur_inst = -1;
+          continue;
+        }
+        if (__int_as_float(e.y) > bt) continue;
+        if (e.x <= -2) {  // a leaf
+          const int leaf = -2 - e.x;
+          const i4 h = ldg4(S.leaf_hdr + leaf);
+          const int type = h.x & LEAF_TYPE_MASK;
+          float t;
+          int face = -1;
+          if (type == LT_INSTANCE) {
+            const f4 *d = S.leaf_data + h.y;
+            const Ray o = to_object(d, (int)ldg4(d).x, wr);
+            const RayPre op = precompute(o);
+            if (h.w < 0) {  // one transformed primitive
+              const int cl = ~h.w;
+              if (prim_t(S, ldg4(S.leaf_hdr + cl), o, op.inv, tmin, tmax, t, face) && beats(t, leaf, cl, bt, bo, bn)) {
+                bt = t; bl = cl; bi = leaf; bf = face; bo = leaf; bn = cl;
+              }
+            } else {  // instanced BVH: enter object space if its root box passes
+              float en;
+              const f4 rlo = ldg4(S.node_lo + h.w), rhi = ldg4(S.node_hi + h.w);
+              if (slab(op, rlo, rhi, tmin, tmax, en)) {
+                push(STK_RESTORE, 0);
+                push(h.w, __float_as_int(prune_key(op, rlo, rhi, en)));
+                cur = o;
+                curp = op;
+                cur_inst = leaf;
+              }
             }
+            continue;
+          }
+          const int outer = cur_inst >= 0 ? cur_inst : leaf;
+          const int inner = cur_inst >= 0 ? leaf : -1;
+          bool ok;
+          if (type == LT_MEDIUM)
+            ok = medium_t(S, h, cur, tmin, tmax, medium_u(mrng, S.leaf_user[leaf]), t);
+          else
+            ok = prim_t(S, h, cur, curp.inv, tmin, tmax, t, face);
+          if (ok && beats(t, outer, inner, bt, bo, bn)) {
+            bt = t; bl = leaf; bi = cur_inst; bf = face; bo = outer; bn = inner;
+          }
+          continue;
+        }
+        // internal node: test the child boxes, push near child last
+        const f4 lo = ldg4(S.node_lo + e.x), hi = ldg4(S.node_hi + e.x);
+        const int left = __float_as_int(lo.w), right = __float_as_int(hi.w);
+        int2 q[2];
+        float ent[2];
+        int nq = 0;
+        for (int c = 0; c < 2; c++) {
+          const int ref = c == 0 ? left : right;
+          if (c == 1 && right == left) break;  // n == 1 node: left_ == right_
+          if (ref >= 0) {
+            float en;
+            const f4 clo = ldg4(S.node_lo + ref), chi = ldg4(S.node_hi + ref);
+            if (slab(curp, clo, chi, tmin, tmax, en)) {
+              ent[nq] = en;
+              q[nq++] = make_int2(ref, __float_as_int(prune_key(curp, clo, chi, en)));
+            }
+          } else {
+            push(-2 - ~ref, never_pruned);
           }
         }
-        return;
-      }
-      const int outer = cur_inst >= 0 ? cur_inst : leaf;
-      const int inner = cur_inst >= 0 ? leaf : -1;
-      bool ok;
-      if (type == LT_MEDIUM)
-        ok = medium_t(S, h, cur, tmin, tmax, medium_u(mrng, S.leaf_user[leaf]), t);
-      else
-        ok = prim_t(S, h, cur, tmin, tmax, t, face);
-      if (ok && beats(t, outer, inner, bt, bo, bn)) {
-        bt = t; bl = leaf; bi = cur_inst; bf = face; bo = outer; bn = inner;
+        if (nq == 2 && ent[1] > ent[0]) {
+          const int2 tq = q[0];
+          q[0] = q[1];
+          q[1] = tq;
+        }
+        for (int k = 0; k < nq; k++) push(q[k].x, q[k].y);
+        // leaves pushed above go after the near child; order does not matter
       }
     };
 
     if (item.x == ITEM_BVH) {
-      float en;
-      if (slab(W, ldg4(S.node_lo + item.y), ldg4(S.node_hi + item.y), tmin, tmax, en)) {
-        stk[0] = make_int2(item.y, __float_as_int(en));
-        sp = 1;
+      const int root = item.y;
+      const int end = __ldg(S.node_skip + root);
+      if (end - root <= S.flat_max) {
+        for (int i = root; i < end && !overflow;) {
+          const f4 lo = ldg4(S.node_lo + i), hi = ldg4(S.node_hi + i);
+          float en;
+          if (slab(W, lo, hi, tmin, tmax, en)) {
+            const int left = __float_as_int(lo.w), right = __float_as_int(hi.w);
+            if (right < 0) push(-2 - ~right, never_pruned);
+            if (left < 0 && left != right) push(-2 - ~left, never_pruned);
+            if (sp > 0) run_stack();
+            i++;
+          } else {
+            i = __ldg(S.node_skip + i);
+          }
+        }
+      } else {
+        float en;
+        const f4 lo = ldg4(S.node_lo + root), hi = ldg4(S.node_hi + root);
+        if (slab(W, lo, hi, tmin, tmax, en)) {
+          push(root, never_pruned);
+          run_stack();
+        }
       }
     } else {
-      visit_leaf(item.y);
-    }
-
-    while (sp > 0 && !overflow) {
-      --sp;
-      const int2 e = stk[sp * stride];
-      if (e.x == STK_RESTORE) {
-        cur = wr;
-        curp = W;
-        cur_inst = -1;
-        continue;
-      }
-      if (__int_as_float(e.y) > bt) continue;
-      if (e.x <= -2) {  // enter an instanced BVH
-        const int leaf = -2 - e.x;
-        const i4 h = ldg4(S.leaf_hdr + leaf);
-        const f4 *d = S.leaf_data + h.y;
-        cur = to_object(d, (int)ldg4(d).x, wr);
-        curp = precompute(cur);
-        cur_inst = leaf;
-        if (sp + 2 > TRAVERSAL_STACK) {
-          overflow = true;
-          break;
-        }
-        stk[sp * stride] = make_int2(STK_RESTORE, 0);
-        stk[(sp + 1) * stride] = make_int2(h.w, e.y);
-        sp += 2;
-        continue;
-      }
-      const f4 lo = ldg4(S.node_lo + e.x), hi = ldg4(S.node_hi + e.x);
-      const int left = __float_as_int(lo.w), right = __float_as_int(hi.w);
-      int2 push[2];
-      float ent[2];
-      int npush = 0;
-#pragma unroll
-      for (int c = 0; c < 2; c++) {
-        const int ref = c == 0 ? left : right;
-        if (c == 1 && right == left) break;  // n == 1 node: left_ == right_
-        if (ref >= 0) {
-          float en;
-          const f4 clo = ldg4(S.node_lo + ref), chi = ldg4(S.node_hi + ref);
-          if (slab(curp, clo, chi, tmin, tmax, en)) {
-            ent[npush] = en;
-            push[npush++] = make_int2(ref, __float_as_int(prune_key(curp, clo, chi, en)));
-          }
-        } else {
-          visit_leaf(~ref);
-        }
-      }
-      if (sp + npush > TRAVERSAL_STACK) {
-        overflow = true;
-        break;
-      }
-      if (npush == 2) {  // far child below, near child on top
-        const bool swap = ent[1] > ent[0];
-        stk[sp * stride] = swap ? push[1] : push[0];
-        stk[(sp + 1) * stride] = swap ? push[0] : push[1];
-        sp += 2;
-      } else if (npush == 1) {
-        stk[sp * stride] = push[0];
-        sp++;
-      }
+      push(-2 - item.y, never_pruned);
+      run_stack();
     }
     if (overflow) err = TPT_ERR_STACK_OVERFLOW;
     if (bl >= 0) {
@@ -525,8 +569,8 @@ __device__ void finalize(const DevScene &S, const Ray &wr, const HitRef &h, Surf
     float3 c0 = f3(d0), c = c0;
     if (type == LT_MSPHERE) c = msphere_center(d0, ldg4(d + 1), ldg4(d + 2), r.time);
     s.p = at(r, t);
-    uv_map((s.p - c0) / d0.w, s.u, s.v);
-    s.n = (s.p - c) / d0.w;
+    uv_map(xdiv3(xsub3(s.p, c0), d0.w), s.u, s.v);
+    s.n = xdiv3(xsub3(s.p, c), d0.w);
   } else if (type == LT_RECT || type == LT_BOX) {
     int ax;
     float a0, a1, b0, b1;
@@ -546,10 +590,10 @@ __device__ void finalize(const DevScene &S, const Ray &wr, const HitRef &h, Surf
       b1 = ax == 2 ? p1.y : p1.z;
     }
     const int ia = ax == 0 ? 1 : 0, ib = ax == 2 ? 1 : 2;
-    const float a = comp(r.o, ia) + t * comp(r.d, ia);
-    const float b = comp(r.o, ib) + t * comp(r.d, ib);
-    s.u = (a - a0) / (a1 - a0);
-    s.v = (b - b0) / (b1 - b0);
+    const float a = xa(comp(r.o, ia), xm(t, comp(r.d, ia)));
+    const float b = xa(comp(r.o, ib), xm(t, comp(r.d, ib)));
+    s.u = xd(xs(a, a0), xs(a1, a0));
+    s.v = xd(xs(b, b0), xs(b1, b0));
     s.p = at(r, t);
     s.n = v3(ax == 0 ? 1.f : 0.f, ax == 1 ? 1.f : 0.f, ax == 2 ? 1.f : 0.f);
     if (fflip) s.n = -s.n;
@@ -667,7 +711,7 @@ __device__ float light_item_pdf(const DevScene &S, int i, float3 o, float3 d) {
   float t;
   if (li.x == LS_XZ_RECT) {
     const float k = ldg4(S.light_f + 2 * i + 1).x;
-    if (!rect_t<1>(a.x, a.y, a.z, a.w, k, r, 0.0001f, 3.402823466e38f, t)) return 0.f;
+    if (!rect_t<1>(a.x, a.y, a.z, a.w, k, r, __frcp_rn(d.y), 0.0001f, 3.402823466e38f, t)) return 0.f;
     const float area = fabsf((a.y - a.x) * (a.w - a.z));
     const float3 td = t * d;
     const float d2 = dot3(td, td);
@@ -853,7 +897,7 @@ __device__ bool shade_vertex(const DevScene &S, const RenderCfg &cfg, Ray &ray, 
       }
       const float cs = dot3(sf.n, unit3(dir));
       const float spdf = cs < 0.f ? 0.f : cs * 0.318309886183790671538f;
-      wgt = atten * (spdf / pdf);
+      wgt = atten * __fdividef(spdf, pdf);
       break;
     }
     default:  // diffuse_light and the base material: no scatter

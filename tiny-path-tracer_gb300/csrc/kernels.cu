@@ -232,33 +232,54 @@ __global__ void k_wf_shade(DevScene S, RenderCfg cfg, FrameDesc F, PathBuf in, P
   }
 }
 
-// Persistent engine: warps claim camera samples until all are issued and
-// trace each path to termination.
-__global__ void k_persistent(DevScene S, RenderCfg cfg, FrameDesc F, WfCounters *C) {
+// Persistent engine: every lane carries one path in registers; when its
+// path ends it accumulates and claims the next camera sample (one atomic per
+// warp for all lanes that need one), so lanes do not idle behind the longest
+// path of their warp.
+template <int MIN_BLOCKS>
+__global__ void __launch_bounds__(128, MIN_BLOCKS) k_persistent(DevScene S, RenderCfg cfg, FrameDesc F, WfCounters *C) {
   extern __shared__ int2 stack_smem[];
   int2 *stk = stack_smem + threadIdx.x;
   int e = 0;
   unsigned long long segs = 0;
+  bool alive = false, done = false;
+  Ray r{};
+  float3 T = v3(0.f, 0.f, 0.f), L = v3(0.f, 0.f, 0.f);
+  uint32_t pixel = 0, sample = 0;
+  int depth = 0;
   for (;;) {
-    unsigned long long base;
-    int rank;
-    warp_claim(true, &C->issued, base, rank);
-    const unsigned long long s = base + (unsigned long long)rank;
-    if (base >= F.total) break;  // warp-uniform
-    if (s < F.total) {
-      uint32_t pixel, sample;
-      int i, j;
-      sample_coords(F, s, pixel, sample, i, j);
-      Ray r = camera_ray(S.cam, i, j, F.nx, F.ny, pixel, sample, cfg.key);
-      float3 T = v3(1.f, 1.f, 1.f), L = v3(0.f, 0.f, 0.f);
-      for (int depth = 0;; depth++) {
-        MediumRng m{make_uint4(pixel, sample, (uint32_t)depth, 0u), cfg.key, 1};
-        HitRef h;
-        const bool hit = trace_closest(S, r, 0.001f, stk, blockDim.x, m, h, e);
-        segs++;
-        if (!shade_vertex(S, cfg, r, hit, h, T, L, depth, pixel, sample)) break;
+    const bool want = !alive && !done;
+    if (__any_sync(0xffffffffu, want)) {
+      unsigned long long base;
+      int rank;
+      warp_claim(want, &C->issued, base, rank);
+      if (want) {
+        const unsigned long long s = base + (unsigned long long)rank;
+        if (s < F.total) {
+          int i, j;
+          sample_coords(F, s, pixel, sample, i, j);
+          r = camera_ray(S.cam, i, j, F.nx, F.ny, pixel, sample, cfg.key);
+          T = v3(1.f, 1.f, 1.f);
+          L = v3(0.f, 0.f, 0.f);
+          depth = 0;
+          alive = true;
+        } else {
+          done = true;
+        }
       }
-      accumulate(F, pixel, L);
+    }
+    if (__all_sync(0xffffffffu, done)) break;
+    if (alive) {
+      MediumRng m{make_uint4(pixel, sample, (uint32_t)depth, 0u), cfg.key, 1};
+      HitRef h;
+      const bool hit = trace_closest(S, r, 0.001f, stk, blockDim.x, m, h, e);
+      segs++;
+      if (shade_vertex(S, cfg, r, hit, h, T, L, depth, pixel, sample)) {
+        depth++;
+      } else {
+        accumulate(F, pixel, L);
+        alive = false;
+      }
     }
   }
   if (segs) atomicAdd(&C->segments, segs);
@@ -317,9 +338,7 @@ struct tpt_context {
   int *err = nullptr;                   // device error flag for trace
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t prof_ev[24] = {};  // per-launch timing of one graph (8 iterations x 3)
-  // cached wavefront graph
-  cudaGraphExec_t graph = nullptr;
-  size_t graph_key = 0;
+  int flat_nodes = DEFAULT_FLAT_MAX;
 };
 
 static thread_local char g_last_error[256] = "";
@@ -348,6 +367,13 @@ static tpt_status ensure(DevBuf &b, size_t bytes) {
 }
 
 static int stack_smem(int block) { return block * TRAVERSAL_STACK * (int)sizeof(int2); }
+
+// Dynamic shared memory above 48 KB needs the per-kernel opt-in.
+template <class K>
+static cudaError_t smem_optin(K kernel, int smem) {
+  if (smem <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
 
 template <class K>
 static int grid_for(const tpt_context *ctx, K kernel, int block, int smem) {
@@ -396,7 +422,6 @@ void tpt_context_destroy(tpt_context *c) {
                     &c->staging, &c->rays, &c->hitf, &c->hiti};
   for (DevBuf *b : bufs)
     if (b->p) cudaFree(b->p);
-  if (c->graph) cudaGraphExecDestroy(c->graph);
   if (c->counters) cudaFree(c->counters);
   if (c->counters_host) cudaFreeHost(c->counters_host);
   if (c->err) cudaFree(c->err);
@@ -411,11 +436,17 @@ void tpt_context_destroy(tpt_context *c) {
 tpt_status tpt_context_set_stream(tpt_context *c, void *stream) {
   if (!c) return TPT_ERR_INVALID_ARGUMENT;
   c->stream = stream ? (cudaStream_t)stream : c->own;
-  if (c->graph) {
-    cudaGraphExecDestroy(c->graph);
-    c->graph = nullptr;
-  }
   return TPT_OK;
+}
+
+tpt_status tpt_context_set_option(tpt_context *c, int32_t option, int64_t value) {
+  if (!c) return TPT_ERR_INVALID_ARGUMENT;
+  if (option == TPT_OPT_FLAT_NODES) {
+    if (value < 0 || value > (1ll << 30)) return TPT_ERR_INVALID_ARGUMENT;
+    c->flat_nodes = (int)value;
+    return TPT_OK;
+  }
+  return TPT_ERR_INVALID_ARGUMENT;
 }
 
 tpt_status tpt_scene_upload(tpt_context *c, const tpt_scene *sc, int32_t *slot) {
@@ -424,20 +455,10 @@ tpt_status tpt_scene_upload(tpt_context *c, const tpt_scene *sc, int32_t *slot) 
   TPT_CUDA(cudaSetDevice(c->device));
   const ArenaLayout L = arena_layout(S);
   std::vector<uint8_t> host(L.total, 0);
-  const void *src[15] = {S.node_lo.data(),   S.node_hi.data(), S.leaf_hdr.data(), S.leaf_user.data(),
-                         S.leaf_data.data(), S.items.data(),   S.mat_i.data(),    S.mat_f.data(),
-                         S.tex_i.data(),     S.tex_f.data(),   S.images.data(),   S.perlin_grad.data(),
-                         S.perlin_perm.data(), S.light_i.data(), S.light_f.data()};
-  const size_t len[15] = {S.node_lo.size() * sizeof(f4),   S.node_hi.size() * sizeof(f4),
-                          S.leaf_hdr.size() * sizeof(i4),  S.leaf_user.size() * sizeof(int32_t),
-                          S.leaf_data.size() * sizeof(f4), S.items.size() * sizeof(i2),
-                          S.mat_i.size() * sizeof(i4),     S.mat_f.size() * sizeof(f4),
-                          S.tex_i.size() * sizeof(i4),     S.tex_f.size() * sizeof(f4),
-                          S.images.size(),                 S.perlin_grad.size() * sizeof(f4),
-                          S.perlin_perm.size() * sizeof(int32_t), S.light_i.size() * sizeof(i4),
-                          S.light_f.size() * sizeof(f4)};
-  for (int i = 0; i < 15; i++)
-    if (len[i]) std::memcpy(host.data() + L.off[i], src[i], len[i]);
+  ArenaSection sec[ARENA_SECTIONS];
+  arena_sections(S, sec);
+  for (int i = 0; i < ARENA_SECTIONS; i++)
+    if (sec[i].bytes) std::memcpy(host.data() + L.off[i], sec[i].data, sec[i].bytes);
   Slot s;
   TPT_CUDA(cudaMalloc(&s.arena, L.total));
   cudaError_t e = cudaMemcpyAsync(s.arena, host.data(), L.total, cudaMemcpyHostToDevice, c->stream);
@@ -451,19 +472,21 @@ tpt_status tpt_scene_upload(tpt_context *c, const tpt_scene *sc, int32_t *slot) 
   DevScene &d = s.ds;
   d.node_lo = (const f4 *)(base + L.off[0]);
   d.node_hi = (const f4 *)(base + L.off[1]);
-  d.leaf_hdr = (const i4 *)(base + L.off[2]);
-  d.leaf_user = (const int32_t *)(base + L.off[3]);
-  d.leaf_data = (const f4 *)(base + L.off[4]);
-  d.items = (const i2 *)(base + L.off[5]);
-  d.mat_i = (const i4 *)(base + L.off[6]);
-  d.mat_f = (const f4 *)(base + L.off[7]);
-  d.tex_i = (const i4 *)(base + L.off[8]);
-  d.tex_f = (const f4 *)(base + L.off[9]);
-  d.images = base + L.off[10];
-  d.perlin_grad = (const f4 *)(base + L.off[11]);
-  d.perlin_perm = (const int32_t *)(base + L.off[12]);
-  d.light_i = (const i4 *)(base + L.off[13]);
-  d.light_f = (const f4 *)(base + L.off[14]);
+  d.node_skip = (const int32_t *)(base + L.off[2]);
+  d.leaf_hdr = (const i4 *)(base + L.off[3]);
+  d.leaf_user = (const int32_t *)(base + L.off[4]);
+  d.leaf_data = (const f4 *)(base + L.off[5]);
+  d.items = (const i2 *)(base + L.off[6]);
+  d.mat_i = (const i4 *)(base + L.off[7]);
+  d.mat_f = (const f4 *)(base + L.off[8]);
+  d.tex_i = (const i4 *)(base + L.off[9]);
+  d.tex_f = (const f4 *)(base + L.off[10]);
+  d.images = base + L.off[11];
+  d.perlin_grad = (const f4 *)(base + L.off[12]);
+  d.perlin_perm = (const int32_t *)(base + L.off[13]);
+  d.light_i = (const i4 *)(base + L.off[14]);
+  d.light_f = (const f4 *)(base + L.off[15]);
+  d.flat_max = DEFAULT_FLAT_MAX;
   d.n_nodes = (int32_t)S.node_lo.size();
   d.n_leaves = (int32_t)S.leaf_hdr.size();
   d.n_items = (int32_t)S.items.size();
@@ -514,10 +537,12 @@ tpt_status tpt_trace_closest(tpt_context *c, int32_t slot, const float *rays, in
   }
   TPT_CUDA(cudaMemsetAsync(c->err, 0, sizeof(int), c->stream));
   const int block = 128, smem = stack_smem(block);
+  DevScene ds = c->slots[slot].ds;
+  ds.flat_max = c->flat_nodes;
   int grid = grid_for(c, k_trace_closest, block, smem);
   const long long need = (n + block - 1) / block;
   if (grid > need) grid = (int)need;
-  k_trace_closest<<<grid, block, smem, c->stream>>>(c->slots[slot].ds, d_rays, n,
+  k_trace_closest<<<grid, block, smem, c->stream>>>(ds, d_rays, n,
                                                    make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)), d_f, d_i,
                                                    c->err);
   TPT_CUDA(cudaGetLastError());
@@ -566,6 +591,7 @@ static tpt_status run_wavefront(tpt_context *c, const DevScene &S, const RenderC
   std::memcpy(c->counters_host, &init, sizeof(init));
   TPT_CUDA(cudaMemcpyAsync(c->counters, c->counters_host, sizeof(WfCounters), cudaMemcpyHostToDevice, c->stream));
   const int smem = stack_smem(block);
+  TPT_CUDA(smem_optin(k_wf_traverse, smem));
   const int g_gen = std::max(1, std::min<int>((int)((first + block - 1) / block), c->sm_count * 8));
   k_wf_generate<<<g_gen, block, 0, c->stream>>>(S, F, P[0], 0ull, first, cfg.key);
   TPT_CUDA(cudaGetLastError());
@@ -632,19 +658,33 @@ static tpt_status run_wavefront(tpt_context *c, const DevScene &S, const RenderC
   return result;
 }
 
+// Register-capped variants of the persistent kernel (occupancy vs spills),
+// selected by tpt_render_params.wave when the persistent engine runs.
+typedef void (*PersistentKernel)(DevScene, RenderCfg, FrameDesc, WfCounters *);
+static PersistentKernel persistent_variant(int v) {
+  switch (v) {
+    case 6: return k_persistent<6>;
+    case 8: return k_persistent<8>;
+    default: return k_persistent<4>;
+  }
+}
+
 static tpt_status run_persistent(tpt_context *c, const DevScene &S, const RenderCfg &cfg, const FrameDesc &F, int block,
-                                 bool profile, tpt_render_stats *stats) {
+                                 int variant, bool profile, tpt_render_stats *stats) {
   WfCounters init{};
   std::memcpy(c->counters_host, &init, sizeof(init));
   TPT_CUDA(cudaMemcpyAsync(c->counters, c->counters_host, sizeof(WfCounters), cudaMemcpyHostToDevice, c->stream));
   const int smem = stack_smem(block);
-  const int grid = grid_for(c, k_persistent, block, smem);
+  const PersistentKernel kern = persistent_variant(variant);
+  if (block > 128) return TPT_ERR_INVALID_ARGUMENT;  // launch bounds of the variants
+  TPT_CUDA(smem_optin(kern, smem));
+  const int grid = grid_for(c, kern, block, smem);
   if (profile && !c->prof_ev[0]) {
     for (auto &ev : c->prof_ev)
       if (cudaEventCreate(&ev) != cudaSuccess) return TPT_ERR_CUDA;
   }
   if (profile) cudaEventRecord(c->prof_ev[0], c->stream);
-  k_persistent<<<grid, block, smem, c->stream>>>(S, cfg, F, c->counters);
+  kern<<<grid, block, smem, c->stream>>>(S, cfg, F, c->counters);
   TPT_CUDA(cudaGetLastError());
   if (profile) cudaEventRecord(c->prof_ev[1], c->stream);
   TPT_CUDA(cudaMemcpyAsync(c->counters_host, c->counters, sizeof(WfCounters), cudaMemcpyDeviceToHost, c->stream));
@@ -687,10 +727,11 @@ extern "C" tpt_status tpt_render(tpt_context *c, int32_t slot, const tpt_render_
   TPT_CUDA(cudaEventRecord(c->ev0, c->stream));
   TPT_CUDA(cudaMemsetAsync(c->accum.p, 0, npix * sizeof(float4), c->stream));
   if (F.accum64) TPT_CUDA(cudaMemsetAsync(c->accum64.p, 0, npix * 3 * sizeof(double), c->stream));
-  const DevScene &S = c->slots[slot].ds;
-  const int engine = p->engine == TPT_ENGINE_AUTO ? TPT_ENGINE_WAVEFRONT : p->engine;
+  DevScene S = c->slots[slot].ds;
+  S.flat_max = p->flat_nodes > 0 ? p->flat_nodes : c->flat_nodes;
+  const int engine = p->engine == TPT_ENGINE_AUTO ? TPT_ENGINE_PERSISTENT : p->engine;
   if (engine == TPT_ENGINE_PERSISTENT)
-    st = run_persistent(c, S, cfg, F, block, p->profile != 0, stats);
+    st = run_persistent(c, S, cfg, F, p->block > 0 ? block : 128, p->wave, p->profile != 0, stats);
   else
     st = run_wavefront(c, S, cfg, F, block, wave, p->profile != 0, stats);
   if (st != TPT_OK) return st;
@@ -716,3 +757,4 @@ extern "C" tpt_status tpt_render(tpt_context *c, int32_t slot, const tpt_render_
   }
   return TPT_OK;
 }
+

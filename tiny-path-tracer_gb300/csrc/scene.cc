@@ -641,6 +641,7 @@ struct Compiler {
     int me = (int)S.node_lo.size();
     S.node_lo.push_back(f4{n.bbox.mn.e[0], n.bbox.mn.e[1], n.bbox.mn.e[2], 0});
     S.node_hi.push_back(f4{n.bbox.mx.e[0], n.bbox.mx.e[1], n.bbox.mx.e[2], 0});
+    S.node_skip.push_back(0);
     int refs[2];
     int ch[2] = {n.left, n.right};
     for (int c = 0; c < 2; c++) {
@@ -661,6 +662,7 @@ struct Compiler {
     int32_t lref = refs[0], rref = refs[1];
     std::memcpy(&S.node_lo[me].w, &lref, 4);
     std::memcpy(&S.node_hi[me].w, &rref, 4);
+    S.node_skip[me] = (int32_t)S.node_lo.size();  // subtree = [me, skip)
     return me;
   }
 
@@ -781,6 +783,44 @@ struct Compiler {
     return (int)S.leaf_hdr.size() - 1;
   }
 
+  // Instanced BVHs are flattened before the top level so that every BVH
+  // owns a contiguous pre-order range (the stackless walk relies on it).
+  void flatten_instanced(int h, std::vector<char> &seen) {
+    if (seen[h]) return;
+    seen[h] = 1;
+    const HNode &n = B.nodes[h];
+    switch (n.kind) {
+      case H_TRANSLATE:
+      case H_ROTY: {
+        int cur = n.child;
+        while (B.nodes[cur].kind == H_TRANSLATE || B.nodes[cur].kind == H_ROTY || B.nodes[cur].kind == H_FLIP)
+          cur = B.nodes[cur].child;
+        if (B.nodes[cur].kind == H_BVH && !blas_root.count(cur)) {
+          int md = 0;
+          int root = flatten_bvh(cur, true, 1, md);
+          if (root < 0) return;
+          blas_root[cur] = root;
+          S.blas_depth = std::max(S.blas_depth, md);
+          S.n_blas++;
+        }
+        return;
+      }
+      case H_FLIP:
+      case H_MEDIUM:
+        flatten_instanced(n.child, seen);
+        return;
+      case H_LIST:
+        for (int it : n.items) flatten_instanced(it, seen);
+        return;
+      case H_BVH:
+        flatten_instanced(n.left, seen);
+        flatten_instanced(n.right, seen);
+        return;
+      default:
+        return;
+    }
+  }
+
   void flatten_list(int h, std::vector<int> &out) {
     const HNode &n = B.nodes[h];
     for (int it : n.items) {
@@ -850,6 +890,11 @@ struct Compiler {
     else
       items.push_back(B.world);
     int top_depth = 0;
+    {
+      std::vector<char> seen(B.nodes.size(), 0);
+      for (int h : items) flatten_instanced(h, seen);
+      if (st != TPT_OK) return st;
+    }
     for (int h : items) {
       if (B.nodes[h].kind == H_BVH) {
         int md = 0;

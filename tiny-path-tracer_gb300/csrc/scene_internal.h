@@ -13,6 +13,7 @@ namespace tpt {
 
 struct HostScene {
   std::vector<f4> node_lo, node_hi;
+  std::vector<int32_t> node_skip;  // pre-order index just past each node's subtree
   std::vector<i4> leaf_hdr;
   std::vector<int32_t> leaf_user;
   std::vector<f4> leaf_data;
@@ -31,26 +32,48 @@ struct HostScene {
   Camera cam{};
 };
 
-// Sections of the device arena, each 256-byte aligned.
+// Sections of the device arena, each 256-byte aligned, in DevScene order.
+enum { ARENA_SECTIONS = 16 };
+struct ArenaSection {
+  const void *data;
+  size_t bytes;
+};
+inline void arena_sections(const HostScene &S, ArenaSection out[ARENA_SECTIONS]) {
+  const ArenaSection t[ARENA_SECTIONS] = {
+      {S.node_lo.data(), S.node_lo.size() * sizeof(f4)},
+      {S.node_hi.data(), S.node_hi.size() * sizeof(f4)},
+      {S.node_skip.data(), S.node_skip.size() * sizeof(int32_t)},
+      {S.leaf_hdr.data(), S.leaf_hdr.size() * sizeof(i4)},
+      {S.leaf_user.data(), S.leaf_user.size() * sizeof(int32_t)},
+      {S.leaf_data.data(), S.leaf_data.size() * sizeof(f4)},
+      {S.items.data(), S.items.size() * sizeof(i2)},
+      {S.mat_i.data(), S.mat_i.size() * sizeof(i4)},
+      {S.mat_f.data(), S.mat_f.size() * sizeof(f4)},
+      {S.tex_i.data(), S.tex_i.size() * sizeof(i4)},
+      {S.tex_f.data(), S.tex_f.size() * sizeof(f4)},
+      {S.images.data(), S.images.size()},
+      {S.perlin_grad.data(), S.perlin_grad.size() * sizeof(f4)},
+      {S.perlin_perm.data(), S.perlin_perm.size() * sizeof(int32_t)},
+      {S.light_i.data(), S.light_i.size() * sizeof(i4)},
+      {S.light_f.data(), S.light_f.size() * sizeof(f4)}};
+  for (int i = 0; i < ARENA_SECTIONS; i++) out[i] = t[i];
+}
+
 struct ArenaLayout {
-  size_t off[15];
+  size_t off[ARENA_SECTIONS];
   size_t total;
 };
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 inline ArenaLayout arena_layout(const HostScene &S) {
-  size_t sizes[15] = {
-      S.node_lo.size() * sizeof(f4),     S.node_hi.size() * sizeof(f4),   S.leaf_hdr.size() * sizeof(i4),
-      S.leaf_user.size() * sizeof(int32_t), S.leaf_data.size() * sizeof(f4), S.items.size() * sizeof(i2),
-      S.mat_i.size() * sizeof(i4),       S.mat_f.size() * sizeof(f4),     S.tex_i.size() * sizeof(i4),
-      S.tex_f.size() * sizeof(f4),       S.images.size(),                 S.perlin_grad.size() * sizeof(f4),
-      S.perlin_perm.size() * sizeof(int32_t), S.light_i.size() * sizeof(i4), S.light_f.size() * sizeof(f4)};
+  ArenaSection sec[ARENA_SECTIONS];
+  arena_sections(S, sec);
   ArenaLayout L;
   size_t at = 0;
-  for (int i = 0; i < 15; i++) {
+  for (int i = 0; i < ARENA_SECTIONS; i++) {
     L.off[i] = at;
-    at += align256(sizes[i] ? sizes[i] : 16);
+    at += align256(sec[i].bytes ? sec[i].bytes : 16);
   }
   L.total = at;
   return L;

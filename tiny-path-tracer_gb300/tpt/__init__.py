@@ -44,7 +44,7 @@ class RenderParams(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("max_depth", C.c_int32),
                 ("semantics", C.c_int32), ("background", C.c_int32), ("sky_scale", C.c_float),
                 ("seed", C.c_uint64), ("engine", C.c_int32), ("block", C.c_int32), ("wave", C.c_int32),
-                ("accumulate_fp64", C.c_int32), ("profile", C.c_int32)]
+                ("accumulate_fp64", C.c_int32), ("profile", C.c_int32), ("flat_nodes", C.c_int32)]
 
 
 class RenderStats(C.Structure):
@@ -104,6 +104,7 @@ _SIGS = {
     "tpt_context_create": (C.c_int32, [C.c_int32, C.c_void_p]),
     "tpt_context_destroy": (None, [C.c_void_p]),
     "tpt_context_set_stream": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "tpt_context_set_option": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int64]),
     "tpt_scene_upload": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int32)]),
     "tpt_scene_release": (C.c_int32, [C.c_void_p, C.c_int32]),
     "tpt_trace_closest": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_uint64, C.c_void_p,
@@ -200,6 +201,10 @@ class Context:
     def set_stream(self, stream_ptr: int | None):
         check(lib().tpt_context_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
 
+    def set_flat_nodes(self, n: int) -> None:
+        """BVHs of at most n nodes use the stackless walk (0: never)."""
+        check(lib().tpt_context_set_option(self._h, 1, n), "set_option")
+
     def upload(self, scene: Scene) -> int:
         slot = C.c_int32()
         check(lib().tpt_scene_upload(self._h, scene.handle, C.byref(slot)), "scene_upload")
@@ -224,9 +229,9 @@ class Context:
     def render(self, slot: int, width: int, height: int, spp: int, max_depth: int = 50,
                semantics: int = SEMANTICS_REFERENCE, background: int = BACKGROUND_BLACK, sky_scale: float = 1.0,
                seed: int = 1, engine: int = ENGINE_AUTO, block: int = 0, wave: int = 0, fp64: bool = False,
-               profile: bool = False, out=None):
+               profile: bool = False, flat_nodes: int = 0, out=None):
         p = make_params(width, height, spp, max_depth, semantics, background, sky_scale, seed, engine, block,
-                        wave, fp64, profile)
+                        wave, fp64, profile, flat_nodes)
         st = RenderStats()
         if out is None:
             img = np.zeros((height, width, 3), np.float32)
@@ -238,13 +243,14 @@ class Context:
 
 
 def make_params(width, height, spp, max_depth=50, semantics=0, background=0, sky_scale=1.0, seed=1, engine=0,
-                block=0, wave=0, fp64=False, profile=False) -> RenderParams:
+                block=0, wave=0, fp64=False, profile=False, flat_nodes=0) -> RenderParams:
     p = RenderParams()
     lib().tpt_render_params_default(C.byref(p))
     p.width, p.height, p.spp, p.max_depth = width, height, spp, max_depth
     p.semantics, p.background, p.sky_scale, p.seed = semantics, background, sky_scale, seed
     p.engine, p.block, p.wave, p.accumulate_fp64 = engine, block, wave, int(bool(fp64))
     p.profile = int(bool(profile))
+    p.flat_nodes = flat_nodes
     return p
 
 
