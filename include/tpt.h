@@ -214,6 +214,31 @@ void tpt_render_params_default(tpt_render_params *p);
 tpt_status tpt_render(tpt_context *ctx, int32_t slot, const tpt_render_params *p, float *out_rgb, int32_t mem,
                       tpt_render_stats *stats);
 
+/* Render without allocating any memory (no counterpart in the reference).
+ * For callers that cannot call cudaMalloc: a plugin inside a host program
+ * that owns all device memory through its own pool, code running while a
+ * CUDA graph is being captured, or a real-time loop that must not take the
+ * implicit device synchronisation of an allocation.  The caller passes, in
+ * memory it owns:
+ *   arena_dev    device buffer of at least tpt_scene_info.arena_bytes bytes;
+ *                each call copies the compiled scene into it (host-to-device
+ *                copies only),
+ *   out_rgb_dev  device buffer of width*height*3 floats (the mean radiance,
+ *                row 0 = top, as tpt_render writes it),
+ *   stream       the cudaStream_t to run on (NULL = the legacy default).
+ * The per-pixel accumulators and counters live in one file-scope device
+ * array of TPT_NOALLOC_MAX_PIXELS*16 + 256 bytes (16 MiB), which every GPU
+ * that loads the library holds until the process exits; images of more than
+ * TPT_NOALLOC_MAX_PIXELS pixels are rejected with TPT_ERR_INVALID_ARGUMENT.
+ * The persistent engine renders; the call returns after the stream has
+ * finished.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (other threads,
+ * other streams) race and corrupt each other's images. */
+#define TPT_NOALLOC_MAX_PIXELS (1 << 20)
+tpt_status tpt_render_noalloc(const tpt_scene *scene, void *arena_dev, int64_t arena_bytes,
+                              const tpt_render_params *p, float *out_rgb_dev, void *stream);
+
 /* Host helpers: reference output quantisation (main.cpp:135-142,176-182) and
  * the PPM P3 writer of main.cpp:69,183-189. */
 void tpt_quantize(const float *mean_rgb, int64_t n_pixels, uint8_t *rgb8);

@@ -758,3 +758,114 @@ extern "C" tpt_status tpt_render(tpt_context *c, int32_t slot, const tpt_render_
   return TPT_OK;
 }
 
+// ======================================================= no-allocation path
+// Scratch of tpt_render_noalloc: float4 accumulators for up to
+// TPT_NOALLOC_MAX_PIXELS pixels, then the counters.  Host code must not use
+// the symbol as an address: its device address comes from
+// cudaGetSymbolAddress, looked up once per device.
+static constexpr size_t kNoallocAccumBytes = (size_t)TPT_NOALLOC_MAX_PIXELS * sizeof(float4);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocAccumBytes + 256];
+
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_addr[64];  // per device ordinal
+
+static tpt_status noalloc_scratch(int device, void **out) {
+  if (device < 0 || device >= 64) return TPT_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[device]) {
+    void *addr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_status(e);
+    g_noalloc_addr[device] = addr;
+  }
+  *out = g_noalloc_addr[device];
+  return TPT_OK;
+}
+
+extern "C" tpt_status tpt_render_noalloc(const tpt_scene *scene, void *arena_dev, int64_t arena_bytes,
+                                         const tpt_render_params *p, float *out_rgb_dev, void *stream_ptr) {
+  if (!scene || !arena_dev || !p || !out_rgb_dev) return TPT_ERR_INVALID_ARGUMENT;
+  if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->max_depth < 0) return TPT_ERR_INVALID_ARGUMENT;
+  const unsigned long long npix = (unsigned long long)p->width * (unsigned long long)p->height;
+  if (npix > (unsigned long long)TPT_NOALLOC_MAX_PIXELS) {
+    std::snprintf(g_last_error, sizeof(g_last_error),
+                  "tpt_render_noalloc: %llu pixels exceed TPT_NOALLOC_MAX_PIXELS (%d)", npix,
+                  TPT_NOALLOC_MAX_PIXELS);
+    return TPT_ERR_INVALID_ARGUMENT;
+  }
+  const HostScene &H = *host_scene(scene);
+  const ArenaLayout L = arena_layout(H);
+  if (arena_bytes < (int64_t)L.total) {
+    std::snprintf(g_last_error, sizeof(g_last_error), "tpt_render_noalloc: arena buffer of %lld bytes, need %zu",
+                  (long long)arena_bytes, L.total);
+    return TPT_ERR_INVALID_ARGUMENT;
+  }
+  const int block = p->block > 0 ? p->block : 128;
+  if (block % 32 || block > 128) return TPT_ERR_INVALID_ARGUMENT;
+  cudaStream_t stream = (cudaStream_t)stream_ptr;
+  int device = 0;
+  TPT_CUDA(cudaGetDevice(&device));
+  void *scratch = nullptr;
+  tpt_status st = noalloc_scratch(device, &scratch);
+  if (st != TPT_OK) return st;
+  int sm_count = 0;
+  TPT_CUDA(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device));
+
+  // the scene: section by section from the host vectors into the caller's buffer
+  ArenaSection sec[ARENA_SECTIONS];
+  arena_sections(H, sec);
+  uint8_t *base = (uint8_t *)arena_dev;
+  for (int i = 0; i < ARENA_SECTIONS; i++)
+    if (sec[i].bytes) TPT_CUDA(cudaMemcpyAsync(base + L.off[i], sec[i].data, sec[i].bytes, cudaMemcpyHostToDevice, stream));
+  DevScene d{};
+  d.node_lo = (const f4 *)(base + L.off[0]);
+  d.node_hi = (const f4 *)(base + L.off[1]);
+  d.node_skip = (const int32_t *)(base + L.off[2]);
+  d.leaf_hdr = (const i4 *)(base + L.off[3]);
+  d.leaf_user = (const int32_t *)(base + L.off[4]);
+  d.leaf_data = (const f4 *)(base + L.off[5]);
+  d.items = (const i2 *)(base + L.off[6]);
+  d.mat_i = (const i4 *)(base + L.off[7]);
+  d.mat_f = (const f4 *)(base + L.off[8]);
+  d.tex_i = (const i4 *)(base + L.off[9]);
+  d.tex_f = (const f4 *)(base + L.off[10]);
+  d.images = base + L.off[11];
+  d.perlin_grad = (const f4 *)(base + L.off[12]);
+  d.perlin_perm = (const int32_t *)(base + L.off[13]);
+  d.light_i = (const i4 *)(base + L.off[14]);
+  d.light_f = (const f4 *)(base + L.off[15]);
+  d.n_nodes = (int32_t)H.node_lo.size();
+  d.n_leaves = (int32_t)H.leaf_hdr.size();
+  d.n_items = (int32_t)H.items.size();
+  d.n_mats = (int32_t)H.mat_i.size();
+  d.n_texs = (int32_t)H.tex_i.size();
+  d.n_lights = (int32_t)H.light_i.size();
+  d.light_is_list = H.light_is_list;
+  d.has_lights = H.has_lights;
+  d.flat_max = p->flat_nodes > 0 ? p->flat_nodes : DEFAULT_FLAT_MAX;
+  d.cam = H.cam;
+
+  // the scratch keeps the previous call's contents: clear accumulators and counters
+  float4 *accum = (float4 *)scratch;
+  WfCounters *counters = (WfCounters *)((uint8_t *)scratch + kNoallocAccumBytes);
+  TPT_CUDA(cudaMemsetAsync(accum, 0, npix * sizeof(float4), stream));
+  TPT_CUDA(cudaMemsetAsync(counters, 0, sizeof(WfCounters), stream));
+  const FrameDesc F{p->width, p->height, p->spp, npix * (unsigned long long)p->spp, accum, nullptr};
+  const RenderCfg cfg{p->max_depth, p->semantics, p->background, p->sky_scale,
+                      make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32))};
+  const PersistentKernel kern = persistent_variant(p->wave);
+  const int smem = stack_smem(block);
+  TPT_CUDA(smem_optin(kern, smem));
+  int per_sm = 0;
+  TPT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem));
+  const int grid = sm_count * (per_sm < 1 ? 1 : per_sm);
+  kern<<<grid, block, smem, stream>>>(d, cfg, F, counters);
+  TPT_CUDA(cudaGetLastError());
+  const int rgrid = (int)std::min<unsigned long long>((npix + 255) / 256, (unsigned long long)sm_count * 16);
+  k_resolve<<<rgrid, 256, 0, stream>>>(F, out_rgb_dev);
+  TPT_CUDA(cudaGetLastError());
+  int err = 0;
+  TPT_CUDA(cudaMemcpyAsync(&err, &counters->err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  TPT_CUDA(cudaStreamSynchronize(stream));
+  return err ? (tpt_status)err : TPT_OK;
+}

@@ -112,6 +112,8 @@ _SIGS = {
     "tpt_render_params_default": (None, [C.POINTER(RenderParams)]),
     "tpt_render": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.c_void_p, C.c_int32,
                                C.POINTER(RenderStats)]),
+    "tpt_render_noalloc": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(RenderParams), C.c_void_p,
+                                       C.c_void_p]),
     "tpt_quantize": (None, [C.c_void_p, C.c_int64, C.c_void_p]),
     "tpt_write_ppm": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int32, C.c_int32]),
 }
