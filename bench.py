@@ -183,6 +183,54 @@ def reference_arm(args) -> None:
     print(json.dumps(out))
 
 
+def batch_bench(args) -> None:
+    """64 seeded random-sphere scenes (50..5000 spheres, 256^2..1024^2, 8..64
+    spp) rendered in one persistent launch replayed from a CUDA graph."""
+    import torch
+    import tpt
+    from tpt import scenes
+
+    torch.cuda.set_device(0)
+    ctx = tpt.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    sds = scenes.batch_scenes(seed=2, count=64)
+    t0 = time.perf_counter()
+    slots = [ctx.upload(tpt.Scene(sd.text())) for sd in sds]
+    build_s = time.perf_counter() - t0
+    jobs = [(slot, sd.meta["width"], sd.meta["height"], sd.meta["spp"]) for slot, sd in zip(slots, sds)]
+    outs = [torch.empty((h, w, 3), dtype=torch.float32, device="cuda") for _, w, h, _ in jobs]
+    ptrs = [o.data_ptr() for o in outs]
+    kw = dict(max_depth=50, background=tpt.BACKGROUND_SKY, seed=1, block=args.block, variant=args.wave)
+    for _ in range(args.warmup):
+        tpt.render_batch(ctx, jobs, outs=ptrs, **kw)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    times, st = [], None
+    for k in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _, st = tpt.render_batch(ctx, jobs, outs=ptrs, **kw)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    samples = st["samples"]
+    ms = float(np.mean(times))
+    out = {"metric": "Msamples/s (64-scene random-sphere batch, one persistent launch, 1 GPU)",
+           "value": samples / (ms / 1e3) / 1e6, "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "batch_64_random_sphere_scenes", "scenes": len(jobs), "samples_per_step": samples,
+                      "spheres": [sd.meta["n_spheres"] for sd in sds][:8] + ["..."],
+                      "segments_per_step": st["segments"], "scene_build_and_upload_s": build_s},
+           "gpu_launches": st["kernel_launches"] * args.steps, "clocks": clk}
+    print(json.dumps(out))
+    ctx.close()
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -194,9 +242,14 @@ def main() -> None:
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--spp", type=int, default=SPP, help="smaller cases for profiling only")
+    ap.add_argument("--workload", default="cornell", choices=["cornell", "batch"],
+                    help="cornell: the headline workload; batch: 64 seeded random-sphere scenes in one launch")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
+        return
+    if args.workload == "batch":
+        batch_bench(args)
         return
 
     import torch

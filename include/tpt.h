@@ -239,6 +239,60 @@ tpt_status tpt_render(tpt_context *ctx, int32_t slot, const tpt_render_params *p
 tpt_status tpt_render_noalloc(const tpt_scene *scene, void *arena_dev, int64_t arena_bytes,
                               const tpt_render_params *p, float *out_rgb_dev, void *stream);
 
+/* Batched render: many scenes of uneven size, resolution and spp in one
+ * persistent launch (configs of many small jobs).  Each item names an
+ * uploaded scene, its frame size and spp, and its output (width*height*3
+ * floats, TPT_MEM_HOST or TPT_MEM_DEVICE for all items).  `common` supplies
+ * the remaining parameters (max_depth, semantics, background, seed, block,
+ * wave = register variant, flat_nodes, profile); an item's image equals what
+ * tpt_render would produce for it with the same parameters.  The launch
+ * sequence (clear, persistent kernel, resolves) is captured once into a CUDA
+ * graph and replayed while the items and parameters stay the same. */
+typedef struct {
+  int32_t slot;
+  int32_t width, height, spp;
+  float *out_rgb;
+} tpt_batch_item;
+enum { TPT_MAX_BATCH = 256 };
+tpt_status tpt_render_batch(tpt_context *ctx, const tpt_batch_item *items, int32_t n, const tpt_render_params *common,
+                            int32_t mem, tpt_render_stats *stats);
+
+/* Autotuner: renders `probe_spp` samples per pixel with each candidate
+ * configuration - engine, threads per block, register variant, wavefront
+ * queue size, stackless-walk threshold - times them with CUDA events, writes
+ * the fastest into *p (engine, block, wave, flat_nodes; the other fields are
+ * kept) and remembers it for the slot, so later renders of that slot with
+ * engine = TPT_ENGINE_AUTO use it.  best_msps (may be NULL) receives the
+ * winner's Msamples/s. */
+tpt_status tpt_autotune(tpt_context *ctx, int32_t slot, tpt_render_params *p, int32_t probe_spp, double *best_msps);
+
+/* ------------------------------------------------------------------------
+ * Learned parts: fully fused FP16 MLPs on the tensor cores (FP32
+ * accumulation), in -> [64, ReLU] x n_hidden -> out, no biases, weights
+ * row-major [out][in] per layer, concatenated.  Supported shapes:
+ * (112, 3, 48) path-guiding network, (64, 5, 16) radiance cache,
+ * (32, 2, 16) test network.  Batches are device buffers of `rows` rows,
+ * rows a multiple of 16; x is row-major f16 [rows][in], y f32 [rows][out].
+ * (No counterpart in the reference.)
+ * ---------------------------------------------------------------------- */
+typedef struct tpt_mlp tpt_mlp;
+tpt_status tpt_mlp_create(int32_t device, int32_t in_dim, int32_t n_hidden, int32_t out_dim, uint64_t seed,
+                          tpt_mlp **out);
+void tpt_mlp_destroy(tpt_mlp *m);
+int64_t tpt_mlp_param_count(const tpt_mlp *m);
+tpt_status tpt_mlp_set_params(tpt_mlp *m, const float *host_params);
+tpt_status tpt_mlp_get_params(const tpt_mlp *m, float *host_params);
+/* f32 weight gradients accumulated since the last Adam step (loss-scaled). */
+tpt_status tpt_mlp_get_grad(const tpt_mlp *m, float *host_grad);
+tpt_status tpt_mlp_forward(tpt_mlp *m, const void *x_f16, int64_t rows, float *y, void *stream);
+/* Accumulates the weight gradient of sum(scale * dy * y) (dy: f32 [rows][out]). */
+tpt_status tpt_mlp_backward_given(tpt_mlp *m, const void *x_f16, const float *dy, int64_t rows, float scale,
+                                  void *stream);
+/* Adam step (lr, beta 0.9/0.999, eps 1e-8) on the accumulated gradient
+ * multiplied by inv_loss_scale; clears the gradient. */
+tpt_status tpt_mlp_adam(tpt_mlp *m, float lr, float inv_loss_scale, void *stream);
+const char *tpt_mlp_last_error(void);
+
 /* Host helpers: reference output quantisation (main.cpp:135-142,176-182) and
  * the PPM P3 writer of main.cpp:69,183-189. */
 void tpt_quantize(const float *mean_rgb, int64_t n_pixels, uint8_t *rgb8);

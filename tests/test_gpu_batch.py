@@ -1,0 +1,64 @@
+"""Batched rendering (one persistent launch over many scenes, replayed from a
+CUDA graph) and the autotuner.  An item of a batch must equal tpt_render of
+the same scene with the same parameters: both draw each sample from the same
+counter-based stream, so images differ only by float accumulation order."""
+import numpy as np
+import pytest
+
+import tpt
+from tpt import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _slots(ctx):
+    sds = [scenes.cornell(), scenes.one_weekend(seed=5), scenes.instance_scene(), scenes.next_week(image_size=(64, 32)),
+           scenes.cornell_guiding()]
+    return [ctx.upload(tpt.Scene(sd.text())) for sd in sds]
+
+
+def test_batch_items_equal_individual_renders(ctx):
+    slots = _slots(ctx)
+    jobs = [(slots[0], 40, 30, 8), (slots[1], 17, 23, 16), (slots[2], 32, 32, 4), (slots[3], 24, 24, 8),
+            (slots[4], 50, 10, 12), (slots[0], 8, 8, 64)]
+    imgs, st = tpt.render_batch(ctx, jobs, max_depth=50, background=tpt.BACKGROUND_SKY, seed=77)
+    assert st["samples"] == sum(w * h * s for _, w, h, s in jobs)
+    for (slot, w, h, spp), img in zip(jobs, imgs):
+        ref, _ = ctx.render(slot, w, h, spp, 50, background=tpt.BACKGROUND_SKY, seed=77,
+                            engine=tpt.ENGINE_PERSISTENT)
+        np.testing.assert_allclose(img, ref, rtol=1e-5, atol=1e-6)
+    # replay of the captured graph gives the same images
+    imgs2, _ = tpt.render_batch(ctx, jobs, max_depth=50, background=tpt.BACKGROUND_SKY, seed=77)
+    for a, b in zip(imgs, imgs2):
+        np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-6)
+    for s in set(slots):
+        ctx.release(s)
+
+
+def test_batch_device_outputs_and_errors(ctx):
+    import torch
+
+    slots = _slots(ctx)
+    outs = [torch.zeros((16, 16, 3), device="cuda") for _ in range(2)]
+    torch.cuda.synchronize()
+    jobs = [(slots[0], 16, 16, 4), (slots[1], 16, 16, 4)]
+    _, st = tpt.render_batch(ctx, jobs, seed=3, outs=[o.data_ptr() for o in outs])
+    imgs, _ = tpt.render_batch(ctx, jobs, seed=3)
+    for o, i in zip(outs, imgs):
+        np.testing.assert_allclose(o.cpu().numpy(), i, rtol=1e-5, atol=1e-6)
+    with pytest.raises(tpt.TptError):
+        tpt.render_batch(ctx, [(slots[0] + 100, 8, 8, 1)])
+    with pytest.raises(tpt.TptError):
+        tpt.render_batch(ctx, [(slots[0], 0, 8, 1)])
+    for s in set(slots):
+        ctx.release(s)
+
+
+def test_autotune_picks_a_config_that_auto_renders_use(ctx):
+    slot = ctx.upload(tpt.Scene(scenes.cornell().text()))
+    eng, block, wave, flat, msps = tpt.autotune(ctx, slot, 120, 120, probe_spp=2)
+    assert eng in (tpt.ENGINE_WAVEFRONT, tpt.ENGINE_PERSISTENT) and block in (64, 128, 256) and msps > 0
+    a, _ = ctx.render(slot, 40, 40, 8, seed=5, fp64=True)  # engine AUTO -> tuned
+    b, _ = ctx.render(slot, 40, 40, 8, seed=5, fp64=True, engine=eng, block=block, wave=wave, flat_nodes=flat)
+    np.testing.assert_allclose(a, b, rtol=1e-6, atol=1e-7)
+    ctx.release(slot)

@@ -3,7 +3,8 @@ host scene compiler + C ABI), compiled in-tree into tiny-path-tracer_gb300/_buil
 
     python tiny-path-tracer_gb300/build.py
 
-The two translation units compile in parallel: kernels.cu with nvcc
+The translation units compile in parallel: kernels.cu (path tracing) and
+learn.cu (tensor-core MLPs of the learned parts) with nvcc
 (-gencode arch=compute_103a,code=sm_103a; hit arithmetic is written with
 unfused round-to-nearest intrinsics, so FMA contraction stays on for the
 rest), scene.cc with g++ (-ffp-contract=off).
@@ -50,20 +51,24 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
     cuda = _cuda_home(nvcc)
-    k_obj = os.path.join(OUT, "kernels.o")
+    objs, cmds = [], []
+    for cu in ("kernels.cu", "learn.cu"):
+        obj = os.path.join(OUT, cu.replace(".cu", ".o"))
+        objs.append(obj)
+        cmds.append([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
+                     "-Xcompiler", "-fPIC", "-c", os.path.join(CSRC, cu), "-o", obj])
     s_obj = os.path.join(OUT, "scene.o")
-    nv = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
-          "-Xcompiler", "-fPIC", "-c", os.path.join(CSRC, "kernels.cu"), "-o", k_obj]
-    gx = ["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fPIC", "-Wall", f"-I{cuda}/include", "-c",
-          os.path.join(CSRC, "scene.cc"), "-o", s_obj]
-    procs = [subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT) for cmd in (nv, gx)]
-    for cmd, p in zip((nv, gx), procs):
+    objs.append(s_obj)
+    cmds.append(["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fPIC", "-Wall", f"-I{cuda}/include", "-c",
+                 os.path.join(CSRC, "scene.cc"), "-o", s_obj])
+    procs = [subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT) for cmd in cmds]
+    for cmd, p in zip(cmds, procs):
         out, _ = p.communicate()
         if p.returncode != 0:
             raise RuntimeError(f"build failed: {' '.join(cmd)}\n{out.decode(errors='replace')}")
         if verbose and out:
             sys.stdout.write(out.decode(errors="replace"))
-    link = [nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", k_obj, s_obj, "-o", LIB + ".tmp"]
+    link = [nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", *objs, "-o", LIB + ".tmp"]
     r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))

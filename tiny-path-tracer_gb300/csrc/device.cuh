@@ -376,13 +376,13 @@ enum { STK_RESTORE = -1 };
 // semantics of hitable_list::hit across the top-level items (sequential,
 // shrinking t_max) and bvh_node::hit within an item (every child tested with
 // the same interval, ties to the right).  The candidate set is the
-// reference's: a leaf is tested iff every ancestor box passes.  Small BVHs
-// are walked stacklessly in pre-order (a box miss jumps to the node's skip
-// index), which keeps a warp's lanes on the same node sequence; large ones
-// near-first with a shared-memory stack and pruning, which cannot change the
-// result: the winner is the minimum of (t, -leaf order), and a subtree is
-// skipped only when the lower bound prune_key() on any t its primitives can
-// report exceeds the best t.  stk: this thread's stack slots, `stride`
+// reference's: a leaf is tested iff every ancestor box passes.  BVHs of at
+// most flat_max nodes are walked stacklessly in pre-order (a box miss jumps
+// to the node's skip index), which keeps a warp's lanes on the same node
+// sequence; larger ones near-first with a shared-memory stack.  Both prune,
+// which cannot change the result: the winner is the minimum of
+// (t, -leaf order), and a subtree is skipped only when the lower bound
+// prune_key() on any t its primitives can report exceeds the best t.  stk: this thread's stack slots, `stride`
 // entries apart.  err receives TPT_ERR_STACK_OVERFLOW on overflow.
 __device__ bool trace_closest(const DevScene &S, const Ray &wr, float tmin, int2 *stk, int stride,
                               const MediumRng &mrng, HitRef &res, int &err) {
@@ -498,7 +498,7 @@ __device__ bool trace_closest(const DevScene &S, const Ray &wr, float tmin, int2
         for (int i = root; i < end && !overflow;) {
           const f4 lo = ldg4(S.node_lo + i), hi = ldg4(S.node_hi + i);
           float en;
-          if (slab(W, lo, hi, tmin, tmax, en)) {
+          if (slab(W, lo, hi, tmin, tmax, en) && !(prune_key(W, lo, hi, en) > bt)) {
             const int left = __float_as_int(lo.w), right = __float_as_int(hi.w);
             if (right < 0) push(-2 - ~right, never_pruned);
             if (left < 0 && left != right) push(-2 - ~left, never_pruned);

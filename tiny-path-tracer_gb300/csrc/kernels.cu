@@ -286,6 +286,79 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS) k_persistent(DevScene S, Rend
   if (e) atomicExch(&C->err, e);
 }
 
+// Batched persistent engine: the samples of all items form one sequence
+// (prefix sums `first`, kept in shared memory); a claimed sample is mapped
+// to its item by binary search and traced in that item's scene.  Warps claim
+// consecutive samples, so a warp's lanes nearly always share a scene.
+struct BatchItem {
+  DevScene scene;
+  FrameDesc frame;
+  unsigned long long first;
+};
+
+template <int MIN_BLOCKS>
+__global__ void __launch_bounds__(128, MIN_BLOCKS)
+    k_persistent_batch(const BatchItem *__restrict__ items, int n_items, unsigned long long total_all, RenderCfg cfg,
+                       WfCounters *C) {
+  extern __shared__ int2 stack_smem[];
+  __shared__ unsigned long long s_first[TPT_MAX_BATCH];
+  for (int i = threadIdx.x; i < n_items; i += blockDim.x) s_first[i] = items[i].first;
+  __syncthreads();
+  int2 *stk = stack_smem + threadIdx.x;
+  int e = 0;
+  unsigned long long segs = 0;
+  bool alive = false, done = false;
+  Ray r{};
+  float3 T = v3(0.f, 0.f, 0.f), L = v3(0.f, 0.f, 0.f);
+  uint32_t pixel = 0, sample = 0;
+  int depth = 0, item = 0;
+  for (;;) {
+    const bool want = !alive && !done;
+    if (__any_sync(0xffffffffu, want)) {
+      unsigned long long base;
+      int rank;
+      warp_claim(want, &C->issued, base, rank);
+      if (want) {
+        const unsigned long long s = base + (unsigned long long)rank;
+        if (s < total_all) {
+          int lo = 0, hi = n_items - 1;  // last item with first <= s
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_first[mid] <= s) lo = mid; else hi = mid - 1;
+          }
+          item = lo;
+          const BatchItem &B = items[item];
+          int i, j;
+          sample_coords(B.frame, s - s_first[item], pixel, sample, i, j);
+          r = camera_ray(B.scene.cam, i, j, B.frame.nx, B.frame.ny, pixel, sample, cfg.key);
+          T = v3(1.f, 1.f, 1.f);
+          L = v3(0.f, 0.f, 0.f);
+          depth = 0;
+          alive = true;
+        } else {
+          done = true;
+        }
+      }
+    }
+    if (__all_sync(0xffffffffu, done)) break;
+    if (alive) {
+      const DevScene &S = items[item].scene;
+      MediumRng m{make_uint4(pixel, sample, (uint32_t)depth, 0u), cfg.key, 1};
+      HitRef h;
+      const bool hit = trace_closest(S, r, 0.001f, stk, blockDim.x, m, h, e);
+      segs++;
+      if (shade_vertex(S, cfg, r, hit, h, T, L, depth, pixel, sample)) {
+        depth++;
+      } else {
+        accumulate(items[item].frame, pixel, L);
+        alive = false;
+      }
+    }
+  }
+  if (segs) atomicAdd(&C->segments, segs);
+  if (e) atomicExch(&C->err, e);
+}
+
 // mean = sum / spp, image order (row 0 = top).
 __global__ void k_resolve(FrameDesc F, float *__restrict__ out) {
   const long long npix = (long long)F.nx * F.ny;
@@ -317,6 +390,8 @@ struct Slot {
   size_t bytes = 0;
   DevScene ds{};
   bool live = false;
+  bool tuned = false;        // tpt_autotune result for engine = AUTO
+  tpt_render_params tp{};
 };
 
 struct DevBuf {
@@ -333,6 +408,9 @@ struct tpt_context {
   int sm_count = 0;
   std::vector<Slot> slots;
   DevBuf path[2], hits, accum, accum64, staging, rays, hitf, hiti;
+  DevBuf batch_table, batch_accum, batch_staging;
+  cudaGraphExec_t batch_graph = nullptr;  // replayed while the batch key matches
+  uint64_t batch_key = 0;
   WfCounters *counters = nullptr;       // device
   WfCounters *counters_host = nullptr;  // pinned
   int *err = nullptr;                   // device error flag for trace
@@ -418,10 +496,11 @@ void tpt_context_destroy(tpt_context *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (auto &s : c->slots)
     if (s.arena) cudaFree(s.arena);
-  DevBuf *bufs[] = {&c->path[0], &c->path[1], &c->hits, &c->accum, &c->accum64,
-                    &c->staging, &c->rays, &c->hitf, &c->hiti};
+  DevBuf *bufs[] = {&c->path[0], &c->path[1], &c->hits,        &c->accum,       &c->accum64,      &c->staging,
+                    &c->rays,    &c->hitf,    &c->hiti,        &c->batch_table, &c->batch_accum, &c->batch_staging};
   for (DevBuf *b : bufs)
     if (b->p) cudaFree(b->p);
+  if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
   if (c->counters) cudaFree(c->counters);
   if (c->counters_host) cudaFreeHost(c->counters_host);
   if (c->err) cudaFree(c->err);
@@ -513,6 +592,11 @@ tpt_status tpt_scene_release(tpt_context *c, int32_t slot) {
   cudaStreamSynchronize(c->stream);
   cudaFree(c->slots[slot].arena);
   c->slots[slot] = Slot{};
+  if (c->batch_graph) {  // its table may point at the released arena
+    cudaGraphExecDestroy(c->batch_graph);
+    c->batch_graph = nullptr;
+    c->batch_key = 0;
+  }
   return TPT_OK;
 }
 
@@ -720,6 +804,15 @@ extern "C" tpt_status tpt_render(tpt_context *c, int32_t slot, const tpt_render_
               p->accumulate_fp64 ? (double *)c->accum64.p : nullptr};
   RenderCfg cfg{p->max_depth, p->semantics, p->background, p->sky_scale,
                 make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32))};
+  tpt_render_params tuned;
+  if (p->engine == TPT_ENGINE_AUTO && c->slots[slot].tuned) {
+    tuned = *p;
+    tuned.engine = c->slots[slot].tp.engine;
+    tuned.block = c->slots[slot].tp.block;
+    tuned.wave = c->slots[slot].tp.wave;
+    tuned.flat_nodes = c->slots[slot].tp.flat_nodes;
+    p = &tuned;
+  }
   const int block = p->block > 0 ? p->block : 128;
   if (block % 32 || block > 1024) return TPT_ERR_INVALID_ARGUMENT;
   size_t wave = p->wave > 0 ? (size_t)p->wave : (size_t)1 << 20;
@@ -755,6 +848,174 @@ extern "C" tpt_status tpt_render(tpt_context *c, int32_t slot, const tpt_render_
     stats->samples = (int64_t)total;
     stats->kernel_launches += 1;
   }
+  return TPT_OK;
+}
+
+// =============================================================== batches ==
+static uint64_t fnv1a(uint64_t h, const void *data, size_t n) {
+  const uint8_t *b = (const uint8_t *)data;
+  for (size_t i = 0; i < n; i++) {
+    h ^= b[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+typedef void (*BatchKernel)(const BatchItem *, int, unsigned long long, RenderCfg, WfCounters *);
+static BatchKernel batch_variant(int v) {
+  switch (v) {
+    case 6: return k_persistent_batch<6>;
+    case 8: return k_persistent_batch<8>;
+    default: return k_persistent_batch<4>;
+  }
+}
+
+extern "C" tpt_status tpt_render_batch(tpt_context *c, const tpt_batch_item *items, int32_t n,
+                                       const tpt_render_params *p, int32_t mem, tpt_render_stats *stats) {
+  if (!c || !items || !p || n < 1 || n > TPT_MAX_BATCH) return TPT_ERR_INVALID_ARGUMENT;
+  const int block = p->block > 0 ? p->block : 128;
+  if (block % 32 || block > 128 || p->max_depth < 0) return TPT_ERR_INVALID_ARGUMENT;
+  TPT_CUDA(cudaSetDevice(c->device));
+  std::vector<BatchItem> table(n);
+  std::vector<size_t> pix_off(n + 1, 0);
+  unsigned long long total = 0;
+  for (int k = 0; k < n; k++) {
+    const tpt_batch_item &it = items[k];
+    if (it.slot < 0 || it.slot >= (int32_t)c->slots.size() || !c->slots[it.slot].live) return TPT_ERR_BAD_HANDLE;
+    if (it.width <= 0 || it.height <= 0 || it.spp <= 0 || !it.out_rgb) return TPT_ERR_INVALID_ARGUMENT;
+    const unsigned long long npix = (unsigned long long)it.width * it.height;
+    if (npix > 0x7fffffffull) return TPT_ERR_INVALID_ARGUMENT;
+    pix_off[k + 1] = pix_off[k] + (size_t)npix;
+    table[k].first = total;
+    total += npix * (unsigned long long)it.spp;
+  }
+  tpt_status st;
+  if ((st = ensure(c->batch_accum, pix_off[n] * sizeof(float4))) != TPT_OK) return st;
+  if ((st = ensure(c->batch_table, (size_t)n * sizeof(BatchItem))) != TPT_OK) return st;
+  if (mem == TPT_MEM_HOST && (st = ensure(c->batch_staging, pix_off[n] * 3 * sizeof(float))) != TPT_OK) return st;
+  float4 *acc = (float4 *)c->batch_accum.p;
+  for (int k = 0; k < n; k++) {
+    const tpt_batch_item &it = items[k];
+    table[k].scene = c->slots[it.slot].ds;
+    table[k].scene.flat_max = p->flat_nodes > 0 ? p->flat_nodes : c->flat_nodes;
+    table[k].frame = FrameDesc{it.width, it.height, it.spp, (unsigned long long)it.width * it.height * it.spp,
+                               acc + pix_off[k], nullptr};
+  }
+  const RenderCfg cfg{p->max_depth, p->semantics, p->background, p->sky_scale,
+                      make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32))};
+  uint64_t key = 1469598103934665603ull;
+  key = fnv1a(key, table.data(), table.size() * sizeof(BatchItem));
+  key = fnv1a(key, &cfg, sizeof(cfg));
+  key = fnv1a(key, &block, sizeof(block));
+  key = fnv1a(key, &p->wave, sizeof(p->wave));
+  key = fnv1a(key, &mem, sizeof(mem));
+  for (int k = 0; k < n; k++) key = fnv1a(key, &items[k].out_rgb, sizeof(float *));
+  const BatchKernel kern = batch_variant(p->wave);
+  const int smem = stack_smem(block);
+  if (!c->batch_graph || c->batch_key != key) {
+    if (c->batch_graph) {
+      cudaGraphExecDestroy(c->batch_graph);
+      c->batch_graph = nullptr;
+    }
+    TPT_CUDA(cudaMemcpyAsync(c->batch_table.p, table.data(), (size_t)n * sizeof(BatchItem), cudaMemcpyHostToDevice,
+                             c->stream));
+    TPT_CUDA(cudaStreamSynchronize(c->stream));
+    TPT_CUDA(smem_optin(kern, smem));
+    const int grid = grid_for(c, kern, block, smem);
+    cudaGraph_t graph = nullptr;
+    TPT_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(c->batch_accum.p, 0, pix_off[n] * sizeof(float4), c->stream);
+    cudaMemsetAsync(c->counters, 0, sizeof(WfCounters), c->stream);
+    kern<<<grid, block, smem, c->stream>>>((const BatchItem *)c->batch_table.p, n, total, cfg, c->counters);
+    for (int k = 0; k < n; k++) {
+      const unsigned long long npix = pix_off[k + 1] - pix_off[k];
+      float *dst = mem == TPT_MEM_HOST ? (float *)c->batch_staging.p + 3 * pix_off[k] : items[k].out_rgb;
+      const int rgrid = (int)std::min<unsigned long long>((npix + 255) / 256, (unsigned long long)c->sm_count * 8);
+      k_resolve<<<rgrid, 256, 0, c->stream>>>(table[k].frame, dst);
+    }
+    cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&c->batch_graph, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      c->batch_graph = nullptr;
+      return cuda_status(e);
+    }
+    c->batch_key = key;
+  }
+  TPT_CUDA(cudaEventRecord(c->ev0, c->stream));
+  TPT_CUDA(cudaGraphLaunch(c->batch_graph, c->stream));
+  TPT_CUDA(cudaEventRecord(c->ev1, c->stream));
+  TPT_CUDA(cudaMemcpyAsync(c->counters_host, c->counters, sizeof(WfCounters), cudaMemcpyDeviceToHost, c->stream));
+  if (mem == TPT_MEM_HOST)
+    for (int k = 0; k < n; k++)
+      TPT_CUDA(cudaMemcpyAsync(items[k].out_rgb, (float *)c->batch_staging.p + 3 * pix_off[k],
+                               (pix_off[k + 1] - pix_off[k]) * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  TPT_CUDA(cudaStreamSynchronize(c->stream));
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    stats->device_ms = ms;
+    stats->samples = (int64_t)total;
+    stats->segments = (int64_t)c->counters_host->segments;
+    stats->iterations = 1;
+    stats->kernel_launches = 1 + n;
+    if (p->profile) {
+      stats->traverse_ms = ms;
+      stats->traverse_launches = 1;
+    }
+  }
+  return c->counters_host->err ? (tpt_status)c->counters_host->err : TPT_OK;
+}
+
+// ============================================================= autotuner ==
+extern "C" tpt_status tpt_autotune(tpt_context *c, int32_t slot, tpt_render_params *p, int32_t probe_spp,
+                                   double *best_msps) {
+  if (!c || !p || probe_spp <= 0 || p->width <= 0 || p->height <= 0) return TPT_ERR_INVALID_ARGUMENT;
+  if (slot < 0 || slot >= (int32_t)c->slots.size() || !c->slots[slot].live) return TPT_ERR_BAD_HANDLE;
+  struct Cand {
+    int engine, block, wave, flat;
+  };
+  std::vector<Cand> cands;
+  for (int block : {64, 128})
+    for (int var : {4, 6})
+      for (int flat : {16, 48, 1 << 20}) cands.push_back({TPT_ENGINE_PERSISTENT, block, var, flat});
+  for (int block : {128, 256})
+    for (int wave : {1 << 19, 1 << 20}) cands.push_back({TPT_ENGINE_WAVEFRONT, block, wave, 48});
+  const size_t npix = (size_t)p->width * p->height;
+  tpt_status st;
+  if ((st = ensure(c->staging, npix * 3 * sizeof(float))) != TPT_OK) return st;
+  double best = -1.0;
+  Cand win = cands[0];
+  for (const Cand &cd : cands) {
+    tpt_render_params q = *p;
+    q.engine = cd.engine;
+    q.block = cd.block;
+    q.wave = cd.wave;
+    q.flat_nodes = cd.flat;
+    q.spp = probe_spp;
+    q.profile = 0;
+    q.accumulate_fp64 = 0;
+    tpt_render_stats rs;
+    double t = 0.0;
+    for (int rep = 0; rep < 2; rep++) {  // first run warms caches and allocations
+      st = tpt_render(c, slot, &q, (float *)c->staging.p, TPT_MEM_DEVICE, &rs);
+      if (st != TPT_OK) return st;
+      t = rs.device_ms;
+    }
+    const double msps = (double)npix * probe_spp / (t * 1e3);
+    if (msps > best) {
+      best = msps;
+      win = cd;
+    }
+  }
+  p->engine = win.engine;
+  p->block = win.block;
+  p->wave = win.wave;
+  p->flat_nodes = win.flat;
+  c->slots[slot].tuned = true;
+  c->slots[slot].tp = *p;
+  if (best_msps) *best_msps = best;
   return TPT_OK;
 }
 

@@ -1,0 +1,712 @@
+// learn.cu - training and inference kernels of the learned parts (FP16
+// tensor-core MLPs with FP32 accumulation) and their C ABI.
+//
+// Training step of a batch of `rows` samples (rows a multiple of 16):
+//   k_mlp_train   forward (activations in registers; each layer's input also
+//                 written transposed to Ht), per-row loss gradient dY, and the
+//                 backward pass through the layers (ReLU masks from the saved
+//                 activations, transposed weights in shared memory), writing
+//                 each layer's output gradient transposed to dZt;
+//   k_mlp_wgrad   dW_l = dZt_l * Ht_l^T as a tensor-core GEMM over the batch
+//                 (split into row chunks, f32 atomics into the gradient);
+//   k_adam        Adam on f32 master weights, refreshing the f16 copy.
+// Shapes are template parameters: <IN, NH, OUT> with hidden width 64.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "../../include/tpt.h"
+#include "mlp.cuh"
+
+namespace tpt {
+namespace mlp {
+
+// ------------------------------------------------------------ losses ----
+// Each loss writes dL/dy for one row (already multiplied by `scale`, the
+// loss scale over the batch size) and returns the row's loss.
+struct LossGiven {  // dY supplied by the caller (tests)
+  const float *dy;
+  float scale;
+  template <int OUT>
+  __device__ float grad(int row, const float *y, float *dy_out) const {
+    for (int o = 0; o < OUT; o++) dy_out[o] = dy[(size_t)row * OUT + o] * scale;
+    return 0.f;
+  }
+};
+
+// ------------------------------------------------------------ kernels ---
+template <int IN, int NH, int OUT>
+__global__ void __launch_bounds__(WARPS * 32) k_mlp_forward(Net n, const __half *__restrict__ X, int rows,
+                                                            float *__restrict__ Y) {
+  extern __shared__ __half smem[];
+  load_weights(n, smem, nullptr);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  for (int tile = blockIdx.x * WARPS + warp; tile * 16 < rows; tile += gridDim.x * WARPS) {
+    const int r0 = tile * 16;
+    uint32_t a0[IN / 16][4];
+    load_frag_rows<IN>(X + (size_t)r0 * IN, IN, a0);
+    float acc[HID / 8][4];
+    layer_mma<IN, HID>(a0, smem + smem_w_offset(n, 0), acc);
+    uint32_t h[HID / 16][4];
+    relu_to_frag<HID>(acc, h);
+#pragma unroll
+    for (int l = 1; l < NH; l++) {
+      layer_mma<HID, HID>(h, smem + smem_w_offset(n, l), acc);
+      relu_to_frag<HID>(acc, h);
+    }
+    float out[OUT / 8][4];
+    layer_mma<HID, OUT>(h, smem + smem_w_offset(n, NH), out);
+#pragma unroll
+    for (int j = 0; j < OUT / 8; j++) {
+      float *y0 = Y + (size_t)(r0 + g) * OUT + j * 8 + 2 * t;
+      float *y1 = y0 + 8 * OUT;
+      y0[0] = out[j][0];
+      y0[1] = out[j][1];
+      y1[0] = out[j][2];
+      y1[1] = out[j][3];
+    }
+  }
+}
+
+// Writes the 16 x K block held in A fragments, transposed, into T (row
+// stride `rows`): T[col][r0 + row].
+template <int K>
+__device__ __forceinline__ void store_frag_t(const uint32_t (&a)[K / 16][4], __half *T, int rows, int r0) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int kk = 0; kk < K / 16; kk++) {
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const int row = r0 + g + 8 * (i & 1);
+      const int col = kk * 16 + 2 * t + 8 * (i >> 1);
+      const __half2 v = *reinterpret_cast<const __half2 *>(&a[kk][i]);
+      T[(size_t)col * rows + row] = __low2half(v);
+      T[(size_t)(col + 1) * rows + row] = __high2half(v);
+    }
+  }
+}
+
+template <int IN, int NH, int OUT, class Loss>
+__global__ void __launch_bounds__(WARPS * 32)
+    k_mlp_train(Net n, const __half *__restrict__ X, int rows, Loss loss, __half *__restrict__ Ht,
+                __half *__restrict__ dZt, float *loss_sum) {
+  extern __shared__ __half smem[];
+  __half *sw = smem;
+  __half *swt = sw + smem_w_halves(n);
+  uint32_t *sh = reinterpret_cast<uint32_t *>(swt + smem_wt_halves(n));  // [warp][layer][16][32] h frags
+  float *sy = reinterpret_cast<float *>(sh + WARPS * NH * 16 * 32);      // [warp][16][OUT]
+  float *sdy = sy + WARPS * 16 * OUT;                                     // [warp][16][OUT]
+  load_weights(n, sw, swt);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  uint32_t *my_h = sh + warp * NH * 16 * 32;
+  float *my_y = sy + warp * 16 * OUT, *my_dy = sdy + warp * 16 * OUT;
+  // transposed activation / gradient buffers per layer
+  size_t ht_off[NH + 1], dz_off[NH + 1];
+  {
+    size_t a = 0, b = 0;
+    for (int l = 0; l <= NH; l++) {
+      ht_off[l] = a;
+      dz_off[l] = b;
+      a += (size_t)(l == 0 ? IN : HID) * rows;
+      b += (size_t)(l == NH ? OUT : HID) * rows;
+    }
+  }
+  float lsum = 0.f;
+  for (int tile = blockIdx.x * WARPS + warp; tile * 16 < rows; tile += gridDim.x * WARPS) {
+    const int r0 = tile * 16;
+    // ---- forward
+    uint32_t a0[IN / 16][4];
+    load_frag_rows<IN>(X + (size_t)r0 * IN, IN, a0);
+    store_frag_t<IN>(a0, Ht + ht_off[0], rows, r0);
+    float acc[HID / 8][4];
+    layer_mma<IN, HID>(a0, sw + smem_w_offset(n, 0), acc);
+    uint32_t h[HID / 16][4];
+    relu_to_frag<HID>(acc, h);
+#pragma unroll
+    for (int l = 1; l <= NH; l++) {
+      // h = H_l (input of layer l): keep for the masks and the weight gradient
+#pragma unroll
+      for (int kk = 0; kk < HID / 16; kk++)
+#pragma unroll
+        for (int i = 0; i < 4; i++) my_h[((l - 1) * 16 + kk * 4 + i) * 32 + lane] = h[kk][i];
+      store_frag_t<HID>(h, Ht + ht_off[l], rows, r0);
+      if (l < NH) {
+        layer_mma<HID, HID>(h, sw + smem_w_offset(n, l), acc);
+        relu_to_frag<HID>(acc, h);
+      }
+    }
+    float out[OUT / 8][4];
+    layer_mma<HID, OUT>(h, sw + smem_w_offset(n, NH), out);
+    // ---- loss: rows through shared memory
+#pragma unroll
+    for (int j = 0; j < OUT / 8; j++) {
+      my_y[g * OUT + j * 8 + 2 * t] = out[j][0];
+      my_y[g * OUT + j * 8 + 2 * t + 1] = out[j][1];
+      my_y[(g + 8) * OUT + j * 8 + 2 * t] = out[j][2];
+      my_y[(g + 8) * OUT + j * 8 + 2 * t + 1] = out[j][3];
+    }
+    __syncwarp();
+    if (lane < 16) lsum += loss.template grad<OUT>(r0 + lane, my_y + lane * OUT, my_dy + lane * OUT);
+    __syncwarp();
+    // ---- backward: dZ of the output layer as A fragments (k = output index)
+    uint32_t dz_out[OUT / 16][4];
+#pragma unroll
+    for (int kk = 0; kk < OUT / 16; kk++) {
+      const float *d0 = my_dy + g * OUT + kk * 16 + 2 * t, *d1 = d0 + 8 * OUT;
+      dz_out[kk][0] = pack2(d0[0], d0[1]);
+      dz_out[kk][1] = pack2(d1[0], d1[1]);
+      dz_out[kk][2] = pack2(d0[8], d0[9]);
+      dz_out[kk][3] = pack2(d1[8], d1[9]);
+    }
+    store_frag_t<OUT>(dz_out, dZt + dz_off[NH], rows, r0);
+    // dH_NH = dZ_out * W_out, then through the hidden layers
+    layer_mma<OUT, HID>(dz_out, swt + smem_wt_offset(n, NH), acc);
+    uint32_t dz[HID / 16][4];
+#pragma unroll
+    for (int l = NH - 1; l >= 0; l--) {
+      // mask with H_{l+1} > 0 (the ReLU output of layer l)
+#pragma unroll
+      for (int kk = 0; kk < HID / 16; kk++) {
+        const float2 m0 = unpack2(my_h[(l * 16 + kk * 4 + 0) * 32 + lane]);
+        const float2 m1 = unpack2(my_h[(l * 16 + kk * 4 + 1) * 32 + lane]);
+        const float2 m2 = unpack2(my_h[(l * 16 + kk * 4 + 2) * 32 + lane]);
+        const float2 m3 = unpack2(my_h[(l * 16 + kk * 4 + 3) * 32 + lane]);
+        dz[kk][0] = pack2(m0.x > 0.f ? acc[2 * kk][0] : 0.f, m0.y > 0.f ? acc[2 * kk][1] : 0.f);
+        dz[kk][1] = pack2(m1.x > 0.f ? acc[2 * kk][2] : 0.f, m1.y > 0.f ? acc[2 * kk][3] : 0.f);
+        dz[kk][2] = pack2(m2.x > 0.f ? acc[2 * kk + 1][0] : 0.f, m2.y > 0.f ? acc[2 * kk + 1][1] : 0.f);
+        dz[kk][3] = pack2(m3.x > 0.f ? acc[2 * kk + 1][2] : 0.f, m3.y > 0.f ? acc[2 * kk + 1][3] : 0.f);
+      }
+      store_frag_t<HID>(dz, dZt + dz_off[l], rows, r0);
+      if (l > 0) layer_mma<HID, HID>(dz, swt + smem_wt_offset(n, l), acc);
+    }
+  }
+  if (loss_sum) {
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if (lane == 0) atomicAdd(loss_sum, lsum);
+  }
+}
+
+// dW_l[o][i] += sum over rows r of dZt_l[o][r] * Ht_l[i][r], one warp per
+// (layer, 16-output tile, chunk of `chunk` rows).
+template <int IN, int NH, int OUT>
+__global__ void k_mlp_wgrad(Net n, const __half *__restrict__ Ht, const __half *__restrict__ dZt, int rows,
+                            int chunk) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int warp_global = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int n_chunks = (rows + chunk - 1) / chunk;
+  // enumerate (layer, mtile, chunk)
+  int w = warp_global, layer = -1, mt = 0;
+  size_t ht_off = 0, dz_off = 0;
+  for (int l = 0; l <= NH; l++) {
+    const int N = l == NH ? OUT : HID;
+    const int units = (N / 16) * n_chunks;
+    if (w < units) {
+      layer = l;
+      mt = w / n_chunks;
+      w -= mt * n_chunks;
+      break;
+    }
+    w -= units;
+    ht_off += (size_t)(l == 0 ? IN : HID) * rows;
+    dz_off += (size_t)N * rows;
+  }
+  if (layer < 0) return;
+  const int K = layer == 0 ? IN : HID;  // layer input width (GEMM N dimension)
+  const int ck = w;
+  const int k_begin = ck * chunk, k_end = min(rows, k_begin + chunk);
+  const __half *A = dZt + dz_off + (size_t)(mt * 16) * rows;
+  const __half *B = Ht + ht_off;
+  float acc[MAX_IN / 8][4];
+#pragma unroll
+  for (int j = 0; j < MAX_IN / 8; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+  for (int k0 = k_begin; k0 < k_end; k0 += 16) {
+    const __half *ra = A + (size_t)g * rows + k0 + 2 * t;
+    const uint32_t a0 = *reinterpret_cast<const uint32_t *>(ra);
+    const uint32_t a1 = *reinterpret_cast<const uint32_t *>(ra + 8 * (size_t)rows);
+    const uint32_t a2 = *reinterpret_cast<const uint32_t *>(ra + 8);
+    const uint32_t a3 = *reinterpret_cast<const uint32_t *>(ra + 8 * (size_t)rows + 8);
+#pragma unroll
+    for (int j = 0; j < MAX_IN / 8; j++) {
+      if (j < K / 8) {
+        const __half *rb = B + (size_t)(j * 8 + g) * rows + k0 + 2 * t;
+        mma16816(acc[j], a0, a1, a2, a3, *reinterpret_cast<const uint32_t *>(rb),
+                 *reinterpret_cast<const uint32_t *>(rb + 8));
+      }
+    }
+  }
+  float *G = n.grad + layer_offset(n, layer);
+#pragma unroll
+  for (int j = 0; j < MAX_IN / 8; j++) {
+    if (j < K / 8) {
+      const int o0 = mt * 16 + g, i0 = j * 8 + 2 * t;
+      atomicAdd(G + (size_t)o0 * K + i0, acc[j][0]);
+      atomicAdd(G + (size_t)o0 * K + i0 + 1, acc[j][1]);
+      atomicAdd(G + (size_t)(o0 + 8) * K + i0, acc[j][2]);
+      atomicAdd(G + (size_t)(o0 + 8) * K + i0 + 1, acc[j][3]);
+    }
+  }
+}
+
+// Adam (Kingma & Ba, ICLR 2015) on the f32 master weights; the gradient is
+// divided by the loss scale first and cleared afterwards.
+__global__ void k_adam(int count, float *__restrict__ w32, __half *__restrict__ w16, float *__restrict__ grad,
+                       float *__restrict__ m, float *__restrict__ v, float lr, float b1, float b2, float eps,
+                       float inv_scale, float bc1, float bc2) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    const float gr = grad[i] * inv_scale;
+    const float mi = b1 * m[i] + (1.f - b1) * gr;
+    const float vi = b2 * v[i] + (1.f - b2) * gr * gr;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w32[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+    w32[i] = wi;
+    w16[i] = __float2half_rn(wi);
+    grad[i] = 0.f;
+  }
+}
+
+// ------------------------------------------------------- path guiding ---
+// Network input: one-blob encoding of the position normalised to the scene
+// box (3 axes x 32 bins, triangle kernel of one bin width; Mueller et al.,
+// "Neural Importance Sampling", ACM TOG 2019) and the surface normal; 99
+// values padded to 112.  Output: 8 lobes x (weight logit, kappa
+// pre-activation, mean direction xyz), 40 values padded to 48.
+constexpr int GUIDE_IN = 112, GUIDE_NH = 3, GUIDE_OUT = 48, GUIDE_LOBES = 8, BLOB_BINS = 32;
+
+__device__ __forceinline__ void guide_encode(float3 xn, float3 n, __half *out) {
+  const float c[3] = {xn.x, xn.y, xn.z};
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const float u = fminf(fmaxf(c[a], 0.f), 1.f) * BLOB_BINS;
+    for (int b = 0; b < BLOB_BINS; b++) out[a * BLOB_BINS + b] = __float2half_rn(fmaxf(0.f, 1.f - fabsf(u - (b + 0.5f))));
+  }
+  out[96] = __float2half_rn(n.x);
+  out[97] = __float2half_rn(n.y);
+  out[98] = __float2half_rn(n.z);
+  for (int i = 99; i < GUIDE_IN; i++) out[i] = __float2half_rn(0.f);
+}
+
+// Weighted maximum likelihood of the vMF mixture: loss = -w log q(omega);
+// gradient as in oracle/mlp_ref.py vmf_nll_grad.
+struct LossVmf {
+  const float4 *target;  // (omega.xyz, weight)
+  float scale;
+  template <int OUT>
+  __device__ float grad(int row, const float *y, float *dy) const {
+    const float4 tg = target[row];
+    const float3 w = make_float3(tg.x, tg.y, tg.z);
+    float logit[GUIDE_LOBES], kap[GUIDE_LOBES], cs[GUIDE_LOBES], f[GUIDE_LOBES], mn[GUIDE_LOBES];
+    float3 mu[GUIDE_LOBES];
+    float lmax = -1e30f;
+    for (int i = 0; i < GUIDE_LOBES; i++) lmax = fmaxf(lmax, y[5 * i]);
+    float zsum = 0.f;
+    for (int i = 0; i < GUIDE_LOBES; i++) {
+      logit[i] = __expf(y[5 * i] - lmax);
+      zsum += logit[i];
+      const float kp = y[5 * i + 1];
+      kap[i] = (kp > 20.f ? kp : log1pf(__expf(kp))) + 1e-2f;
+      const float3 m = make_float3(y[5 * i + 2], y[5 * i + 3], y[5 * i + 4]);
+      mn[i] = fmaxf(sqrtf(m.x * m.x + m.y * m.y + m.z * m.z), 1e-12f);
+      mu[i] = make_float3(m.x / mn[i], m.y / mn[i], m.z / mn[i]);
+      cs[i] = mu[i].x * w.x + mu[i].y * w.y + mu[i].z * w.z;
+    }
+    float p = 0.f;
+    for (int i = 0; i < GUIDE_LOBES; i++) {
+      logit[i] /= zsum;  // pi
+      const float e2 = __expf(-2.f * kap[i]);
+      f[i] = kap[i] / (6.28318530717958647692f * (1.f - e2)) * __expf(kap[i] * (cs[i] - 1.f));
+      p += logit[i] * f[i];
+    }
+    p = fmaxf(p, 1e-30f);
+    const float wt = tg.w * scale;
+    for (int i = 0; i < GUIDE_LOBES; i++) {
+      const float r = logit[i] * f[i] / p;
+      const float e2 = __expf(-2.f * kap[i]);
+      dy[5 * i] = wt * (logit[i] - r);
+      const float dlk = 1.f / kap[i] - 2.f * e2 / (1.f - e2) + (cs[i] - 1.f);
+      dy[5 * i + 1] = wt * (-r * dlk / (1.f + __expf(-y[5 * i + 1])));
+      const float k = -r * kap[i] / mn[i];
+      dy[5 * i + 2] = wt * k * (w.x - cs[i] * mu[i].x);
+      dy[5 * i + 3] = wt * k * (w.y - cs[i] * mu[i].y);
+      dy[5 * i + 4] = wt * k * (w.z - cs[i] * mu[i].z);
+    }
+    for (int o = 5 * GUIDE_LOBES; o < OUT; o++) dy[o] = 0.f;
+    return -tg.w * logf(p);
+  }
+};
+
+// Training rows: a random record per row (with replacement), encoded.
+__global__ void k_guide_encode_records(const float4 *__restrict__ rec, int count, int rows, uint2 key, uint32_t step,
+                                       float3 lo, float3 inv_ext, __half *__restrict__ X, float4 *__restrict__ target) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+    uint32_t h = (uint32_t)r * 0x9E3779B1u ^ (step * 0x85EBCA77u) ^ key.x;
+    h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12; h *= 0x297A2D39u; h ^= h >> 15;
+    const int idx = (int)(h % (uint32_t)count);
+    const float4 xw = rec[3 * idx], nn = rec[3 * idx + 1], dd = rec[3 * idx + 2];
+    const float3 xn = make_float3((xw.x - lo.x) * inv_ext.x, (xw.y - lo.y) * inv_ext.y, (xw.z - lo.z) * inv_ext.z);
+    guide_encode(xn, make_float3(nn.x, nn.y, nn.z), X + (size_t)r * GUIDE_IN);
+    target[r] = make_float4(dd.x, dd.y, dd.z, xw.w);
+  }
+}
+
+// Grid rows: cell centres x 6 axis normals (+x,-x,+y,-y,+z,-z).
+__global__ void k_guide_encode_grid(int res, int rows_valid, int rows, __half *__restrict__ X) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+    __half *out = X + (size_t)r * GUIDE_IN;
+    if (r >= rows_valid) {
+      for (int i = 0; i < GUIDE_IN; i++) out[i] = __float2half_rn(0.f);
+      continue;
+    }
+    const int bin = r % 6, cell = r / 6;
+    const int cx = cell % res, cy = (cell / res) % res, cz = cell / (res * res);
+    const float3 xn = make_float3((cx + 0.5f) / res, (cy + 0.5f) / res, (cz + 0.5f) / res);
+    const float sgn = (bin & 1) ? -1.f : 1.f;
+    const float3 n = make_float3(bin / 2 == 0 ? sgn : 0.f, bin / 2 == 1 ? sgn : 0.f, bin / 2 == 2 ? sgn : 0.f);
+    guide_encode(xn, n, out);
+  }
+}
+
+// Network outputs -> lobe table: per row 8 lobes x 2 float4:
+// {mu.xyz, kappa}, {pi, kappa / (2 pi (1 - exp(-2 kappa))), exp(-2 kappa), 0}.
+__global__ void k_guide_post(const float *__restrict__ Y, int rows_valid, float4 *__restrict__ lobes) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows_valid; r += gridDim.x * blockDim.x) {
+    const float *y = Y + (size_t)r * GUIDE_OUT;
+    float lmax = -1e30f;
+    for (int i = 0; i < GUIDE_LOBES; i++) lmax = fmaxf(lmax, y[5 * i]);
+    float e[GUIDE_LOBES], z = 0.f;
+    for (int i = 0; i < GUIDE_LOBES; i++) {
+      e[i] = __expf(y[5 * i] - lmax);
+      z += e[i];
+    }
+    for (int i = 0; i < GUIDE_LOBES; i++) {
+      const float kp = y[5 * i + 1];
+      const float k = (kp > 20.f ? kp : log1pf(__expf(kp))) + 1e-2f;
+      float mx = y[5 * i + 2], my = y[5 * i + 3], mz = y[5 * i + 4];
+      const float mnorm = fmaxf(sqrtf(mx * mx + my * my + mz * mz), 1e-12f);
+      const float e2 = __expf(-2.f * k);
+      lobes[(size_t)r * 2 * GUIDE_LOBES + 2 * i] = make_float4(mx / mnorm, my / mnorm, mz / mnorm, k);
+      lobes[(size_t)r * 2 * GUIDE_LOBES + 2 * i + 1] =
+          make_float4(e[i] / z, k / (6.28318530717958647692f * (1.f - e2)), e2, 0.f);
+    }
+  }
+}
+
+}  // namespace mlp
+}  // namespace tpt
+
+using namespace tpt;
+using namespace tpt::mlp;
+
+// ================================================================ C ABI ===
+struct tpt_mlp {
+  int device = 0;
+  Net net{};
+  int in_dim = 0, n_hidden = 0, out_dim = 0;
+  int params = 0;
+  float *w32 = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
+  __half *w16 = nullptr;
+  __half *ht = nullptr, *dzt = nullptr;
+  float *loss = nullptr;
+  int ws_rows = 0;
+  int steps = 0;
+};
+
+namespace {
+
+thread_local char g_mlp_err[256] = "";
+
+tpt_status mlp_cuda(cudaError_t e) {
+  if (e == cudaSuccess) return TPT_OK;
+  std::snprintf(g_mlp_err, sizeof(g_mlp_err), "%s", cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? TPT_ERR_OUT_OF_MEMORY : TPT_ERR_CUDA;
+}
+#define MLP_CUDA(x)                                  \
+  do {                                               \
+    cudaError_t e_ = (x);                            \
+    if (e_ != cudaSuccess) return mlp_cuda(e_);      \
+  } while (0)
+
+bool supported(int in, int nh, int out) {
+  return (in == 112 && nh == 3 && out == 48) || (in == 64 && nh == 5 && out == 16) || (in == 32 && nh == 2 && out == 16);
+}
+
+size_t train_smem(const Net &n) {
+  return (size_t)(smem_w_halves(n) + smem_wt_halves(n)) * 2 + (size_t)WARPS * n.n_hidden * 16 * 32 * 4 +
+         (size_t)2 * WARPS * 16 * n.out_dim * 4;
+}
+
+template <int IN, int NH, int OUT>
+tpt_status launch_forward(tpt_mlp *M, const __half *x, int rows, float *y, cudaStream_t s) {
+  const size_t smem = (size_t)smem_w_halves(M->net) * 2;
+  MLP_CUDA(cudaFuncSetAttribute(k_mlp_forward<IN, NH, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, M->device);
+  const int tiles = rows / 16;
+  int grid = (tiles + WARPS - 1) / WARPS;
+  if (grid > sms * 4) grid = sms * 4;
+  if (grid < 1) grid = 1;
+  k_mlp_forward<IN, NH, OUT><<<grid, WARPS * 32, smem, s>>>(M->net, x, rows, y);
+  return mlp_cuda(cudaGetLastError());
+}
+
+template <int IN, int NH, int OUT, class Loss>
+tpt_status launch_train(tpt_mlp *M, const __half *x, int rows, const Loss &loss, cudaStream_t s) {
+  const size_t smem = train_smem(M->net);
+  MLP_CUDA(cudaFuncSetAttribute(k_mlp_train<IN, NH, OUT, Loss>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, M->device);
+  const int tiles = rows / 16;
+  int grid = (tiles + WARPS - 1) / WARPS;
+  if (grid > sms * 2) grid = sms * 2;
+  if (grid < 1) grid = 1;
+  MLP_CUDA(cudaMemsetAsync(M->loss, 0, sizeof(float), s));
+  k_mlp_train<IN, NH, OUT, Loss><<<grid, WARPS * 32, smem, s>>>(M->net, x, rows, loss, M->ht, M->dzt, M->loss);
+  MLP_CUDA(cudaGetLastError());
+  const int chunk = 512;
+  const int n_chunks = (rows + chunk - 1) / chunk;
+  int units = 0;
+  for (int l = 0; l <= NH; l++) units += ((l == NH ? OUT : HID) / 16) * n_chunks;
+  k_mlp_wgrad<IN, NH, OUT><<<(units + 3) / 4, 128, 0, s>>>(M->net, M->ht, M->dzt, rows, chunk);
+  return mlp_cuda(cudaGetLastError());
+}
+
+tpt_status ensure_ws(tpt_mlp *M, int rows) {
+  if (rows <= M->ws_rows) return TPT_OK;
+  if (M->ht) cudaFree(M->ht);
+  if (M->dzt) cudaFree(M->dzt);
+  M->ht = M->dzt = nullptr;
+  const size_t hh = (size_t)(M->in_dim + M->n_hidden * HID) * rows;
+  const size_t dd = (size_t)(M->n_hidden * HID + M->out_dim) * rows;
+  MLP_CUDA(cudaMalloc(&M->ht, hh * sizeof(__half)));
+  MLP_CUDA(cudaMalloc(&M->dzt, dd * sizeof(__half)));
+  M->ws_rows = rows;
+  return TPT_OK;
+}
+
+}  // namespace
+
+namespace tpt {
+
+// Guiding network state used by the guided renderer (kernels.cu).
+struct GuideNet {
+  tpt_mlp *net = nullptr;
+  __half *x = nullptr;
+  float *y = nullptr;
+  float4 *target = nullptr;
+  int cap_rows = 0;
+  float last_loss = 0.f;
+};
+
+static tpt_status guide_ws(GuideNet *G, int rows) {
+  if (rows <= G->cap_rows) return TPT_OK;
+  if (G->x) cudaFree(G->x);
+  if (G->y) cudaFree(G->y);
+  if (G->target) cudaFree(G->target);
+  G->x = nullptr;
+  G->y = nullptr;
+  G->target = nullptr;
+  MLP_CUDA(cudaMalloc(&G->x, (size_t)rows * GUIDE_IN * sizeof(__half)));
+  MLP_CUDA(cudaMalloc(&G->y, (size_t)rows * GUIDE_OUT * sizeof(float)));
+  MLP_CUDA(cudaMalloc(&G->target, (size_t)rows * sizeof(float4)));
+  G->cap_rows = rows;
+  return TPT_OK;
+}
+
+tpt_status guide_create(int device, uint64_t seed, GuideNet **out) {
+  auto *G = new GuideNet();
+  tpt_status st = tpt_mlp_create(device, GUIDE_IN, GUIDE_NH, GUIDE_OUT, seed, &G->net);
+  if (st != TPT_OK) {
+    delete G;
+    return st;
+  }
+  *out = G;
+  return TPT_OK;
+}
+
+void guide_destroy(GuideNet *G) {
+  if (!G) return;
+  tpt_mlp_destroy(G->net);
+  if (G->x) cudaFree(G->x);
+  if (G->y) cudaFree(G->y);
+  if (G->target) cudaFree(G->target);
+  delete G;
+}
+
+// `steps` Adam steps on batches of `batch` records drawn from rec[0, count).
+tpt_status guide_train(GuideNet *G, const float4 *rec, int count, int steps, int batch, float lr, float3 lo,
+                       float3 ext, uint64_t seed, cudaStream_t s) {
+  if (count <= 0 || steps <= 0) return TPT_OK;
+  batch = (batch + 15) / 16 * 16;
+  tpt_status st = guide_ws(G, batch);
+  if (st != TPT_OK) return st;
+  if ((st = ensure_ws(G->net, batch)) != TPT_OK) return st;
+  const float3 inv = make_float3(1.f / ext.x, 1.f / ext.y, 1.f / ext.z);
+  const float loss_scale = 1024.f;
+  for (int k = 0; k < steps; k++) {
+    k_guide_encode_records<<<(batch + 255) / 256, 256, 0, s>>>(
+        rec, count, batch, make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)), (uint32_t)(G->net->steps + 1), lo,
+        inv, G->x, G->target);
+    LossVmf L{G->target, loss_scale / (float)batch};
+    st = launch_train<GUIDE_IN, GUIDE_NH, GUIDE_OUT>(G->net, G->x, batch, L, s);
+    if (st != TPT_OK) return st;
+    st = tpt_mlp_adam(G->net, lr, 1.f / loss_scale, s);
+    if (st != TPT_OK) return st;
+  }
+  float l = 0.f;
+  MLP_CUDA(cudaMemcpyAsync(&l, G->net->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+  MLP_CUDA(cudaStreamSynchronize(s));
+  G->last_loss = l / (float)batch;
+  return TPT_OK;
+}
+
+// Evaluates the network at every (cell, normal bin) of a res^3 grid and
+// writes the lobe table (res^3 * 6 * 8 * 2 float4).
+tpt_status guide_refresh(GuideNet *G, int res, float4 *table, cudaStream_t s) {
+  const int valid = res * res * res * 6;
+  const int rows = (valid + 15) / 16 * 16;
+  tpt_status st = guide_ws(G, rows);
+  if (st != TPT_OK) return st;
+  k_guide_encode_grid<<<(rows + 255) / 256, 256, 0, s>>>(res, valid, rows, G->x);
+  st = launch_forward<GUIDE_IN, GUIDE_NH, GUIDE_OUT>(G->net, G->x, rows, G->y, s);
+  if (st != TPT_OK) return st;
+  k_guide_post<<<(valid + 255) / 256, 256, 0, s>>>(G->y, valid, table);
+  return mlp_cuda(cudaGetLastError());
+}
+
+float guide_last_loss(const GuideNet *G) { return G->last_loss; }
+
+}  // namespace tpt
+
+extern "C" {
+
+const char *tpt_mlp_last_error(void) { return g_mlp_err; }
+
+tpt_status tpt_mlp_create(int32_t device, int32_t in_dim, int32_t n_hidden, int32_t out_dim, uint64_t seed,
+                          tpt_mlp **out) {
+  if (!out || !supported(in_dim, n_hidden, out_dim)) return TPT_ERR_INVALID_ARGUMENT;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return TPT_ERR_NO_DEVICE;
+  MLP_CUDA(cudaSetDevice(device));
+  auto *M = new tpt_mlp();
+  M->device = device;
+  M->in_dim = in_dim;
+  M->n_hidden = n_hidden;
+  M->out_dim = out_dim;
+  M->net = Net{in_dim, n_hidden, out_dim, nullptr, nullptr};
+  M->params = param_count(M->net);
+  const size_t P = (size_t)M->params;
+  cudaError_t e = cudaMalloc(&M->w32, P * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&M->grad, P * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&M->m, P * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&M->v, P * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&M->w16, P * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&M->loss, 4);
+  if (e != cudaSuccess) {
+    tpt_mlp_destroy(M);
+    return mlp_cuda(e);
+  }
+  M->net.w16 = M->w16;
+  M->net.grad = M->grad;
+  // He-uniform initialisation from a seeded engine
+  std::vector<float> w(P);
+  std::mt19937_64 rng(seed);
+  for (int l = 0; l <= n_hidden; l++) {
+    const int K = layer_in(M->net, l), N = layer_out(M->net, l);
+    const float lim = std::sqrt(6.0f / (float)K);
+    std::uniform_real_distribution<float> U(-lim, lim);
+    float *p = w.data() + layer_offset(M->net, l);
+    for (int i = 0; i < N * K; i++) p[i] = U(rng);
+  }
+  *out = M;
+  tpt_status st = tpt_mlp_set_params(M, w.data());
+  if (st != TPT_OK) {
+    tpt_mlp_destroy(M);
+    *out = nullptr;
+  }
+  return st;
+}
+
+void tpt_mlp_destroy(tpt_mlp *M) {
+  if (!M) return;
+  cudaSetDevice(M->device);
+  void *ptrs[] = {M->w32, M->grad, M->m, M->v, M->w16, M->ht, M->dzt, M->loss};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  delete M;
+}
+
+int64_t tpt_mlp_param_count(const tpt_mlp *M) { return M ? M->params : -1; }
+
+tpt_status tpt_mlp_set_params(tpt_mlp *M, const float *host) {
+  if (!M || !host) return TPT_ERR_INVALID_ARGUMENT;
+  MLP_CUDA(cudaSetDevice(M->device));
+  const size_t P = (size_t)M->params;
+  std::vector<__half> h(P);
+  for (size_t i = 0; i < P; i++) h[i] = __float2half_rn(host[i]);
+  MLP_CUDA(cudaMemcpy(M->w32, host, P * 4, cudaMemcpyHostToDevice));
+  MLP_CUDA(cudaMemcpy(M->w16, h.data(), P * 2, cudaMemcpyHostToDevice));
+  MLP_CUDA(cudaMemset(M->grad, 0, P * 4));
+  MLP_CUDA(cudaMemset(M->m, 0, P * 4));
+  MLP_CUDA(cudaMemset(M->v, 0, P * 4));
+  M->steps = 0;
+  return TPT_OK;
+}
+
+tpt_status tpt_mlp_get_params(const tpt_mlp *M, float *host) {
+  if (!M || !host) return TPT_ERR_INVALID_ARGUMENT;
+  MLP_CUDA(cudaSetDevice(M->device));
+  MLP_CUDA(cudaMemcpy(host, M->w32, (size_t)M->params * 4, cudaMemcpyDeviceToHost));
+  return TPT_OK;
+}
+
+tpt_status tpt_mlp_get_grad(const tpt_mlp *M, float *host) {
+  if (!M || !host) return TPT_ERR_INVALID_ARGUMENT;
+  MLP_CUDA(cudaSetDevice(M->device));
+  MLP_CUDA(cudaMemcpy(host, M->grad, (size_t)M->params * 4, cudaMemcpyDeviceToHost));
+  return TPT_OK;
+}
+
+tpt_status tpt_mlp_forward(tpt_mlp *M, const void *x_f16, int64_t rows, float *y, void *stream) {
+  if (!M || !x_f16 || !y || rows <= 0 || rows % 16 || rows > (1 << 28)) return TPT_ERR_INVALID_ARGUMENT;
+  MLP_CUDA(cudaSetDevice(M->device));
+  cudaStream_t s = (cudaStream_t)stream;
+  const __half *x = (const __half *)x_f16;
+  if (M->in_dim == 112) return launch_forward<112, 3, 48>(M, x, (int)rows, y, s);
+  if (M->in_dim == 64) return launch_forward<64, 5, 16>(M, x, (int)rows, y, s);
+  return launch_forward<32, 2, 16>(M, x, (int)rows, y, s);
+}
+
+tpt_status tpt_mlp_backward_given(tpt_mlp *M, const void *x_f16, const float *dy, int64_t rows, float scale,
+                                  void *stream) {
+  if (!M || !x_f16 || !dy || rows <= 0 || rows % 16 || rows > (1 << 26)) return TPT_ERR_INVALID_ARGUMENT;
+  MLP_CUDA(cudaSetDevice(M->device));
+  tpt_status st = ensure_ws(M, (int)rows);
+  if (st != TPT_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const __half *x = (const __half *)x_f16;
+  LossGiven L{dy, scale};
+  if (M->in_dim == 112) return launch_train<112, 3, 48>(M, x, (int)rows, L, s);
+  if (M->in_dim == 64) return launch_train<64, 5, 16>(M, x, (int)rows, L, s);
+  return launch_train<32, 2, 16>(M, x, (int)rows, L, s);
+}
+
+tpt_status tpt_mlp_adam(tpt_mlp *M, float lr, float inv_loss_scale, void *stream) {
+  if (!M) return TPT_ERR_INVALID_ARGUMENT;
+  MLP_CUDA(cudaSetDevice(M->device));
+  M->steps++;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float bc1 = 1.f - std::pow(b1, (float)M->steps), bc2 = 1.f - std::pow(b2, (float)M->steps);
+  k_adam<<<(M->params + 255) / 256, 256, 0, (cudaStream_t)stream>>>(M->params, M->w32, M->w16, M->grad, M->m, M->v,
+                                                                     lr, b1, b2, 1e-8f, inv_loss_scale, bc1, bc2);
+  return mlp_cuda(cudaGetLastError());
+}
+
+}  // extern "C"

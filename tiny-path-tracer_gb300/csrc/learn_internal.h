@@ -1,0 +1,18 @@
+// learn_internal.h - host interface between the renderer (kernels.cu) and
+// the learned parts (learn.cu).
+#ifndef TPT_LEARN_INTERNAL_H
+#define TPT_LEARN_INTERNAL_H
+#include <cuda_runtime.h>
+
+#include "../../include/tpt.h"
+
+namespace tpt {
+struct GuideNet;
+tpt_status guide_create(int device, uint64_t seed, GuideNet **out);
+void guide_destroy(GuideNet *g);
+tpt_status guide_train(GuideNet *g, const float4 *records, int count, int steps, int batch, float lr, float3 lo,
+                       float3 ext, uint64_t seed, cudaStream_t s);
+tpt_status guide_refresh(GuideNet *g, int res, float4 *table, cudaStream_t s);
+float guide_last_loss(const GuideNet *g);
+}  // namespace tpt
+#endif

@@ -56,6 +56,11 @@ class RenderStats(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("slot", C.c_int32), ("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32),
+                ("out_rgb", C.c_void_p)]
+
+
 class SceneInfo(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("n_nodes", "n_leaves", "n_items", "n_blas", "n_materials",
                                          "n_textures", "n_lights", "max_stack")] + [("arena_bytes", C.c_int64)]
@@ -114,6 +119,21 @@ _SIGS = {
                                C.POINTER(RenderStats)]),
     "tpt_render_noalloc": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(RenderParams), C.c_void_p,
                                        C.c_void_p]),
+    "tpt_render_batch": (C.c_int32, [C.c_void_p, C.POINTER(BatchItem), C.c_int32, C.POINTER(RenderParams),
+                                     C.c_int32, C.POINTER(RenderStats)]),
+    "tpt_autotune": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.c_int32,
+                                 C.POINTER(C.c_double)]),
+    "tpt_mlp_create": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_void_p]),
+    "tpt_mlp_destroy": (None, [C.c_void_p]),
+    "tpt_mlp_param_count": (C.c_int64, [C.c_void_p]),
+    "tpt_mlp_set_params": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "tpt_mlp_get_params": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "tpt_mlp_get_grad": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "tpt_mlp_forward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "tpt_mlp_backward_given": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float,
+                                           C.c_void_p]),
+    "tpt_mlp_adam": (C.c_int32, [C.c_void_p, C.c_float, C.c_float, C.c_void_p]),
+    "tpt_mlp_last_error": (C.c_char_p, []),
     "tpt_quantize": (None, [C.c_void_p, C.c_int64, C.c_void_p]),
     "tpt_write_ppm": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int32, C.c_int32]),
 }
@@ -244,6 +264,38 @@ class Context:
         return None, st.as_dict()
 
 
+def render_batch(ctx: "Context", jobs, max_depth=50, semantics=SEMANTICS_REFERENCE, background=BACKGROUND_BLACK,
+                 sky_scale=1.0, seed=1, block=0, variant=0, flat_nodes=0, profile=False, outs=None):
+    """jobs: list of (slot, width, height, spp).  outs: None -> host images are
+    returned; else a list of device pointers (one per job)."""
+    n = len(jobs)
+    arr = (BatchItem * n)()
+    host = outs is None
+    imgs = []
+    for k, (slot, w, h, spp) in enumerate(jobs):
+        if host:
+            img = np.zeros((h, w, 3), np.float32)
+            imgs.append(img)
+            ptr = img.ctypes.data
+        else:
+            ptr = int(outs[k])
+        arr[k] = BatchItem(slot, w, h, spp, ptr)
+    p = make_params(1, 1, 1, max_depth, semantics, background, sky_scale, seed, ENGINE_PERSISTENT, block, variant,
+                    False, profile, flat_nodes)
+    st = RenderStats()
+    check(lib().tpt_render_batch(ctx._h, arr, n, C.byref(p), TPT_MEM_HOST if host else TPT_MEM_DEVICE,
+                                 C.byref(st)), "render_batch")
+    return (imgs if host else None), st.as_dict()
+
+
+def autotune(ctx: "Context", slot: int, width: int, height: int, probe_spp: int = 4, **kw):
+    """Runs tpt_autotune; returns (engine, block, wave, flat_nodes, Msamples/s)."""
+    p = make_params(width, height, probe_spp, **kw)
+    best = C.c_double()
+    check(lib().tpt_autotune(ctx._h, slot, C.byref(p), probe_spp, C.byref(best)), "autotune")
+    return p.engine, p.block, p.wave, p.flat_nodes, best.value
+
+
 def make_params(width, height, spp, max_depth=50, semantics=0, background=0, sky_scale=1.0, seed=1, engine=0,
                 block=0, wave=0, fp64=False, profile=False, flat_nodes=0) -> RenderParams:
     p = RenderParams()
@@ -266,6 +318,49 @@ def quantize(mean_rgb: np.ndarray) -> np.ndarray:
 def write_ppm(path: str, rgb8: np.ndarray) -> None:
     h, w, _ = rgb8.shape
     check(lib().tpt_write_ppm(path.encode(), _ptr(np.ascontiguousarray(rgb8)), w, h), "write_ppm")
+
+
+class Mlp:
+    """A tensor-core MLP of the learned parts (device buffers via torch)."""
+
+    def __init__(self, in_dim: int, n_hidden: int, out_dim: int, seed: int = 1, device: int = 0):
+        h = C.c_void_p()
+        check(lib().tpt_mlp_create(device, in_dim, n_hidden, out_dim, seed, C.byref(h)), "mlp_create")
+        self._h = h
+        self.shape = (in_dim, n_hidden, out_dim)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.tpt_mlp_destroy(self._h)
+            self._h = None
+
+    @property
+    def n_params(self) -> int:
+        return int(lib().tpt_mlp_param_count(self._h))
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.n_params, np.float32)
+        check(lib().tpt_mlp_get_params(self._h, _ptr(p)))
+        return p
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        check(lib().tpt_mlp_set_params(self._h, _ptr(p)))
+
+    def get_grad(self) -> np.ndarray:
+        g = np.zeros(self.n_params, np.float32)
+        check(lib().tpt_mlp_get_grad(self._h, _ptr(g)))
+        return g
+
+    def forward(self, x_f16_ptr: int, rows: int, y_ptr: int) -> None:
+        check(lib().tpt_mlp_forward(self._h, C.c_void_p(x_f16_ptr), rows, C.c_void_p(y_ptr), None), "mlp_forward")
+
+    def backward_given(self, x_f16_ptr: int, dy_ptr: int, rows: int, scale: float = 1.0) -> None:
+        check(lib().tpt_mlp_backward_given(self._h, C.c_void_p(x_f16_ptr), C.c_void_p(dy_ptr), rows, scale, None),
+              "mlp_backward")
+
+    def adam(self, lr: float, inv_loss_scale: float = 1.0) -> None:
+        check(lib().tpt_mlp_adam(self._h, lr, inv_loss_scale, None), "mlp_adam")
 
 
 def exported_symbols() -> list[str]:
