@@ -288,10 +288,78 @@ tpt_status tpt_mlp_forward(tpt_mlp *m, const void *x_f16, int64_t rows, float *y
 /* Accumulates the weight gradient of sum(scale * dy * y) (dy: f32 [rows][out]). */
 tpt_status tpt_mlp_backward_given(tpt_mlp *m, const void *x_f16, const float *dy, int64_t rows, float scale,
                                   void *stream);
+/* Guiding network only: accumulates the weight gradient of the weighted vMF
+ * mixture negative log-likelihood, sum_rows w * -log q(omega), times `scale`;
+ * target: f32 [rows][4] = (omega.xyz unit, w).  loss_out (host, may be NULL)
+ * receives the unscaled loss sum. */
+tpt_status tpt_mlp_backward_vmf(tpt_mlp *m, const void *x_f16, const float *target, int64_t rows, float scale,
+                                float *loss_out, void *stream);
 /* Adam step (lr, beta 0.9/0.999, eps 1e-8) on the accumulated gradient
  * multiplied by inv_loss_scale; clears the gradient. */
 tpt_status tpt_mlp_adam(tpt_mlp *m, float lr, float inv_loss_scale, void *stream);
 const char *tpt_mlp_last_error(void);
+
+/* Learned path guiding (no counterpart in the reference).  The image is
+ * rendered in `passes` passes of spp/passes samples per pixel; after each
+ * pass the guiding network (one-blob position + normal -> 8-lobe vMF mixture,
+ * shape (112, 3, 48)) takes `train_steps` Adam steps on records of the
+ * paths' first diffuse vertices (position, normal, sampled direction,
+ * weight = the sample's contribution f L cos / pdf), and is then evaluated on
+ * a grid_res^3 x 6-normal table.  From the second pass on, diffuse vertices
+ * sample the table's mixture with probability alpha and the plain mixture
+ * (light + cosine) otherwise, weighting by the one-sample MIS density
+ * alpha q + (1 - alpha) p_plain, so the estimator stays unbiased.  Requires
+ * TPT_SEMANTICS_PHYSICAL.  out_rgb as tpt_render. */
+typedef struct {
+  int32_t passes;       /* >= 1 */
+  int32_t train_steps;  /* Adam steps after each pass */
+  int32_t batch;        /* training rows per step (multiple of 16) */
+  float lr;             /* Adam learning rate (1e-3) */
+  int32_t grid_res;     /* table cells per axis (16) */
+  float alpha;          /* guide probability at a diffuse vertex (0.5) */
+  int32_t record_cap;   /* training records kept per pass */
+  uint64_t seed;        /* network initialisation and record sampling */
+} tpt_guide_params;
+typedef struct {
+  double render_ms, train_ms;  /* device time spent rendering / training + table refresh */
+  float final_loss;            /* mean training loss of the last step */
+  int64_t records;             /* training records collected (all passes) */
+} tpt_guide_stats;
+void tpt_guide_params_default(tpt_guide_params *g);
+tpt_status tpt_render_guided(tpt_context *ctx, int32_t slot, const tpt_render_params *p, const tpt_guide_params *g,
+                             float *out_rgb, int32_t mem, tpt_render_stats *stats, tpt_guide_stats *gstats);
+
+/* Neural radiance cache (no counterpart in the reference).  Rendered in
+ * `passes` passes; in every pass after the first, a path that reaches its
+ * vertex number terminate_depth (0 = camera hit) stops there and adds
+ * throughput x cache(position, outgoing direction, normal, albedo,
+ * roughness), the cache being an MLP of shape (64, 5, 16) evaluated on the
+ * tensor cores for all such vertices at once.  Every train_stride-th path is
+ * a training path: it is traced to full depth (contributing its unbiased
+ * estimate) and records its first vertices with their measured outgoing
+ * radiance; after each pass the cache takes train_steps Adam steps on them
+ * (relative L2 loss).  The first pass traces every path to full depth.
+ * The estimator is biased by the cache's error; the plain tracer is its
+ * fallback and its judge. */
+typedef struct {
+  int32_t passes;
+  int32_t train_steps;
+  int32_t batch;
+  float lr;
+  int32_t terminate_depth;  /* 2: two bounces, then the cache */
+  int32_t train_stride;     /* every n-th path trains the cache (16) */
+  int32_t record_cap;       /* training records per pass */
+  int32_t query_cap;        /* cache queries per launch (paths are launched in chunks) */
+  uint64_t seed;
+} tpt_nrc_params;
+typedef struct {
+  double render_ms, infer_ms, train_ms;
+  float final_loss;
+  int64_t records, queries;
+} tpt_nrc_stats;
+void tpt_nrc_params_default(tpt_nrc_params *n);
+tpt_status tpt_render_nrc(tpt_context *ctx, int32_t slot, const tpt_render_params *p, const tpt_nrc_params *n,
+                          float *out_rgb, int32_t mem, tpt_render_stats *stats, tpt_nrc_stats *nstats);
 
 /* Host helpers: reference output quantisation (main.cpp:135-142,176-182) and
  * the PPM P3 writer of main.cpp:69,183-189. */

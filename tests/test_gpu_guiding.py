@@ -1,0 +1,63 @@
+"""Learned path guiding on the GPU: the guided estimator is unbiased (its
+per-pixel means agree with the plain tracer's, physical semantics), online
+training lowers the guiding loss, and on the small-light Cornell box the
+trained guide does not lose to the plain tracer at equal spp (relMSE against
+a high-spp FP64-accumulated plain render)."""
+import numpy as np
+import pytest
+
+import tpt
+from tpt import scenes
+
+pytestmark = pytest.mark.gpu
+
+EPS = 1e-2
+
+
+def relmse(x, ref):
+    return float(np.mean((x - ref) ** 2 / (ref * ref + EPS)))
+
+
+def test_guided_is_unbiased(ctx):
+    slot = ctx.upload(tpt.Scene(scenes.cornell_guiding().text()))
+    w = h = 32
+    k = 8
+    guided = np.stack([tpt.render_guided(ctx, slot, w, h, 64, seed=10 + i, passes=4, train_steps=16, batch=4096,
+                                         grid_res=8, record_cap=1 << 16)[0] for i in range(k)]).astype(np.float64)
+    plain = np.stack([ctx.render(slot, w, h, 64, semantics=tpt.SEMANTICS_PHYSICAL, seed=100 + i)[0]
+                      for i in range(k)]).astype(np.float64)
+    ma, mb = guided.mean(axis=(1, 2, 3)), plain.mean(axis=(1, 2, 3))
+    se = np.sqrt(ma.var(ddof=1) / k + mb.var(ddof=1) / k)
+    assert abs(ma.mean() - mb.mean()) < 4 * se, (ma.mean(), mb.mean(), se)
+    # 4x4-pixel blocks: per-pixel estimates of this scene are heavy-tailed
+    # (rare light hits), which skews per-pixel t statistics; block means are
+    # close to normal
+    def blocks(x):
+        return x.reshape(k, h // 4, 4, w // 4, 4, 3).mean(axis=(2, 4))
+    gb, pb = blocks(guided), blocks(plain)
+    d = gb.mean(0) - pb.mean(0)
+    s = np.sqrt(gb.var(0, ddof=1) / k + pb.var(0, ddof=1) / k)
+    z = d[s > 0] / s[s > 0]
+    assert abs(z.mean()) < 0.5 and z.std() < 1.8, (z.mean(), z.std())
+    ctx.release(slot)
+
+
+def test_training_lowers_the_loss(ctx):
+    slot = ctx.upload(tpt.Scene(scenes.cornell_guiding().text()))
+    _, _, g1 = tpt.render_guided(ctx, slot, 48, 48, 16, passes=2, train_steps=1, batch=8192, seed=3)
+    _, _, g2 = tpt.render_guided(ctx, slot, 48, 48, 16, passes=2, train_steps=300, batch=8192, seed=3)
+    assert g1["records"] > 1000 and g2["final_loss"] < g1["final_loss"], (g1, g2)
+    ctx.release(slot)
+
+
+def test_guided_does_not_lose_at_equal_spp(ctx):
+    slot = ctx.upload(tpt.Scene(scenes.cornell_guiding().text()))
+    w = h = 64
+    ref, _ = ctx.render(slot, w, h, 16384, semantics=tpt.SEMANTICS_PHYSICAL, seed=999, fp64=True)
+    plain = [relmse(ctx.render(slot, w, h, 256, semantics=tpt.SEMANTICS_PHYSICAL, seed=20 + i)[0], ref)
+             for i in range(3)]
+    guided = [relmse(tpt.render_guided(ctx, slot, w, h, 256, seed=40 + i, passes=8, train_steps=32)[0], ref)
+              for i in range(3)]
+    print("relMSE plain", np.mean(plain), "guided", np.mean(guided))
+    assert np.mean(guided) < 1.1 * np.mean(plain)
+    ctx.release(slot)

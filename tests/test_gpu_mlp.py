@@ -74,3 +74,36 @@ def test_mlp_weight_gradients_match_reference(built, shape):
     big = np.abs(gr) > 1e-3 * np.abs(gr).max()
     assert (moved[big] == -np.sign(gr[big])).mean() > 0.97
     assert np.abs(net.get_grad()).max() == 0.0
+
+
+def test_vmf_loss_gradient_matches_reference(built):
+    """The guiding loss on the GPU (weighted vMF-mixture NLL) against the
+    analytic float64 gradient of oracle/mlp_ref.py, itself checked against
+    finite differences in tests/test_learn_ref.py."""
+    import torch
+
+    net = tpt.Mlp(112, 3, 48, seed=11)
+    p16 = net.get_params().astype(np.float16).astype(np.float32)
+    rows = 1024
+    rng = np.random.default_rng(4)
+    x = rng.uniform(0, 1, size=(rows, 112)).astype(np.float16)
+    w = rng.normal(size=(rows, 3))
+    w /= np.linalg.norm(w, axis=1, keepdims=True)
+    wt = rng.uniform(0.1, 2.0, size=rows)
+    target = np.concatenate([w, wt[:, None]], axis=1).astype(np.float32)
+    xd = torch.from_numpy(x).cuda()
+    td = torch.from_numpy(target).cuda()
+    torch.cuda.synchronize()
+    scale = 64.0 / rows
+    loss = net.backward_vmf(xd.data_ptr(), td.data_ptr(), rows, scale)
+    g = net.get_grad() / scale
+    y, acts = mlp_ref.forward(p16, x.astype(np.float64), 112, 3, 48)
+    dy = mlp_ref.vmf_nll_grad(y, w, wt)
+    gr = mlp_ref.backward(p16, acts, dy.astype(np.float32).astype(np.float64), 112, 3, 48)
+    ref_loss = mlp_ref.vmf_nll(y, w, wt).sum()
+    assert abs(loss - ref_loss) < 2e-2 * abs(ref_loss)
+    off = 0
+    for (o, i) in mlp_ref.shapes(112, 3, 48):
+        a, b = g[off:off + o * i], gr[off:off + o * i]
+        off += o * i
+        assert np.abs(a - b).max() < 5e-2 * np.abs(b).max() + 1e-6, (o, i, np.abs(a - b).max(), np.abs(b).max())

@@ -1,0 +1,57 @@
+"""Neural radiance cache on the GPU: with the cache never queried the
+renderer is the plain tracer (statistically identical images); online
+training lowers the cache loss; a cached render is finite and its relMSE
+against a high-spp FP64 plain render stays within a bound of the plain
+tracer's at equal spp (the cache trades bias for shorter paths)."""
+import numpy as np
+import pytest
+
+import tpt
+from tpt import scenes
+
+pytestmark = pytest.mark.gpu
+EPS = 1e-2
+
+
+def relmse(x, ref):
+    return float(np.mean((x - ref) ** 2 / (ref * ref + EPS)))
+
+
+def _slot(ctx):
+    return ctx.upload(tpt.Scene(scenes.next_week(image_size=(256, 128)).text()))
+
+
+def test_uncached_nrc_render_equals_plain_tracer(ctx):
+    slot = _slot(ctx)
+    w = h = 24
+    k = 6
+    a = np.stack([tpt.render_nrc(ctx, slot, w, h, 32, seed=10 + i, passes=2, terminate_depth=1 << 20,
+                                 train_steps=4, batch=1024)[0] for i in range(k)]).astype(np.float64)
+    b = np.stack([ctx.render(slot, w, h, 32, semantics=tpt.SEMANTICS_PHYSICAL, seed=200 + i)[0]
+                  for i in range(k)]).astype(np.float64)
+    ma, mb = a.mean(axis=(1, 2, 3)), b.mean(axis=(1, 2, 3))
+    se = np.sqrt(ma.var(ddof=1) / k + mb.var(ddof=1) / k)
+    assert abs(ma.mean() - mb.mean()) < 4 * se + 1e-7, (ma.mean(), mb.mean(), se)
+    ctx.release(slot)
+
+
+def test_cache_training_lowers_loss_and_renders(ctx):
+    slot = _slot(ctx)
+    _, _, n1 = tpt.render_nrc(ctx, slot, 64, 64, 16, passes=2, train_steps=1, batch=8192, seed=3)
+    img, st, n2 = tpt.render_nrc(ctx, slot, 64, 64, 16, passes=2, train_steps=300, batch=8192, seed=3)
+    assert n1["records"] > 1000 and n2["queries"] > 0
+    assert n2["final_loss"] < n1["final_loss"], (n1, n2)
+    assert np.isfinite(img).all() and img.mean() > 0
+    ctx.release(slot)
+
+
+def test_cached_render_error_is_bounded(ctx):
+    slot = _slot(ctx)
+    w = h = 48
+    ref, _ = ctx.render(slot, w, h, 4096, semantics=tpt.SEMANTICS_PHYSICAL, seed=999, fp64=True)
+    plain = relmse(ctx.render(slot, w, h, 64, semantics=tpt.SEMANTICS_PHYSICAL, seed=5)[0], ref)
+    cached, st, ns = tpt.render_nrc(ctx, slot, w, h, 64, passes=4, train_steps=64, seed=5)
+    r = relmse(cached, ref)
+    print("relMSE plain", plain, "nrc", r, ns)
+    assert r < 5 * plain + 0.05
+    ctx.release(slot)

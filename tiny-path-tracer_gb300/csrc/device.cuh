@@ -100,7 +100,7 @@ __device__ __forceinline__ float4 uniforms(uint4 c, uint2 k) {
 }
 
 // Stream purposes (counter word w).
-enum { RNG_CAMERA_A = 0, RNG_CAMERA_B = 1, RNG_SCATTER = 2, RNG_MEDIUM = 3 };
+enum { RNG_CAMERA_A = 0, RNG_CAMERA_B = 1, RNG_SCATTER = 2, RNG_MEDIUM = 3, RNG_GUIDE = 4 };
 
 // Medium free-flight uniforms: a trace query keys them by (ray index,
 // medium id); a render path by (pixel, sample, bounce, medium id).
@@ -762,6 +762,27 @@ __device__ float3 light_random(const DevScene &S, float3 o, float pick, float r1
   return v3(1.f, 0.f, 0.f);
 }
 
+__device__ float3 guide_sample(const float4 *lob, float u_lobe, float u1, float u2) {
+  int pick = 7;
+  float cdf = 0.f;
+  for (int i = 0; i < 8; i++) {
+    cdf += __ldg(reinterpret_cast<const float4 *>(lob) + 2 * i + 1).x;
+    if (u_lobe < cdf) {
+      pick = i;
+      break;
+    }
+  }
+  const float4 a = __ldg(reinterpret_cast<const float4 *>(lob) + 2 * pick);
+  const float e2 = __ldg(reinterpret_cast<const float4 *>(lob) + 2 * pick + 1).z;
+  float w = 1.f + __logf(u1 + (1.f - u1) * e2) / a.w;
+  w = fminf(fmaxf(w, -1.f), 1.f);
+  const float sw = sqrtf(fmaxf(0.f, 1.f - w * w));
+  float sn, cs;
+  sincospif(2.f * u2, &sn, &cs);
+  const Onb f(v3(a.x, a.y, a.z));
+  return f.local(v3(cs * sw, sn * sw, w));
+}
+
 // ----------------------------------------------------------------- camera -
 // camera::get_ray (camera.cc:23-31) at the pixel-jittered (s, t) of
 // main.cpp:121-124.  Row j counts from the bottom of the image.
@@ -787,6 +808,48 @@ __device__ __forceinline__ Ray camera_ray(const Camera &c, int i, int j, int nx,
   return Ray{org + off, ll + s * hz + t * vt - org - off, time};
 }
 
+// ---------------------------------------------------------- path guiding --
+// The guiding network, evaluated on a res^3 grid of the scene box x 6 normal
+// bins after each training round, as a table of 8 vMF lobes per entry:
+// {mu.xyz, kappa}, {pi, kappa / (2 pi (1 - exp(-2 kappa))), exp(-2 kappa), 0}.
+struct GuideView {
+  const float4 *lobes;  // nullptr: not guided
+  float3 lo, inv_ext;
+  int res;
+  float alpha;  // probability of sampling the guide at a diffuse vertex
+};
+// The first diffuse vertex of a path, kept to form a training record.
+struct GuideRec {
+  float3 x, n, d, T, L;
+  bool valid;
+};
+
+__device__ __forceinline__ const float4 *guide_entry(const GuideView &g, float3 p, float3 n) {
+  const int r = g.res;
+  const int cx = min(max((int)((p.x - g.lo.x) * g.inv_ext.x * r), 0), r - 1);
+  const int cy = min(max((int)((p.y - g.lo.y) * g.inv_ext.y * r), 0), r - 1);
+  const int cz = min(max((int)((p.z - g.lo.z) * g.inv_ext.z * r), 0), r - 1);
+  const float ax = fabsf(n.x), ay = fabsf(n.y), az = fabsf(n.z);
+  const int bin = (ax >= ay && ax >= az) ? (n.x >= 0.f ? 0 : 1) : (ay >= az ? (n.y >= 0.f ? 2 : 3) : (n.z >= 0.f ? 4 : 5));
+  return g.lobes + ((size_t)((cz * r + cy) * r + cx) * 6 + bin) * 16;
+}
+
+// Mixture density of unit direction w (solid-angle measure).
+__device__ __forceinline__ float guide_pdf(const float4 *lob, float3 w) {
+  float p = 0.f;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const float4 a = __ldg(reinterpret_cast<const float4 *>(lob) + 2 * i);
+    const float4 b = __ldg(reinterpret_cast<const float4 *>(lob) + 2 * i + 1);
+    p += b.x * b.y * __expf(a.w * (a.x * w.x + a.y * w.y + a.z * w.z - 1.f));
+  }
+  return p;
+}
+
+// Picks a lobe by its weight, then samples the von Mises-Fisher lobe by
+// inverting its cosine distribution: cos = 1 + log(u + (1-u) e^{-2k}) / k.
+__device__ float3 guide_sample(const float4 *lob, float u_lobe, float u1, float u2);
+
 // ------------------------------------------------------------- shading ----
 struct RenderCfg {
   int max_depth;
@@ -810,8 +873,36 @@ __device__ __forceinline__ bool nonzero(float3 e) { return e.x != 0.f || e.y != 
 // terminal vertex T * emitted is always added, so a NaN weight anywhere on
 // the path makes the sample NaN as the recursive form does (de_nan then
 // zeroes it).  Returns true with `ray` replaced when the path continues.
-__device__ bool shade_vertex(const DevScene &S, const RenderCfg &cfg, Ray &ray, bool hit, const HitRef &h,
-                             float3 &T, float3 &L, int depth, uint32_t pixel, uint32_t sample) {
+// Radiance-cache features of a hit vertex: position, outgoing direction,
+// normal, albedo, roughness (lambertian/isotropic 1, metal fuzz, dielectric 0).
+struct VertexInfo {
+  float3 p, wo, n, albedo;
+  float rough;
+};
+
+__device__ __forceinline__ void vertex_info(const DevScene &S, const Ray &ray, const Surface &sf, const i4 &mi,
+                                            VertexInfo &vi) {
+  vi.p = sf.p;
+  vi.wo = -unit3(ray.d);
+  vi.n = sf.n;
+  vi.rough = 1.f;
+  vi.albedo = v3(0.f, 0.f, 0.f);
+  if (mi.x == MT_LAMBERTIAN || mi.x == MT_ISOTROPIC) {
+    vi.albedo = tex_value(S, mi.y, sf.u, sf.v, sf.p);
+  } else if (mi.x == MT_METAL) {
+    const f4 mf = ldg4(S.mat_f + sf.mat);
+    vi.albedo = f3(mf);
+    vi.rough = mf.w;
+  } else if (mi.x == MT_DIELECTRIC) {
+    vi.albedo = v3(1.f, 1.f, 1.f);
+    vi.rough = 0.f;
+  }
+}
+
+template <bool GUIDED>
+__device__ bool shade_vertex_t(const DevScene &S, const RenderCfg &cfg, Ray &ray, bool hit, const HitRef &h,
+                               float3 &T, float3 &L, int depth, uint32_t pixel, uint32_t sample, const GuideView &gv,
+                               GuideRec &rec, VertexInfo *vi = nullptr) {
   if (!hit) {
     L = L + T * background(cfg, ray);
     return false;
@@ -819,6 +910,7 @@ __device__ bool shade_vertex(const DevScene &S, const RenderCfg &cfg, Ray &ray, 
   Surface sf;
   finalize(S, ray, h, sf);
   const i4 mi = ldg4(S.mat_i + sf.mat);
+  if (vi) vertex_info(S, ray, sf, mi, *vi);
   float3 E = v3(0.f, 0.f, 0.f);
   if (mi.x == MT_LIGHT && dot3(sf.n, ray.d) < 0.f) E = tex_value(S, mi.y, sf.u, sf.v, sf.p);  // material.cc:79-86
   if (depth >= cfg.max_depth) {
@@ -886,15 +978,26 @@ __device__ bool shade_vertex(const DevScene &S, const RenderCfg &cfg, Ray &ray, 
       const Onb uvw(sf.n);
       const float cos_scale = cfg.semantics == 0 ? 1.f : 0.318309886183790671538f;
       float pdf;
-      if (S.has_lights) {
+      const float4 *lob = nullptr;
+      float4 q = make_float4(1.f, 0.f, 0.f, 0.f);
+      if (GUIDED && gv.lobes) {
+        lob = guide_entry(gv, sf.p, sf.n);
+        q = uniforms(make_uint4(pixel, sample, (uint32_t)depth, RNG_GUIDE), cfg.key);
+      }
+      if (GUIDED && lob && q.x < gv.alpha) {
+        dir = guide_sample(lob, q.y, q.z, q.w);
+      } else if (S.has_lights) {
         dir = r.x < 0.5f ? light_random(S, sf.p, r.y, r.z, r.w) : uvw.local(cos_hemisphere(r.z, r.w));
-        const float c = dot3(unit3(dir), uvw.w);
-        pdf = 0.5f * light_pdf(S, sf.p, dir) + 0.5f * (c > 0.f ? c * cos_scale : 0.f);
       } else {
         dir = uvw.local(cos_hemisphere(r.z, r.w));
-        const float c = dot3(unit3(dir), uvw.w);
-        pdf = c > 0.f ? c * cos_scale : 0.f;
       }
+      {
+        const float c = dot3(unit3(dir), uvw.w);
+        const float pc = c > 0.f ? c * cos_scale : 0.f;
+        pdf = S.has_lights ? 0.5f * light_pdf(S, sf.p, dir) + 0.5f * pc : pc;
+        if (GUIDED && lob) pdf = gv.alpha * guide_pdf(lob, unit3(dir)) + (1.f - gv.alpha) * pdf;
+      }
+      if (GUIDED && !rec.valid) rec = GuideRec{sf.p, sf.n, unit3(dir), T, L, true};
       const float cs = dot3(sf.n, unit3(dir));
       const float spdf = cs < 0.f ? 0.f : cs * 0.318309886183790671538f;
       wgt = atten * __fdividef(spdf, pdf);
@@ -908,6 +1011,14 @@ __device__ bool shade_vertex(const DevScene &S, const RenderCfg &cfg, Ray &ray, 
   T = T * wgt;
   ray = Ray{sf.p, dir, time};
   return true;
+}
+
+__device__ __forceinline__ bool shade_vertex(const DevScene &S, const RenderCfg &cfg, Ray &ray, bool hit,
+                                             const HitRef &h, float3 &T, float3 &L, int depth, uint32_t pixel,
+                                             uint32_t sample) {
+  GuideView gv{};
+  GuideRec rec{};
+  return shade_vertex_t<false>(S, cfg, ray, hit, h, T, L, depth, pixel, sample, gv, rec);
 }
 
 // utils.h:100-109

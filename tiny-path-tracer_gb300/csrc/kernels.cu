@@ -25,6 +25,7 @@
 #include "../../include/tpt.h"
 #include "arena.h"
 #include "device.cuh"
+#include "learn_internal.h"
 #include "scene_internal.h"
 
 namespace tpt {
@@ -359,6 +360,211 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
   if (e) atomicExch(&C->err, e);
 }
 
+// Guided persistent engine: as k_persistent, with guided diffuse vertices
+// and one training record per recorded path (every `rec_stride`-th sample).
+template <int MIN_BLOCKS>
+__global__ void __launch_bounds__(128, MIN_BLOCKS)
+    k_persistent_guided(DevScene S, RenderCfg cfg, FrameDesc F, WfCounters *C, GuideView gv, uint32_t sample_base,
+                        float4 *__restrict__ records, unsigned *rec_count, unsigned rec_cap, uint32_t rec_stride) {
+  extern __shared__ int2 stack_smem[];
+  int2 *stk = stack_smem + threadIdx.x;
+  int e = 0;
+  unsigned long long segs = 0;
+  bool alive = false, done = false;
+  Ray r{};
+  float3 T = v3(0.f, 0.f, 0.f), L = v3(0.f, 0.f, 0.f);
+  uint32_t pixel = 0, sample = 0;
+  int depth = 0;
+  GuideRec rec{};
+  bool want_rec = false;
+  for (;;) {
+    const bool want = !alive && !done;
+    if (__any_sync(0xffffffffu, want)) {
+      unsigned long long base;
+      int rank;
+      warp_claim(want, &C->issued, base, rank);
+      if (want) {
+        const unsigned long long s = base + (unsigned long long)rank;
+        if (s < F.total) {
+          int i, j;
+          sample_coords(F, s, pixel, sample, i, j);
+          sample += sample_base;
+          r = camera_ray(S.cam, i, j, F.nx, F.ny, pixel, sample, cfg.key);
+          T = v3(1.f, 1.f, 1.f);
+          L = v3(0.f, 0.f, 0.f);
+          depth = 0;
+          rec.valid = false;
+          want_rec = (s % rec_stride) == 0;
+          alive = true;
+        } else {
+          done = true;
+        }
+      }
+    }
+    if (__all_sync(0xffffffffu, done)) break;
+    bool emit = false;
+    float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0;
+    if (alive) {
+      MediumRng m{make_uint4(pixel, sample, (uint32_t)depth, 0u), cfg.key, 1};
+      HitRef h;
+      const bool hit = trace_closest(S, r, 0.001f, stk, blockDim.x, m, h, e);
+      segs++;
+      if (shade_vertex_t<true>(S, cfg, r, hit, h, T, L, depth, pixel, sample, gv, rec)) {
+        depth++;
+      } else {
+        accumulate(F, pixel, L);
+        alive = false;
+        if (want_rec && rec.valid) {
+          // contribution of the sampled direction: (L_final - L_k) / T_k
+          const float3 c = v3((L.x - rec.L.x) / rec.T.x, (L.y - rec.L.y) / rec.T.y, (L.z - rec.L.z) / rec.T.z);
+          float wgt = (c.x + c.y + c.z) * (1.f / 3.f);
+          if (!(wgt >= 0.f) || !(wgt < 1e6f)) wgt = 0.f;
+          emit = true;
+          r0 = make_float4(rec.x.x, rec.x.y, rec.x.z, wgt);
+          r1 = make_float4(rec.n.x, rec.n.y, rec.n.z, 0.f);
+          r2 = make_float4(rec.d.x, rec.d.y, rec.d.z, 0.f);
+        }
+      }
+    }
+    const unsigned slot = warp_append(emit, rec_count);
+    if (emit && slot < rec_cap) {
+      records[3 * (size_t)slot] = r0;
+      records[3 * (size_t)slot + 1] = r1;
+      records[3 * (size_t)slot + 2] = r2;
+    }
+  }
+  if (segs) atomicAdd(&C->segments, segs);
+  if (e) atomicExch(&C->err, e);
+}
+
+// Radiance-cache engine.  Paths stop at vertex `term_depth` and leave a
+// query; every `train_stride`-th path is traced to full depth and records its
+// vertices 0..2 (features now, target (L_final - L_k) / T_k at its end).
+template <int MIN_BLOCKS>
+__global__ void __launch_bounds__(128, MIN_BLOCKS)
+    k_persistent_nrc(DevScene S, RenderCfg cfg, FrameDesc F, WfCounters *C, unsigned long long sample_offset,
+                     int term_depth, uint32_t train_stride, float4 *__restrict__ records, unsigned *rec_count,
+                     unsigned rec_cap, float4 *__restrict__ queries, unsigned *q_count, unsigned q_cap) {
+  extern __shared__ int2 stack_smem[];
+  int2 *stk = stack_smem + threadIdx.x;
+  int e = 0;
+  unsigned long long segs = 0;
+  bool alive = false, done = false, training = false;
+  Ray r{};
+  float3 T = v3(0.f, 0.f, 0.f), L = v3(0.f, 0.f, 0.f);
+  uint32_t pixel = 0, sample = 0;
+  int depth = 0;
+  unsigned rslot[3];
+  float3 rT[3], rL[3];
+  int nrec = 0;
+  GuideView gv{};
+  GuideRec grec{};
+  for (;;) {
+    const bool want = !alive && !done;
+    if (__any_sync(0xffffffffu, want)) {
+      unsigned long long base;
+      int rank;
+      warp_claim(want, &C->issued, base, rank);
+      if (want) {
+        const unsigned long long s = base + (unsigned long long)rank;
+        if (s < F.total) {
+          int i, j;
+          sample_coords(F, s + sample_offset, pixel, sample, i, j);
+          r = camera_ray(S.cam, i, j, F.nx, F.ny, pixel, sample, cfg.key);
+          T = v3(1.f, 1.f, 1.f);
+          L = v3(0.f, 0.f, 0.f);
+          depth = 0;
+          training = ((s + sample_offset) % train_stride) == 0;
+          nrec = 0;
+          alive = true;
+        } else {
+          done = true;
+        }
+      }
+    }
+    if (__all_sync(0xffffffffu, done)) break;
+    bool want_q = false, want_r = false;
+    VertexInfo vi{};
+    float3 qT = T;
+    if (alive) {
+      MediumRng m{make_uint4(pixel, sample, (uint32_t)depth, 0u), cfg.key, 1};
+      HitRef h;
+      const bool hit = trace_closest(S, r, 0.001f, stk, blockDim.x, m, h, e);
+      segs++;
+      if (hit && !training && depth >= term_depth) {
+        Surface sf;
+        finalize(S, r, h, sf);
+        vertex_info(S, r, sf, ldg4(S.mat_i + sf.mat), vi);
+        want_q = true;
+        accumulate(F, pixel, L);
+        alive = false;
+      } else {
+        const float3 Tb = T, Lb = L;
+        const bool rec_here = training && hit && nrec < 3;
+        const bool cont = shade_vertex_t<false>(S, cfg, r, hit, h, T, L, depth, pixel, sample, gv, grec,
+                                                rec_here ? &vi : nullptr);
+        if (rec_here) {
+          want_r = true;
+          rT[nrec] = Tb;
+          rL[nrec] = Lb;
+        }
+        if (cont) {
+          depth++;
+        } else {
+          accumulate(F, pixel, L);
+          alive = false;
+        }
+      }
+    }
+    const unsigned qs = warp_append(want_q, q_count);
+    if (want_q && qs < q_cap) {
+      float4 *q = queries + 6 * (size_t)qs;
+      q[0] = make_float4(vi.p.x, vi.p.y, vi.p.z, vi.rough);
+      q[1] = make_float4(vi.wo.x, vi.wo.y, vi.wo.z, 0.f);
+      q[2] = make_float4(vi.n.x, vi.n.y, vi.n.z, 0.f);
+      q[3] = make_float4(vi.albedo.x, vi.albedo.y, vi.albedo.z, 0.f);
+      q[4] = make_float4(qT.x, qT.y, qT.z, __int_as_float((int)pixel));
+    }
+    const unsigned rs = warp_append(want_r, rec_count);
+    if (want_r) {
+      rslot[nrec] = rs;
+      if (rs < rec_cap) {
+        float4 *q = records + 5 * (size_t)rs;
+        q[0] = make_float4(vi.p.x, vi.p.y, vi.p.z, vi.rough);
+        q[1] = make_float4(vi.wo.x, vi.wo.y, vi.wo.z, 0.f);
+        q[2] = make_float4(vi.n.x, vi.n.y, vi.n.z, 0.f);
+        q[3] = make_float4(vi.albedo.x, vi.albedo.y, vi.albedo.z, 0.f);
+        q[4] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      nrec++;
+    }
+    if (training && !alive && nrec > 0) {  // path finished: targets of its records
+      const float3 Lf = de_nan(L);
+      for (int k = 0; k < nrec; k++) {
+        if (rslot[k] >= rec_cap) continue;
+        float3 tg = v3((Lf.x - rL[k].x) / rT[k].x, (Lf.y - rL[k].y) / rT[k].y, (Lf.z - rL[k].z) / rT[k].z);
+        tg = v3(isfinite(tg.x) ? fmaxf(tg.x, 0.f) : 0.f, isfinite(tg.y) ? fmaxf(tg.y, 0.f) : 0.f,
+                isfinite(tg.z) ? fmaxf(tg.z, 0.f) : 0.f);
+        records[5 * (size_t)rslot[k] + 4] = make_float4(tg.x, tg.y, tg.z, 1.f);
+      }
+      nrec = 0;
+    }
+  }
+  if (segs) atomicAdd(&C->segments, segs);
+  if (e) atomicExch(&C->err, e);
+}
+
+// accum[pixel] += de_nan(throughput * max(cache, 0)) for every query.
+__global__ void k_nrc_accumulate(const float4 *__restrict__ queries, const float *__restrict__ y, int count,
+                                 FrameDesc F) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    const float4 tq = queries[6 * (size_t)i + 4];
+    const float *c = y + (size_t)i * 16;
+    const float3 L = v3(tq.x * fmaxf(c[0], 0.f), tq.y * fmaxf(c[1], 0.f), tq.z * fmaxf(c[2], 0.f));
+    accumulate(F, (uint32_t)__float_as_int(tq.w), L);
+  }
+}
+
 // mean = sum / spp, image order (row 0 = top).
 __global__ void k_resolve(FrameDesc F, float *__restrict__ out) {
   const long long npix = (long long)F.nx * F.ny;
@@ -392,6 +598,7 @@ struct Slot {
   bool live = false;
   bool tuned = false;        // tpt_autotune result for engine = AUTO
   tpt_render_params tp{};
+  float world_lo[3] = {0, 0, 0}, world_hi[3] = {0, 0, 0};
 };
 
 struct DevBuf {
@@ -409,6 +616,10 @@ struct tpt_context {
   std::vector<Slot> slots;
   DevBuf path[2], hits, accum, accum64, staging, rays, hitf, hiti;
   DevBuf batch_table, batch_accum, batch_staging;
+  DevBuf guide_table, guide_records, guide_count;
+  GuideNet *guide = nullptr;
+  DevBuf nrc_records, nrc_queries, nrc_counts;
+  CacheNet *cache = nullptr;
   cudaGraphExec_t batch_graph = nullptr;  // replayed while the batch key matches
   uint64_t batch_key = 0;
   WfCounters *counters = nullptr;       // device
@@ -501,6 +712,12 @@ void tpt_context_destroy(tpt_context *c) {
   for (DevBuf *b : bufs)
     if (b->p) cudaFree(b->p);
   if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
+  DevBuf *gb[] = {&c->guide_table, &c->guide_records, &c->guide_count, &c->nrc_records, &c->nrc_queries,
+                  &c->nrc_counts};
+  for (DevBuf *b : gb)
+    if (b->p) cudaFree(b->p);
+  guide_destroy(c->guide);
+  cache_destroy(c->cache);
   if (c->counters) cudaFree(c->counters);
   if (c->counters_host) cudaFreeHost(c->counters_host);
   if (c->err) cudaFree(c->err);
@@ -575,6 +792,10 @@ tpt_status tpt_scene_upload(tpt_context *c, const tpt_scene *sc, int32_t *slot) 
   d.light_is_list = S.light_is_list;
   d.has_lights = S.has_lights;
   d.cam = S.cam;
+  for (int i = 0; i < 3; i++) {
+    s.world_lo[i] = S.world_lo[i];
+    s.world_hi[i] = S.world_hi[i];
+  }
   s.live = true;
   for (size_t i = 0; i < c->slots.size(); i++)
     if (!c->slots[i].live) {
@@ -1016,6 +1237,300 @@ extern "C" tpt_status tpt_autotune(tpt_context *c, int32_t slot, tpt_render_para
   c->slots[slot].tuned = true;
   c->slots[slot].tp = *p;
   if (best_msps) *best_msps = best;
+  return TPT_OK;
+}
+
+// ========================================================== path guiding ==
+extern "C" void tpt_guide_params_default(tpt_guide_params *g) {
+  if (!g) return;
+  g->passes = 8;
+  g->train_steps = 32;
+  g->batch = 16384;
+  g->lr = 1e-3f;
+  g->grid_res = 16;
+  g->alpha = 0.5f;
+  g->record_cap = 1 << 20;
+  g->seed = 1;
+}
+
+extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_render_params *p,
+                                        const tpt_guide_params *g, float *out_rgb, int32_t mem,
+                                        tpt_render_stats *stats, tpt_guide_stats *gstats) {
+  if (!c || !p || !g || !out_rgb) return TPT_ERR_INVALID_ARGUMENT;
+  if (slot < 0 || slot >= (int32_t)c->slots.size() || !c->slots[slot].live) return TPT_ERR_BAD_HANDLE;
+  if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->max_depth < 0 || g->passes < 1 ||
+      p->semantics != TPT_SEMANTICS_PHYSICAL || g->grid_res < 1 || g->grid_res > 64 || g->record_cap < 1 ||
+      !(g->alpha >= 0.f && g->alpha <= 1.f) || g->batch < 16)
+    return TPT_ERR_INVALID_ARGUMENT;
+  TPT_CUDA(cudaSetDevice(c->device));
+  const Slot &sl = c->slots[slot];
+  const unsigned long long npix = (unsigned long long)p->width * p->height;
+  const int spp_pass = (p->spp + g->passes - 1) / g->passes;
+  const int spp_total = spp_pass * g->passes;
+  tpt_status st;
+  if (!c->guide && (st = guide_create(c->device, g->seed, &c->guide)) != TPT_OK) return st;
+  {  // fresh network for every render: reproducible online training
+    guide_destroy(c->guide);
+    c->guide = nullptr;
+    if ((st = guide_create(c->device, g->seed, &c->guide)) != TPT_OK) return st;
+  }
+  const size_t table_f4 = (size_t)g->grid_res * g->grid_res * g->grid_res * 6 * 16;
+  if ((st = ensure(c->guide_table, table_f4 * sizeof(float4))) != TPT_OK) return st;
+  if ((st = ensure(c->guide_records, (size_t)g->record_cap * 3 * sizeof(float4))) != TPT_OK) return st;
+  if ((st = ensure(c->guide_count, sizeof(unsigned))) != TPT_OK) return st;
+  if ((st = ensure(c->accum, npix * sizeof(float4))) != TPT_OK) return st;
+  const float3 lo = make_float3(sl.world_lo[0], sl.world_lo[1], sl.world_lo[2]);
+  const float3 ext = make_float3(fmaxf(sl.world_hi[0] - sl.world_lo[0], 1e-6f),
+                                 fmaxf(sl.world_hi[1] - sl.world_lo[1], 1e-6f),
+                                 fmaxf(sl.world_hi[2] - sl.world_lo[2], 1e-6f));
+  DevScene S = sl.ds;
+  S.flat_max = p->flat_nodes > 0 ? p->flat_nodes : c->flat_nodes;
+  const RenderCfg cfg{p->max_depth, p->semantics, p->background, p->sky_scale,
+                      make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32))};
+  FrameDesc F{p->width, p->height, spp_pass, npix * (unsigned long long)spp_pass, (float4 *)c->accum.p, nullptr};
+  const int block = 128, smem = stack_smem(block);
+  auto kern = k_persistent_guided<4>;
+  TPT_CUDA(smem_optin(kern, smem));
+  const int grid = grid_for(c, kern, block, smem);
+  const unsigned long long per_pass = F.total;
+  const uint32_t stride = (uint32_t)std::max<unsigned long long>(1ull, per_pass / (unsigned long long)g->record_cap);
+  cudaEvent_t e[4];
+  for (auto &ev : e) TPT_CUDA(cudaEventCreate(&ev));
+  double render_ms = 0.0, train_ms = 0.0;
+  long long records = 0, segments = 0;
+  TPT_CUDA(cudaMemsetAsync(c->accum.p, 0, npix * sizeof(float4), c->stream));
+  bool have_table = false;
+  tpt_status result = TPT_OK;
+  for (int pass = 0; pass < g->passes && result == TPT_OK; pass++) {
+    GuideView gv{have_table ? (const float4 *)c->guide_table.p : nullptr, lo,
+                 make_float3(1.f / ext.x, 1.f / ext.y, 1.f / ext.z), g->grid_res, g->alpha};
+    WfCounters init{};
+    std::memcpy(c->counters_host, &init, sizeof(init));
+    cudaMemcpyAsync(c->counters, c->counters_host, sizeof(WfCounters), cudaMemcpyHostToDevice, c->stream);
+    cudaMemsetAsync(c->guide_count.p, 0, sizeof(unsigned), c->stream);
+    cudaEventRecord(e[0], c->stream);
+    kern<<<grid, block, smem, c->stream>>>(S, cfg, F, c->counters, gv, (uint32_t)(pass * spp_pass),
+                                          (float4 *)c->guide_records.p, (unsigned *)c->guide_count.p,
+                                          (unsigned)g->record_cap, stride);
+    cudaEventRecord(e[1], c->stream);
+    unsigned count = 0;
+    cudaMemcpyAsync(&count, c->guide_count.p, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t ce = cudaMemcpyAsync(c->counters_host, c->counters, sizeof(WfCounters), cudaMemcpyDeviceToHost,
+                                     c->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(c->stream);
+    if (ce != cudaSuccess) {
+      result = cuda_status(ce);
+      break;
+    }
+    if (c->counters_host->err) {
+      result = c->counters_host->err;
+      break;
+    }
+    segments += (long long)c->counters_host->segments;
+    count = std::min<unsigned>(count, (unsigned)g->record_cap);
+    records += count;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e[0], e[1]);
+    render_ms += ms;
+    if (pass + 1 < g->passes && count > 0) {
+      cudaEventRecord(e[2], c->stream);
+      result = guide_train(c->guide, (const float4 *)c->guide_records.p, (int)count, g->train_steps, g->batch, g->lr,
+                           lo, ext, g->seed + 7919ull * (pass + 1), c->stream);
+      if (result == TPT_OK) result = guide_refresh(c->guide, g->grid_res, (float4 *)c->guide_table.p, c->stream);
+      cudaEventRecord(e[3], c->stream);
+      cudaStreamSynchronize(c->stream);
+      cudaEventElapsedTime(&ms, e[2], e[3]);
+      train_ms += ms;
+      have_table = true;
+    }
+  }
+  for (auto &ev : e) cudaEventDestroy(ev);
+  if (result != TPT_OK) return result;
+  // resolve over all passes
+  FrameDesc R = F;
+  R.spp = spp_total;
+  float *dst = out_rgb;
+  if (mem == TPT_MEM_HOST) {
+    if ((st = ensure(c->staging, npix * 3 * sizeof(float))) != TPT_OK) return st;
+    dst = (float *)c->staging.p;
+  }
+  const int rgrid = (int)std::min<unsigned long long>((npix + 255) / 256, (unsigned long long)c->sm_count * 16);
+  k_resolve<<<rgrid, 256, 0, c->stream>>>(R, dst);
+  TPT_CUDA(cudaGetLastError());
+  if (mem == TPT_MEM_HOST)
+    TPT_CUDA(cudaMemcpyAsync(out_rgb, dst, npix * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  TPT_CUDA(cudaStreamSynchronize(c->stream));
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->samples = (int64_t)(npix * (unsigned long long)spp_total);
+    stats->segments = segments;
+    stats->iterations = g->passes;
+    stats->device_ms = render_ms + train_ms;
+  }
+  if (gstats) {
+    gstats->render_ms = render_ms;
+    gstats->train_ms = train_ms;
+    gstats->final_loss = guide_last_loss(c->guide);
+    gstats->records = records;
+  }
+  return TPT_OK;
+}
+
+// ============================================== neural radiance cache =====
+extern "C" void tpt_nrc_params_default(tpt_nrc_params *n) {
+  if (!n) return;
+  n->passes = 8;
+  n->train_steps = 32;
+  n->batch = 16384;
+  n->lr = 1e-3f;
+  n->terminate_depth = 2;
+  n->train_stride = 16;
+  n->record_cap = 1 << 20;
+  n->query_cap = 1 << 22;
+  n->seed = 1;
+}
+
+extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_render_params *p,
+                                     const tpt_nrc_params *n, float *out_rgb, int32_t mem, tpt_render_stats *stats,
+                                     tpt_nrc_stats *nstats) {
+  if (!c || !p || !n || !out_rgb) return TPT_ERR_INVALID_ARGUMENT;
+  if (slot < 0 || slot >= (int32_t)c->slots.size() || !c->slots[slot].live) return TPT_ERR_BAD_HANDLE;
+  if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->max_depth < 0 || n->passes < 1 ||
+      n->terminate_depth < 0 || n->train_stride < 1 || n->record_cap < 16 || n->query_cap < 1024 || n->batch < 16)
+    return TPT_ERR_INVALID_ARGUMENT;
+  TPT_CUDA(cudaSetDevice(c->device));
+  const Slot &sl = c->slots[slot];
+  const unsigned long long npix = (unsigned long long)p->width * p->height;
+  const int spp_pass = (p->spp + n->passes - 1) / n->passes;
+  const int spp_total = spp_pass * n->passes;
+  tpt_status st;
+  cache_destroy(c->cache);  // fresh cache for every render: reproducible online training
+  c->cache = nullptr;
+  if ((st = cache_create(c->device, n->seed, &c->cache)) != TPT_OK) return st;
+  if ((st = ensure(c->nrc_records, (size_t)n->record_cap * 5 * sizeof(float4))) != TPT_OK) return st;
+  if ((st = ensure(c->nrc_queries, (size_t)n->query_cap * 6 * sizeof(float4))) != TPT_OK) return st;
+  if ((st = ensure(c->nrc_counts, 2 * sizeof(unsigned))) != TPT_OK) return st;
+  if ((st = ensure(c->accum, npix * sizeof(float4))) != TPT_OK) return st;
+  const float3 lo = make_float3(sl.world_lo[0], sl.world_lo[1], sl.world_lo[2]);
+  const float3 ext = make_float3(fmaxf(sl.world_hi[0] - sl.world_lo[0], 1e-6f),
+                                 fmaxf(sl.world_hi[1] - sl.world_lo[1], 1e-6f),
+                                 fmaxf(sl.world_hi[2] - sl.world_lo[2], 1e-6f));
+  DevScene S = sl.ds;
+  S.flat_max = p->flat_nodes > 0 ? p->flat_nodes : c->flat_nodes;
+  const RenderCfg cfg{p->max_depth, p->semantics, p->background, p->sky_scale,
+                      make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32))};
+  const int block = 128, smem = stack_smem(block);
+  auto kern = k_persistent_nrc<4>;
+  TPT_CUDA(smem_optin(kern, smem));
+  const int grid = grid_for(c, kern, block, smem);
+  unsigned *counts = (unsigned *)c->nrc_counts.p;  // [0] records, [1] queries
+  cudaEvent_t ev[6];
+  for (auto &x : ev) TPT_CUDA(cudaEventCreate(&x));
+  double render_ms = 0, infer_ms = 0, train_ms = 0;
+  long long n_rec = 0, n_q = 0, segments = 0;
+  TPT_CUDA(cudaMemsetAsync(c->accum.p, 0, npix * sizeof(float4), c->stream));
+  FrameDesc F{p->width, p->height, spp_pass, 0, (float4 *)c->accum.p, nullptr};
+  const unsigned long long chunk = (unsigned long long)n->query_cap;  // samples per launch
+  tpt_status result = TPT_OK;
+  for (int pass = 0; pass < n->passes && result == TPT_OK; pass++) {
+    const bool cached = pass > 0;
+    const int term = cached ? n->terminate_depth : (1 << 30);
+    cudaMemsetAsync(counts, 0, sizeof(unsigned), c->stream);  // records of this pass
+    const unsigned long long pass_begin = (unsigned long long)pass * spp_pass * npix;
+    const unsigned long long pass_total = (unsigned long long)spp_pass * npix;
+    for (unsigned long long off = 0; off < pass_total && result == TPT_OK; off += chunk) {
+      const unsigned long long cnt = std::min(chunk, pass_total - off);
+      FrameDesc Fc = F;
+      Fc.total = cnt;
+      WfCounters init{};
+      std::memcpy(c->counters_host, &init, sizeof(init));
+      cudaMemcpyAsync(c->counters, c->counters_host, sizeof(WfCounters), cudaMemcpyHostToDevice, c->stream);
+      cudaMemsetAsync(counts + 1, 0, sizeof(unsigned), c->stream);
+      cudaEventRecord(ev[0], c->stream);
+      kern<<<grid, block, smem, c->stream>>>(S, cfg, Fc, c->counters, pass_begin + off, term,
+                                            (uint32_t)n->train_stride, (float4 *)c->nrc_records.p, counts,
+                                            (unsigned)n->record_cap, (float4 *)c->nrc_queries.p, counts + 1,
+                                            (unsigned)n->query_cap);
+      cudaEventRecord(ev[1], c->stream);
+      unsigned q = 0;
+      cudaMemcpyAsync(&q, counts + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
+      cudaError_t ce = cudaMemcpyAsync(c->counters_host, c->counters, sizeof(WfCounters), cudaMemcpyDeviceToHost,
+                                       c->stream);
+      if (ce == cudaSuccess) ce = cudaStreamSynchronize(c->stream);
+      if (ce != cudaSuccess) {
+        result = cuda_status(ce);
+        break;
+      }
+      if (c->counters_host->err) {
+        result = c->counters_host->err;
+        break;
+      }
+      segments += (long long)c->counters_host->segments;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[0], ev[1]);
+      render_ms += ms;
+      q = std::min<unsigned>(q, (unsigned)n->query_cap);
+      n_q += q;
+      if (q > 0) {
+        cudaEventRecord(ev[2], c->stream);
+        const float *y = nullptr;
+        result = cache_infer(c->cache, (const float4 *)c->nrc_queries.p, (int)q, lo, ext, &y, c->stream);
+        if (result != TPT_OK) break;
+        const int g2 = (int)std::min<unsigned>((q + 255) / 256, (unsigned)c->sm_count * 16);
+        k_nrc_accumulate<<<g2, 256, 0, c->stream>>>((const float4 *)c->nrc_queries.p, y, (int)q, F);
+        cudaEventRecord(ev[3], c->stream);
+        cudaStreamSynchronize(c->stream);
+        cudaEventElapsedTime(&ms, ev[2], ev[3]);
+        infer_ms += ms;
+      }
+    }
+    if (result != TPT_OK) break;
+    unsigned nr = 0;
+    cudaMemcpyAsync(&nr, counts, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
+    cudaStreamSynchronize(c->stream);
+    nr = std::min<unsigned>(nr, (unsigned)n->record_cap);
+    n_rec += nr;
+    if (pass + 1 < n->passes && nr > 0) {
+      cudaEventRecord(ev[4], c->stream);
+      result = cache_train(c->cache, (const float4 *)c->nrc_records.p, (int)nr, n->train_steps, n->batch, n->lr, lo,
+                           ext, (uint32_t)(n->seed * 2654435761ull + pass), c->stream);
+      cudaEventRecord(ev[5], c->stream);
+      cudaStreamSynchronize(c->stream);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[4], ev[5]);
+      train_ms += ms;
+    }
+  }
+  for (auto &x : ev) cudaEventDestroy(x);
+  if (result != TPT_OK) return result;
+  FrameDesc R = F;
+  R.spp = spp_total;
+  float *dst = out_rgb;
+  if (mem == TPT_MEM_HOST) {
+    if ((st = ensure(c->staging, npix * 3 * sizeof(float))) != TPT_OK) return st;
+    dst = (float *)c->staging.p;
+  }
+  const int rgrid = (int)std::min<unsigned long long>((npix + 255) / 256, (unsigned long long)c->sm_count * 16);
+  k_resolve<<<rgrid, 256, 0, c->stream>>>(R, dst);
+  TPT_CUDA(cudaGetLastError());
+  if (mem == TPT_MEM_HOST)
+    TPT_CUDA(cudaMemcpyAsync(out_rgb, dst, npix * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  TPT_CUDA(cudaStreamSynchronize(c->stream));
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->samples = (int64_t)(npix * (unsigned long long)spp_total);
+    stats->segments = segments;
+    stats->iterations = n->passes;
+    stats->device_ms = render_ms + infer_ms + train_ms;
+  }
+  if (nstats) {
+    nstats->render_ms = render_ms;
+    nstats->infer_ms = infer_ms;
+    nstats->train_ms = train_ms;
+    nstats->final_loss = cache_last_loss(c->cache);
+    nstats->records = n_rec;
+    nstats->queries = n_q;
+  }
   return TPT_OK;
 }
 

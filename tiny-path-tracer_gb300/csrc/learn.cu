@@ -160,10 +160,10 @@ __global__ void __launch_bounds__(WARPS * 32)
 #pragma unroll
     for (int kk = 0; kk < OUT / 16; kk++) {
       const float *d0 = my_dy + g * OUT + kk * 16 + 2 * t, *d1 = d0 + 8 * OUT;
-      dz_out[kk][0] = pack2(d0[0], d0[1]);
-      dz_out[kk][1] = pack2(d1[0], d1[1]);
-      dz_out[kk][2] = pack2(d0[8], d0[9]);
-      dz_out[kk][3] = pack2(d1[8], d1[9]);
+      dz_out[kk][0] = pack2_sat(d0[0], d0[1]);
+      dz_out[kk][1] = pack2_sat(d1[0], d1[1]);
+      dz_out[kk][2] = pack2_sat(d0[8], d0[9]);
+      dz_out[kk][3] = pack2_sat(d1[8], d1[9]);
     }
     store_frag_t<OUT>(dz_out, dZt + dz_off[NH], rows, r0);
     // dH_NH = dZ_out * W_out, then through the hidden layers
@@ -178,10 +178,10 @@ __global__ void __launch_bounds__(WARPS * 32)
         const float2 m1 = unpack2(my_h[(l * 16 + kk * 4 + 1) * 32 + lane]);
         const float2 m2 = unpack2(my_h[(l * 16 + kk * 4 + 2) * 32 + lane]);
         const float2 m3 = unpack2(my_h[(l * 16 + kk * 4 + 3) * 32 + lane]);
-        dz[kk][0] = pack2(m0.x > 0.f ? acc[2 * kk][0] : 0.f, m0.y > 0.f ? acc[2 * kk][1] : 0.f);
-        dz[kk][1] = pack2(m1.x > 0.f ? acc[2 * kk][2] : 0.f, m1.y > 0.f ? acc[2 * kk][3] : 0.f);
-        dz[kk][2] = pack2(m2.x > 0.f ? acc[2 * kk + 1][0] : 0.f, m2.y > 0.f ? acc[2 * kk + 1][1] : 0.f);
-        dz[kk][3] = pack2(m3.x > 0.f ? acc[2 * kk + 1][2] : 0.f, m3.y > 0.f ? acc[2 * kk + 1][3] : 0.f);
+        dz[kk][0] = pack2_sat(m0.x > 0.f ? acc[2 * kk][0] : 0.f, m0.y > 0.f ? acc[2 * kk][1] : 0.f);
+        dz[kk][1] = pack2_sat(m1.x > 0.f ? acc[2 * kk][2] : 0.f, m1.y > 0.f ? acc[2 * kk][3] : 0.f);
+        dz[kk][2] = pack2_sat(m2.x > 0.f ? acc[2 * kk + 1][0] : 0.f, m2.y > 0.f ? acc[2 * kk + 1][1] : 0.f);
+        dz[kk][3] = pack2_sat(m3.x > 0.f ? acc[2 * kk + 1][2] : 0.f, m3.y > 0.f ? acc[2 * kk + 1][3] : 0.f);
       }
       store_frag_t<HID>(dz, dZt + dz_off[l], rows, r0);
       if (l > 0) layer_mma<HID, HID>(dz, swt + smem_wt_offset(n, l), acc);
@@ -260,7 +260,8 @@ __global__ void k_adam(int count, float *__restrict__ w32, __half *__restrict__ 
                        float *__restrict__ m, float *__restrict__ v, float lr, float b1, float b2, float eps,
                        float inv_scale, float bc1, float bc2) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-    const float gr = grad[i] * inv_scale;
+    float gr = grad[i] * inv_scale;
+    if (!isfinite(gr)) gr = 0.f;  // an overflowed element skips this step
     const float mi = b1 * m[i] + (1.f - b1) * gr;
     const float vi = b2 * v[i] + (1.f - b2) * gr * gr;
     m[i] = mi;
@@ -298,6 +299,9 @@ __device__ __forceinline__ void guide_encode(float3 xn, float3 n, __half *out) {
 struct LossVmf {
   const float4 *target;  // (omega.xyz, weight)
   float scale;
+  const float *wsum;     // if set: weights are normalised by the batch sum
+  float clip;            // if > 0: per-row bound on the gradient's L2 norm (before `scale`)
+  static constexpr float KAPPA_MAX = 500.f;
   template <int OUT>
   __device__ float grad(int row, const float *y, float *dy) const {
     const float4 tg = target[row];
@@ -311,7 +315,7 @@ struct LossVmf {
       logit[i] = __expf(y[5 * i] - lmax);
       zsum += logit[i];
       const float kp = y[5 * i + 1];
-      kap[i] = (kp > 20.f ? kp : log1pf(__expf(kp))) + 1e-2f;
+      kap[i] = fminf((kp > 20.f ? kp : log1pf(__expf(kp))) + 1e-2f, KAPPA_MAX);
       const float3 m = make_float3(y[5 * i + 2], y[5 * i + 3], y[5 * i + 4]);
       mn[i] = fmaxf(sqrtf(m.x * m.x + m.y * m.y + m.z * m.z), 1e-12f);
       mu[i] = make_float3(m.x / mn[i], m.y / mn[i], m.z / mn[i]);
@@ -325,26 +329,35 @@ struct LossVmf {
       p += logit[i] * f[i];
     }
     p = fmaxf(p, 1e-30f);
-    const float wt = tg.w * scale;
+    const float wn = wsum ? tg.w / fmaxf(*wsum, 1e-30f) : tg.w;
+    float n2 = 0.f;
     for (int i = 0; i < GUIDE_LOBES; i++) {
       const float r = logit[i] * f[i] / p;
       const float e2 = __expf(-2.f * kap[i]);
-      dy[5 * i] = wt * (logit[i] - r);
+      dy[5 * i] = wn * (logit[i] - r);
       const float dlk = 1.f / kap[i] - 2.f * e2 / (1.f - e2) + (cs[i] - 1.f);
-      dy[5 * i + 1] = wt * (-r * dlk / (1.f + __expf(-y[5 * i + 1])));
+      const bool capped = kap[i] >= KAPPA_MAX;
+      dy[5 * i + 1] = capped ? 0.f : wn * (-r * dlk / (1.f + __expf(-y[5 * i + 1])));
       const float k = -r * kap[i] / mn[i];
-      dy[5 * i + 2] = wt * k * (w.x - cs[i] * mu[i].x);
-      dy[5 * i + 3] = wt * k * (w.y - cs[i] * mu[i].y);
-      dy[5 * i + 4] = wt * k * (w.z - cs[i] * mu[i].z);
+      dy[5 * i + 2] = wn * k * (w.x - cs[i] * mu[i].x);
+      dy[5 * i + 3] = wn * k * (w.y - cs[i] * mu[i].y);
+      dy[5 * i + 4] = wn * k * (w.z - cs[i] * mu[i].z);
+      for (int c = 0; c < 5; c++) n2 += dy[5 * i + c] * dy[5 * i + c];
     }
+    // per-row gradient clipping: a sharp lobe on a heavy record (or a mean
+    // vector of tiny norm) must not dominate the step or overflow f16
+    const float sc = (clip > 0.f && n2 > clip * clip) ? scale * clip * rsqrtf(n2) : scale;
+    for (int o = 0; o < 5 * GUIDE_LOBES; o++) dy[o] *= sc;
     for (int o = 5 * GUIDE_LOBES; o < OUT; o++) dy[o] = 0.f;
-    return -tg.w * logf(p);
+    return -wn * logf(p);
   }
 };
 
 // Training rows: a random record per row (with replacement), encoded.
 __global__ void k_guide_encode_records(const float4 *__restrict__ rec, int count, int rows, uint2 key, uint32_t step,
-                                       float3 lo, float3 inv_ext, __half *__restrict__ X, float4 *__restrict__ target) {
+                                       float3 lo, float3 inv_ext, __half *__restrict__ X, float4 *__restrict__ target,
+                                       float *wsum) {
+  float part = 0.f;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
     uint32_t h = (uint32_t)r * 0x9E3779B1u ^ (step * 0x85EBCA77u) ^ key.x;
     h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12; h *= 0x297A2D39u; h ^= h >> 15;
@@ -353,7 +366,10 @@ __global__ void k_guide_encode_records(const float4 *__restrict__ rec, int count
     const float3 xn = make_float3((xw.x - lo.x) * inv_ext.x, (xw.y - lo.y) * inv_ext.y, (xw.z - lo.z) * inv_ext.z);
     guide_encode(xn, make_float3(nn.x, nn.y, nn.z), X + (size_t)r * GUIDE_IN);
     target[r] = make_float4(dd.x, dd.y, dd.z, xw.w);
+    part += xw.w;
   }
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if ((threadIdx.x & 31) == 0 && part != 0.f) atomicAdd(wsum, part);
 }
 
 // Grid rows: cell centres x 6 axis normals (+x,-x,+y,-y,+z,-z).
@@ -385,16 +401,99 @@ __global__ void k_guide_post(const float *__restrict__ Y, int rows_valid, float4
       e[i] = __expf(y[5 * i] - lmax);
       z += e[i];
     }
+    float4 out[2 * GUIDE_LOBES];
+    bool ok = z > 0.f && isfinite(z);
     for (int i = 0; i < GUIDE_LOBES; i++) {
       const float kp = y[5 * i + 1];
-      const float k = (kp > 20.f ? kp : log1pf(__expf(kp))) + 1e-2f;
+      const float k = fminf((kp > 20.f ? kp : log1pf(__expf(kp))) + 1e-2f, LossVmf::KAPPA_MAX);
       float mx = y[5 * i + 2], my = y[5 * i + 3], mz = y[5 * i + 4];
       const float mnorm = fmaxf(sqrtf(mx * mx + my * my + mz * mz), 1e-12f);
       const float e2 = __expf(-2.f * k);
-      lobes[(size_t)r * 2 * GUIDE_LOBES + 2 * i] = make_float4(mx / mnorm, my / mnorm, mz / mnorm, k);
-      lobes[(size_t)r * 2 * GUIDE_LOBES + 2 * i + 1] =
-          make_float4(e[i] / z, k / (6.28318530717958647692f * (1.f - e2)), e2, 0.f);
+      out[2 * i] = make_float4(mx / mnorm, my / mnorm, mz / mnorm, k);
+      out[2 * i + 1] = make_float4(e[i] / z, k / (6.28318530717958647692f * (1.f - e2)), e2, 0.f);
+      ok = ok && isfinite(out[2 * i].x) && isfinite(out[2 * i].y) && isfinite(out[2 * i].z) && isfinite(k) &&
+           isfinite(out[2 * i + 1].x) && isfinite(out[2 * i + 1].y);
     }
+    if (!ok) {  // a broad lobe: sampling and density stay consistent
+      for (int i = 0; i < GUIDE_LOBES; i++) {
+        const float k = 0.01f, e2 = __expf(-2.f * k);
+        out[2 * i] = make_float4(0.f, 0.f, 1.f, k);
+        out[2 * i + 1] = make_float4(i == 0 ? 1.f : 0.f, k / (6.28318530717958647692f * (1.f - e2)), e2, 0.f);
+      }
+    }
+    for (int i = 0; i < 2 * GUIDE_LOBES; i++) lobes[(size_t)r * 2 * GUIDE_LOBES + i] = out[i];
+  }
+}
+
+// ------------------------------------------------- neural radiance cache --
+// Input: one-blob position (3 x 16 bins) + outgoing direction + normal +
+// albedo + roughness = 58 values padded to 64; output RGB (3 of 16).
+// Records / queries are 4 float4: (x, roughness), (w_out, 0), (n, 0),
+// (albedo, 0); training targets float4 (rgb, 0).
+constexpr int NRC_IN = 64, NRC_NH = 5, NRC_OUT = 16, NRC_BINS = 16;
+
+__device__ __forceinline__ void nrc_encode(const float4 *f, float3 lo, float3 inv_ext, __half *out) {
+  const float c[3] = {(f[0].x - lo.x) * inv_ext.x, (f[0].y - lo.y) * inv_ext.y, (f[0].z - lo.z) * inv_ext.z};
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const float u = fminf(fmaxf(c[a], 0.f), 1.f) * NRC_BINS;
+    for (int b = 0; b < NRC_BINS; b++) out[a * NRC_BINS + b] = __float2half_rn(fmaxf(0.f, 1.f - fabsf(u - (b + 0.5f))));
+  }
+  out[48] = __float2half_rn(f[1].x);
+  out[49] = __float2half_rn(f[1].y);
+  out[50] = __float2half_rn(f[1].z);
+  out[51] = __float2half_rn(f[2].x);
+  out[52] = __float2half_rn(f[2].y);
+  out[53] = __float2half_rn(f[2].z);
+  out[54] = __float2half_rn(f[3].x);
+  out[55] = __float2half_rn(f[3].y);
+  out[56] = __float2half_rn(f[3].z);
+  out[57] = __float2half_rn(f[0].w);
+  for (int i = 58; i < NRC_IN; i++) out[i] = __float2half_rn(0.f);
+}
+
+// Relative L2 (Mueller et al., "Real-time Neural Radiance Caching for Path
+// Tracing", ACM TOG 2021): (y - t)^2 / (sg(y)^2 + 0.01) per channel.
+struct LossRelL2 {
+  const float4 *target;
+  float scale;
+  template <int OUT>
+  __device__ float grad(int row, const float *y, float *dy) const {
+    const float4 t = target[row];
+    const float tv[3] = {t.x, t.y, t.z};
+    float loss = 0.f;
+    for (int c = 0; c < 3; c++) {
+      const float d = y[c] - tv[c];
+      const float den = y[c] * y[c] + 0.01f;
+      loss += d * d / den;
+      dy[c] = scale * 2.f * d / den;
+    }
+    for (int o = 3; o < OUT; o++) dy[o] = 0.f;
+    return loss;
+  }
+};
+
+__global__ void k_nrc_encode_records(const float4 *__restrict__ rec, int count, int rows, uint32_t key,
+                                     uint32_t step, float3 lo, float3 inv_ext, __half *__restrict__ X,
+                                     float4 *__restrict__ target) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+    uint32_t h = (uint32_t)r * 0x9E3779B1u ^ (step * 0x85EBCA77u) ^ key;
+    h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12; h *= 0x297A2D39u; h ^= h >> 15;
+    const int idx = (int)(h % (uint32_t)count);
+    nrc_encode(rec + 5 * (size_t)idx, lo, inv_ext, X + (size_t)r * NRC_IN);
+    target[r] = rec[5 * (size_t)idx + 4];
+  }
+}
+
+__global__ void k_nrc_encode_queries(const float4 *__restrict__ q, int count, int rows, float3 lo, float3 inv_ext,
+                                     __half *__restrict__ X) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+    __half *out = X + (size_t)r * NRC_IN;
+    if (r >= count) {
+      for (int i = 0; i < NRC_IN; i++) out[i] = __float2half_rn(0.f);
+      continue;
+    }
+    nrc_encode(q + 6 * (size_t)r, lo, inv_ext, out);
   }
 }
 
@@ -501,6 +600,7 @@ struct GuideNet {
   __half *x = nullptr;
   float *y = nullptr;
   float4 *target = nullptr;
+  float *wsum = nullptr;
   int cap_rows = 0;
   float last_loss = 0.f;
 };
@@ -516,6 +616,7 @@ static tpt_status guide_ws(GuideNet *G, int rows) {
   MLP_CUDA(cudaMalloc(&G->x, (size_t)rows * GUIDE_IN * sizeof(__half)));
   MLP_CUDA(cudaMalloc(&G->y, (size_t)rows * GUIDE_OUT * sizeof(float)));
   MLP_CUDA(cudaMalloc(&G->target, (size_t)rows * sizeof(float4)));
+  if (!G->wsum) MLP_CUDA(cudaMalloc(&G->wsum, sizeof(float)));
   G->cap_rows = rows;
   return TPT_OK;
 }
@@ -537,6 +638,7 @@ void guide_destroy(GuideNet *G) {
   if (G->x) cudaFree(G->x);
   if (G->y) cudaFree(G->y);
   if (G->target) cudaFree(G->target);
+  if (G->wsum) cudaFree(G->wsum);
   delete G;
 }
 
@@ -549,12 +651,13 @@ tpt_status guide_train(GuideNet *G, const float4 *rec, int count, int steps, int
   if (st != TPT_OK) return st;
   if ((st = ensure_ws(G->net, batch)) != TPT_OK) return st;
   const float3 inv = make_float3(1.f / ext.x, 1.f / ext.y, 1.f / ext.z);
-  const float loss_scale = 1024.f;
+  const float loss_scale = 256.f;  // weights are normalised to sum 1 per batch
   for (int k = 0; k < steps; k++) {
+    MLP_CUDA(cudaMemsetAsync(G->wsum, 0, sizeof(float), s));
     k_guide_encode_records<<<(batch + 255) / 256, 256, 0, s>>>(
         rec, count, batch, make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)), (uint32_t)(G->net->steps + 1), lo,
-        inv, G->x, G->target);
-    LossVmf L{G->target, loss_scale / (float)batch};
+        inv, G->x, G->target, G->wsum);
+    LossVmf L{G->target, loss_scale, G->wsum, 0.25f};
     st = launch_train<GUIDE_IN, GUIDE_NH, GUIDE_OUT>(G->net, G->x, batch, L, s);
     if (st != TPT_OK) return st;
     st = tpt_mlp_adam(G->net, lr, 1.f / loss_scale, s);
@@ -563,7 +666,7 @@ tpt_status guide_train(GuideNet *G, const float4 *rec, int count, int steps, int
   float l = 0.f;
   MLP_CUDA(cudaMemcpyAsync(&l, G->net->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
   MLP_CUDA(cudaStreamSynchronize(s));
-  G->last_loss = l / (float)batch;
+  G->last_loss = l;  // weighted mean NLL of the last batch
   return TPT_OK;
 }
 
@@ -582,6 +685,92 @@ tpt_status guide_refresh(GuideNet *G, int res, float4 *table, cudaStream_t s) {
 }
 
 float guide_last_loss(const GuideNet *G) { return G->last_loss; }
+
+// Radiance-cache network state used by the renderer.
+struct CacheNet {
+  tpt_mlp *net = nullptr;
+  __half *x = nullptr;
+  float *y = nullptr;
+  float4 *target = nullptr;
+  int cap_rows = 0;
+  float last_loss = 0.f;
+};
+
+static tpt_status cache_ws(CacheNet *G, int rows) {
+  if (rows <= G->cap_rows) return TPT_OK;
+  if (G->x) cudaFree(G->x);
+  if (G->y) cudaFree(G->y);
+  if (G->target) cudaFree(G->target);
+  G->x = nullptr;
+  G->y = nullptr;
+  G->target = nullptr;
+  MLP_CUDA(cudaMalloc(&G->x, (size_t)rows * NRC_IN * sizeof(__half)));
+  MLP_CUDA(cudaMalloc(&G->y, (size_t)rows * NRC_OUT * sizeof(float)));
+  MLP_CUDA(cudaMalloc(&G->target, (size_t)rows * sizeof(float4)));
+  G->cap_rows = rows;
+  return TPT_OK;
+}
+
+tpt_status cache_create(int device, uint64_t seed, CacheNet **out) {
+  auto *G = new CacheNet();
+  tpt_status st = tpt_mlp_create(device, NRC_IN, NRC_NH, NRC_OUT, seed, &G->net);
+  if (st != TPT_OK) {
+    delete G;
+    return st;
+  }
+  *out = G;
+  return TPT_OK;
+}
+
+void cache_destroy(CacheNet *G) {
+  if (!G) return;
+  tpt_mlp_destroy(G->net);
+  if (G->x) cudaFree(G->x);
+  if (G->y) cudaFree(G->y);
+  if (G->target) cudaFree(G->target);
+  delete G;
+}
+
+tpt_status cache_train(CacheNet *G, const float4 *rec, int count, int steps, int batch, float lr, float3 lo,
+                       float3 ext, uint32_t key, cudaStream_t s) {
+  if (count <= 0 || steps <= 0) return TPT_OK;
+  batch = (batch + 15) / 16 * 16;
+  tpt_status st = cache_ws(G, batch);
+  if (st != TPT_OK) return st;
+  if ((st = ensure_ws(G->net, batch)) != TPT_OK) return st;
+  const float3 inv = make_float3(1.f / ext.x, 1.f / ext.y, 1.f / ext.z);
+  const float loss_scale = 1024.f;
+  for (int k = 0; k < steps; k++) {
+    k_nrc_encode_records<<<(batch + 255) / 256, 256, 0, s>>>(rec, count, batch, key, (uint32_t)(G->net->steps + 1),
+                                                             lo, inv, G->x, G->target);
+    LossRelL2 L{G->target, loss_scale / (float)batch};
+    st = launch_train<NRC_IN, NRC_NH, NRC_OUT>(G->net, G->x, batch, L, s);
+    if (st != TPT_OK) return st;
+    if ((st = tpt_mlp_adam(G->net, lr, 1.f / loss_scale, s)) != TPT_OK) return st;
+  }
+  float l = 0.f;
+  MLP_CUDA(cudaMemcpyAsync(&l, G->net->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+  MLP_CUDA(cudaStreamSynchronize(s));
+  G->last_loss = l / (float)batch;
+  return TPT_OK;
+}
+
+// Evaluates the cache for `count` queries (6 float4 each: the 4 feature
+// float4 then (throughput, pixel bits), unused); writes RGB rows of
+// NRC_OUT floats to *y_out (workspace owned by the cache).
+tpt_status cache_infer(CacheNet *G, const float4 *queries, int count, float3 lo, float3 ext, const float **y_out,
+                       cudaStream_t s) {
+  const int rows = (count + 15) / 16 * 16;
+  tpt_status st = cache_ws(G, rows);
+  if (st != TPT_OK) return st;
+  const float3 inv = make_float3(1.f / ext.x, 1.f / ext.y, 1.f / ext.z);
+  k_nrc_encode_queries<<<(rows + 255) / 256, 256, 0, s>>>(queries, count, rows, lo, inv, G->x);
+  st = launch_forward<NRC_IN, NRC_NH, NRC_OUT>(G->net, G->x, rows, G->y, s);
+  *y_out = G->y;
+  return st;
+}
+
+float cache_last_loss(const CacheNet *G) { return G->last_loss; }
 
 }  // namespace tpt
 
@@ -696,6 +885,24 @@ tpt_status tpt_mlp_backward_given(tpt_mlp *M, const void *x_f16, const float *dy
   if (M->in_dim == 112) return launch_train<112, 3, 48>(M, x, (int)rows, L, s);
   if (M->in_dim == 64) return launch_train<64, 5, 16>(M, x, (int)rows, L, s);
   return launch_train<32, 2, 16>(M, x, (int)rows, L, s);
+}
+
+tpt_status tpt_mlp_backward_vmf(tpt_mlp *M, const void *x_f16, const float *target, int64_t rows, float scale,
+                                float *loss_out, void *stream) {
+  if (!M || !x_f16 || !target || rows <= 0 || rows % 16 || rows > (1 << 26)) return TPT_ERR_INVALID_ARGUMENT;
+  if (M->in_dim != GUIDE_IN || M->n_hidden != GUIDE_NH || M->out_dim != GUIDE_OUT) return TPT_ERR_INVALID_ARGUMENT;
+  MLP_CUDA(cudaSetDevice(M->device));
+  tpt_status st = ensure_ws(M, (int)rows);
+  if (st != TPT_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  LossVmf L{(const float4 *)target, scale, nullptr, 0.f};
+  st = launch_train<GUIDE_IN, GUIDE_NH, GUIDE_OUT>(M, (const __half *)x_f16, (int)rows, L, s);
+  if (st != TPT_OK) return st;
+  if (loss_out) {
+    MLP_CUDA(cudaMemcpyAsync(loss_out, M->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+    MLP_CUDA(cudaStreamSynchronize(s));
+  }
+  return TPT_OK;
 }
 
 tpt_status tpt_mlp_adam(tpt_mlp *M, float lr, float inv_loss_scale, void *stream) {

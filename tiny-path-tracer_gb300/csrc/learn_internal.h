@@ -14,5 +14,14 @@ tpt_status guide_train(GuideNet *g, const float4 *records, int count, int steps,
                        float3 ext, uint64_t seed, cudaStream_t s);
 tpt_status guide_refresh(GuideNet *g, int res, float4 *table, cudaStream_t s);
 float guide_last_loss(const GuideNet *g);
+
+struct CacheNet;
+tpt_status cache_create(int device, uint64_t seed, CacheNet **out);
+void cache_destroy(CacheNet *g);
+tpt_status cache_train(CacheNet *g, const float4 *records, int count, int steps, int batch, float lr, float3 lo,
+                       float3 ext, uint32_t key, cudaStream_t s);
+tpt_status cache_infer(CacheNet *g, const float4 *queries, int count, float3 lo, float3 ext, const float **y_out,
+                       cudaStream_t s);
+float cache_last_loss(const CacheNet *g);
 }  // namespace tpt
 #endif

@@ -71,6 +71,11 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
   __half2 h = __floats2half2_rn(lo, hi);
   return *reinterpret_cast<uint32_t *>(&h);
 }
+// Gradients: saturate at the largest finite half instead of overflowing to
+// inf (an inf times a zero weight or mask becomes NaN in the next product).
+__device__ __forceinline__ uint32_t pack2_sat(float lo, float hi) {
+  return pack2(fminf(fmaxf(lo, -65504.f), 65504.f), fminf(fmaxf(hi, -65504.f), 65504.f));
+}
 __device__ __forceinline__ float2 unpack2(uint32_t v) {
   __half2 h = *reinterpret_cast<__half2 *>(&v);
   return __half22float2(h);

@@ -926,6 +926,14 @@ struct Compiler {
       if (S.light_i.empty()) S.has_lights = 0;  // empty list: reference UB; treated as no lights
     }
     if (!B.has_cam) return fail(TPT_ERR_INVALID_ARGUMENT, "no camera"), st;
+    {
+      box3 wb;
+      if (hbox(B, B.world, 0, 0, wb))
+        for (int i = 0; i < 3; i++) {
+          S.world_lo[i] = wb.mn.e[i];
+          S.world_hi[i] = wb.mx.e[i];
+        }
+    }
     S.cam = B.cam;
     // keep the BVH trees for topology dumps
     return st;

@@ -29,6 +29,7 @@ struct HostScene {
   std::vector<f4> light_f;
   int32_t light_is_list = 0, has_lights = 0;
   int32_t n_blas = 0, blas_depth = 0, max_stack = 0;
+  float world_lo[3] = {0, 0, 0}, world_hi[3] = {0, 0, 0};  // world bounding box (0 if none)
   Camera cam{};
 };
 

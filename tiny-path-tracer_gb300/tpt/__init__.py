@@ -61,6 +61,33 @@ class BatchItem(C.Structure):
                 ("out_rgb", C.c_void_p)]
 
 
+class GuideParams(C.Structure):
+    _fields_ = [("passes", C.c_int32), ("train_steps", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float),
+                ("grid_res", C.c_int32), ("alpha", C.c_float), ("record_cap", C.c_int32), ("seed", C.c_uint64)]
+
+
+class GuideStats(C.Structure):
+    _fields_ = [("render_ms", C.c_double), ("train_ms", C.c_double), ("final_loss", C.c_float),
+                ("records", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class NrcParams(C.Structure):
+    _fields_ = [("passes", C.c_int32), ("train_steps", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float),
+                ("terminate_depth", C.c_int32), ("train_stride", C.c_int32), ("record_cap", C.c_int32),
+                ("query_cap", C.c_int32), ("seed", C.c_uint64)]
+
+
+class NrcStats(C.Structure):
+    _fields_ = [("render_ms", C.c_double), ("infer_ms", C.c_double), ("train_ms", C.c_double),
+                ("final_loss", C.c_float), ("records", C.c_int64), ("queries", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 class SceneInfo(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("n_nodes", "n_leaves", "n_items", "n_blas", "n_materials",
                                          "n_textures", "n_lights", "max_stack")] + [("arena_bytes", C.c_int64)]
@@ -132,8 +159,16 @@ _SIGS = {
     "tpt_mlp_forward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "tpt_mlp_backward_given": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float,
                                            C.c_void_p]),
+    "tpt_mlp_backward_vmf": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float, C.c_void_p,
+                                         C.c_void_p]),
     "tpt_mlp_adam": (C.c_int32, [C.c_void_p, C.c_float, C.c_float, C.c_void_p]),
     "tpt_mlp_last_error": (C.c_char_p, []),
+    "tpt_guide_params_default": (None, [C.POINTER(GuideParams)]),
+    "tpt_render_guided": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.POINTER(GuideParams),
+                                      C.c_void_p, C.c_int32, C.POINTER(RenderStats), C.POINTER(GuideStats)]),
+    "tpt_nrc_params_default": (None, [C.POINTER(NrcParams)]),
+    "tpt_render_nrc": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.POINTER(NrcParams),
+                                   C.c_void_p, C.c_int32, C.POINTER(RenderStats), C.POINTER(NrcStats)]),
     "tpt_quantize": (None, [C.c_void_p, C.c_int64, C.c_void_p]),
     "tpt_write_ppm": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int32, C.c_int32]),
 }
@@ -264,6 +299,39 @@ class Context:
         return None, st.as_dict()
 
 
+def render_guided(ctx: "Context", slot: int, width: int, height: int, spp: int, max_depth: int = 50,
+                  background: int = BACKGROUND_BLACK, seed: int = 1, **guide):
+    """Learned path guiding (physical semantics).  guide: fields of
+    tpt_guide_params (passes, train_steps, batch, lr, grid_res, alpha,
+    record_cap, seed).  Returns (image, render stats, guide stats)."""
+    p = make_params(width, height, spp, max_depth, SEMANTICS_PHYSICAL, background, 1.0, seed)
+    g = GuideParams()
+    lib().tpt_guide_params_default(C.byref(g))
+    for k, v in guide.items():
+        setattr(g, k, v)
+    img = np.zeros((height, width, 3), np.float32)
+    st, gs = RenderStats(), GuideStats()
+    check(lib().tpt_render_guided(ctx._h, slot, C.byref(p), C.byref(g), _ptr(img), TPT_MEM_HOST, C.byref(st),
+                                  C.byref(gs)), "render_guided")
+    return img, st.as_dict(), gs.as_dict()
+
+
+def render_nrc(ctx: "Context", slot: int, width: int, height: int, spp: int, max_depth: int = 50,
+               semantics: int = SEMANTICS_PHYSICAL, background: int = BACKGROUND_BLACK, seed: int = 1, **nrc):
+    """Neural radiance cache render.  nrc: fields of tpt_nrc_params.
+    Returns (image, render stats, cache stats)."""
+    p = make_params(width, height, spp, max_depth, semantics, background, 1.0, seed)
+    n = NrcParams()
+    lib().tpt_nrc_params_default(C.byref(n))
+    for k, v in nrc.items():
+        setattr(n, k, v)
+    img = np.zeros((height, width, 3), np.float32)
+    st, ns = RenderStats(), NrcStats()
+    check(lib().tpt_render_nrc(ctx._h, slot, C.byref(p), C.byref(n), _ptr(img), TPT_MEM_HOST, C.byref(st),
+                               C.byref(ns)), "render_nrc")
+    return img, st.as_dict(), ns.as_dict()
+
+
 def render_batch(ctx: "Context", jobs, max_depth=50, semantics=SEMANTICS_REFERENCE, background=BACKGROUND_BLACK,
                  sky_scale=1.0, seed=1, block=0, variant=0, flat_nodes=0, profile=False, outs=None):
     """jobs: list of (slot, width, height, spp).  outs: None -> host images are
@@ -358,6 +426,12 @@ class Mlp:
     def backward_given(self, x_f16_ptr: int, dy_ptr: int, rows: int, scale: float = 1.0) -> None:
         check(lib().tpt_mlp_backward_given(self._h, C.c_void_p(x_f16_ptr), C.c_void_p(dy_ptr), rows, scale, None),
               "mlp_backward")
+
+    def backward_vmf(self, x_f16_ptr: int, target_ptr: int, rows: int, scale: float = 1.0) -> float:
+        loss = C.c_float()
+        check(lib().tpt_mlp_backward_vmf(self._h, C.c_void_p(x_f16_ptr), C.c_void_p(target_ptr), rows, scale,
+                                         C.byref(loss), None), "mlp_backward_vmf")
+        return loss.value
 
     def adam(self, lr: float, inv_loss_scale: float = 1.0) -> None:
         check(lib().tpt_mlp_adam(self._h, lr, inv_loss_scale, None), "mlp_adam")
