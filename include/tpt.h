@@ -328,6 +328,12 @@ typedef struct {
 void tpt_guide_params_default(tpt_guide_params *g);
 tpt_status tpt_render_guided(tpt_context *ctx, int32_t slot, const tpt_render_params *p, const tpt_guide_params *g,
                              float *out_rgb, int32_t mem, tpt_render_stats *stats, tpt_guide_stats *gstats);
+/* Training records of the last pass of the last tpt_render_guided call on
+ * this context, copied to host memory: up to `cap` records of 12 floats,
+ * (position, weight), (normal, 0), (sampled direction, 0).  *count receives
+ * the number available.  For tests and diagnostics (no counterpart in the
+ * reference). */
+tpt_status tpt_guide_records(tpt_context *ctx, float *out, int64_t cap, int64_t *count);
 
 /* Neural radiance cache (no counterpart in the reference).  Rendered in
  * `passes` passes; in every pass after the first, a path that reaches its

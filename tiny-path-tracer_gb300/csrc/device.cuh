@@ -461,9 +461,11 @@ __device__ bool trace_closest(const DevScene &S, const Ray &wr, float tmin, int2
           }
           continue;
         }
-        // internal node: test the child boxes, push near child last
-        const f4 lo = ldg4(S.node_lo + e.x), hi = ldg4(S.node_hi + e.x);
-        const int left = __float_as_int(lo.w), right = __float_as_int(hi.w);
+        // internal node: test the child boxes (stored with the node, one
+        // 64-byte record), push near child last
+        const f4 *kid = S.node_kids + 4 * (size_t)e.x;
+        const f4 k0 = ldg4(kid), k1 = ldg4(kid + 1), k2 = ldg4(kid + 2), k3 = ldg4(kid + 3);
+        const int left = __float_as_int(k0.w), right = __float_as_int(k2.w);
         int2 q[2];
         float ent[2];
         int nq = 0;
@@ -472,7 +474,7 @@ __device__ bool trace_closest(const DevScene &S, const Ray &wr, float tmin, int2
           if (c == 1 && right == left) break;  // n == 1 node: left_ == right_
           if (ref >= 0) {
             float en;
-            const f4 clo = ldg4(S.node_lo + ref), chi = ldg4(S.node_hi + ref);
+            const f4 clo = c == 0 ? k0 : k2, chi = c == 0 ? k1 : k3;
             if (slab(curp, clo, chi, tmin, tmax, en)) {
               ent[nq] = en;
               q[nq++] = make_int2(ref, __float_as_int(prune_key(curp, clo, chi, en)));
@@ -865,6 +867,8 @@ __device__ __forceinline__ float3 background(const RenderCfg &cfg, const Ray &r)
   const float t = (ud.y + 1.0f) * 0.5f;
   return cfg.sky_scale * ((1.f - t) * v3(1.f, 1.f, 1.f) + t * v3(0.5f, 0.7f, 1.0f));
 }
+
+__device__ __forceinline__ bool finite3(float3 v) { return isfinite(v.x) && isfinite(v.y) && isfinite(v.z); }
 
 __device__ __forceinline__ bool nonzero(float3 e) { return e.x != 0.f || e.y != 0.f || e.z != 0.f; }
 

@@ -419,15 +419,17 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
           const float3 c = v3((L.x - rec.L.x) / rec.T.x, (L.y - rec.L.y) / rec.T.y, (L.z - rec.L.z) / rec.T.z);
           float wgt = (c.x + c.y + c.z) * (1.f / 3.f);
           if (!(wgt >= 0.f) || !(wgt < 1e6f)) wgt = 0.f;
-          emit = true;
+          // a NaN direction (the reference's sphere cone sampling from inside
+          // the sphere) or position would poison a whole training batch
+          emit = finite3(rec.x) && finite3(rec.n) && finite3(rec.d);
           r0 = make_float4(rec.x.x, rec.x.y, rec.x.z, wgt);
           r1 = make_float4(rec.n.x, rec.n.y, rec.n.z, 0.f);
           r2 = make_float4(rec.d.x, rec.d.y, rec.d.z, 0.f);
         }
       }
     }
-    const unsigned slot = warp_append(emit, rec_count);
-    if (emit && slot < rec_cap) {
+    const unsigned slot = warp_append(emit, rec_count) % rec_cap;  // ring: the newest records win
+    if (emit) {
       records[3 * (size_t)slot] = r0;
       records[3 * (size_t)slot + 1] = r1;
       records[3 * (size_t)slot + 2] = r2;
@@ -560,7 +562,7 @@ __global__ void k_nrc_accumulate(const float4 *__restrict__ queries, const float
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
     const float4 tq = queries[6 * (size_t)i + 4];
     const float *c = y + (size_t)i * 16;
-    const float3 L = v3(tq.x * fmaxf(c[0], 0.f), tq.y * fmaxf(c[1], 0.f), tq.z * fmaxf(c[2], 0.f));
+    const float3 L = de_nan(v3(tq.x * fmaxf(c[0], 0.f), tq.y * fmaxf(c[1], 0.f), tq.z * fmaxf(c[2], 0.f)));
     accumulate(F, (uint32_t)__float_as_int(tq.w), L);
   }
 }
@@ -617,6 +619,7 @@ struct tpt_context {
   DevBuf path[2], hits, accum, accum64, staging, rays, hitf, hiti;
   DevBuf batch_table, batch_accum, batch_staging;
   DevBuf guide_table, guide_records, guide_count;
+  long long guide_last_count = 0;  // records of the last guided pass
   GuideNet *guide = nullptr;
   DevBuf nrc_records, nrc_queries, nrc_counts;
   CacheNet *cache = nullptr;
@@ -745,6 +748,39 @@ tpt_status tpt_context_set_option(tpt_context *c, int32_t option, int64_t value)
   return TPT_ERR_INVALID_ARGUMENT;
 }
 
+// Device view of a scene whose arena (layout L) starts at `base`.
+static DevScene dev_scene_at(const HostScene &S, const ArenaLayout &L, uint8_t *base) {
+  DevScene d{};
+  d.node_lo = (const f4 *)(base + L.off[0]);
+  d.node_hi = (const f4 *)(base + L.off[1]);
+  d.node_skip = (const int32_t *)(base + L.off[2]);
+  d.leaf_hdr = (const i4 *)(base + L.off[3]);
+  d.leaf_user = (const int32_t *)(base + L.off[4]);
+  d.leaf_data = (const f4 *)(base + L.off[5]);
+  d.items = (const i2 *)(base + L.off[6]);
+  d.mat_i = (const i4 *)(base + L.off[7]);
+  d.mat_f = (const f4 *)(base + L.off[8]);
+  d.tex_i = (const i4 *)(base + L.off[9]);
+  d.tex_f = (const f4 *)(base + L.off[10]);
+  d.images = base + L.off[11];
+  d.perlin_grad = (const f4 *)(base + L.off[12]);
+  d.perlin_perm = (const int32_t *)(base + L.off[13]);
+  d.light_i = (const i4 *)(base + L.off[14]);
+  d.light_f = (const f4 *)(base + L.off[15]);
+  d.node_kids = (const f4 *)(base + L.off[16]);
+  d.flat_max = DEFAULT_FLAT_MAX;
+  d.n_nodes = (int32_t)S.node_lo.size();
+  d.n_leaves = (int32_t)S.leaf_hdr.size();
+  d.n_items = (int32_t)S.items.size();
+  d.n_mats = (int32_t)S.mat_i.size();
+  d.n_texs = (int32_t)S.tex_i.size();
+  d.n_lights = (int32_t)S.light_i.size();
+  d.light_is_list = S.light_is_list;
+  d.has_lights = S.has_lights;
+  d.cam = S.cam;
+  return d;
+}
+
 tpt_status tpt_scene_upload(tpt_context *c, const tpt_scene *sc, int32_t *slot) {
   if (!c || !sc || !slot) return TPT_ERR_INVALID_ARGUMENT;
   const HostScene &S = *host_scene(sc);
@@ -765,33 +801,7 @@ tpt_status tpt_scene_upload(tpt_context *c, const tpt_scene *sc, int32_t *slot) 
   }
   s.bytes = L.total;
   uint8_t *base = (uint8_t *)s.arena;
-  DevScene &d = s.ds;
-  d.node_lo = (const f4 *)(base + L.off[0]);
-  d.node_hi = (const f4 *)(base + L.off[1]);
-  d.node_skip = (const int32_t *)(base + L.off[2]);
-  d.leaf_hdr = (const i4 *)(base + L.off[3]);
-  d.leaf_user = (const int32_t *)(base + L.off[4]);
-  d.leaf_data = (const f4 *)(base + L.off[5]);
-  d.items = (const i2 *)(base + L.off[6]);
-  d.mat_i = (const i4 *)(base + L.off[7]);
-  d.mat_f = (const f4 *)(base + L.off[8]);
-  d.tex_i = (const i4 *)(base + L.off[9]);
-  d.tex_f = (const f4 *)(base + L.off[10]);
-  d.images = base + L.off[11];
-  d.perlin_grad = (const f4 *)(base + L.off[12]);
-  d.perlin_perm = (const int32_t *)(base + L.off[13]);
-  d.light_i = (const i4 *)(base + L.off[14]);
-  d.light_f = (const f4 *)(base + L.off[15]);
-  d.flat_max = DEFAULT_FLAT_MAX;
-  d.n_nodes = (int32_t)S.node_lo.size();
-  d.n_leaves = (int32_t)S.leaf_hdr.size();
-  d.n_items = (int32_t)S.items.size();
-  d.n_mats = (int32_t)S.mat_i.size();
-  d.n_texs = (int32_t)S.tex_i.size();
-  d.n_lights = (int32_t)S.light_i.size();
-  d.light_is_list = S.light_is_list;
-  d.has_lights = S.has_lights;
-  d.cam = S.cam;
+  s.ds = dev_scene_at(S, L, base);
   for (int i = 0; i < 3; i++) {
     s.world_lo[i] = S.world_lo[i];
     s.world_hi[i] = S.world_hi[i];
@@ -1299,6 +1309,9 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
   double render_ms = 0.0, train_ms = 0.0;
   long long records = 0, segments = 0;
   TPT_CUDA(cudaMemsetAsync(c->accum.p, 0, npix * sizeof(float4), c->stream));
+  // records accumulate over the passes in a ring of record_cap entries
+  TPT_CUDA(cudaMemsetAsync(c->guide_count.p, 0, sizeof(unsigned), c->stream));
+  unsigned emitted_before = 0;
   bool have_table = false;
   tpt_status result = TPT_OK;
   for (int pass = 0; pass < g->passes && result == TPT_OK; pass++) {
@@ -1307,7 +1320,6 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
     WfCounters init{};
     std::memcpy(c->counters_host, &init, sizeof(init));
     cudaMemcpyAsync(c->counters, c->counters_host, sizeof(WfCounters), cudaMemcpyHostToDevice, c->stream);
-    cudaMemsetAsync(c->guide_count.p, 0, sizeof(unsigned), c->stream);
     cudaEventRecord(e[0], c->stream);
     kern<<<grid, block, smem, c->stream>>>(S, cfg, F, c->counters, gv, (uint32_t)(pass * spp_pass),
                                           (float4 *)c->guide_records.p, (unsigned *)c->guide_count.p,
@@ -1327,8 +1339,10 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
       break;
     }
     segments += (long long)c->counters_host->segments;
-    count = std::min<unsigned>(count, (unsigned)g->record_cap);
-    records += count;
+    records += (unsigned)(count - emitted_before);  // emitted by this pass (counter wraps mod 2^32)
+    emitted_before = count;
+    count = (unsigned)std::min<long long>(records, g->record_cap);  // held in the ring
+    c->guide_last_count = count;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e[0], e[1]);
     render_ms += ms;
@@ -1377,6 +1391,19 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
 }
 
 // ============================================== neural radiance cache =====
+extern "C" tpt_status tpt_guide_records(tpt_context *c, float *out, int64_t cap, int64_t *count) {
+  if (!c || !count || cap < 0 || (cap > 0 && !out)) return TPT_ERR_INVALID_ARGUMENT;
+  *count = c->guide_last_count;
+  const long long n = std::min<long long>(cap, c->guide_last_count);
+  if (n > 0) {
+    TPT_CUDA(cudaSetDevice(c->device));
+    TPT_CUDA(cudaMemcpyAsync(out, c->guide_records.p, (size_t)n * 3 * sizeof(float4), cudaMemcpyDeviceToHost,
+                             c->stream));
+    TPT_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  return TPT_OK;
+}
+
 extern "C" void tpt_nrc_params_default(tpt_nrc_params *n) {
   if (!n) return;
   n->passes = 8;
@@ -1593,33 +1620,8 @@ extern "C" tpt_status tpt_render_noalloc(const tpt_scene *scene, void *arena_dev
   uint8_t *base = (uint8_t *)arena_dev;
   for (int i = 0; i < ARENA_SECTIONS; i++)
     if (sec[i].bytes) TPT_CUDA(cudaMemcpyAsync(base + L.off[i], sec[i].data, sec[i].bytes, cudaMemcpyHostToDevice, stream));
-  DevScene d{};
-  d.node_lo = (const f4 *)(base + L.off[0]);
-  d.node_hi = (const f4 *)(base + L.off[1]);
-  d.node_skip = (const int32_t *)(base + L.off[2]);
-  d.leaf_hdr = (const i4 *)(base + L.off[3]);
-  d.leaf_user = (const int32_t *)(base + L.off[4]);
-  d.leaf_data = (const f4 *)(base + L.off[5]);
-  d.items = (const i2 *)(base + L.off[6]);
-  d.mat_i = (const i4 *)(base + L.off[7]);
-  d.mat_f = (const f4 *)(base + L.off[8]);
-  d.tex_i = (const i4 *)(base + L.off[9]);
-  d.tex_f = (const f4 *)(base + L.off[10]);
-  d.images = base + L.off[11];
-  d.perlin_grad = (const f4 *)(base + L.off[12]);
-  d.perlin_perm = (const int32_t *)(base + L.off[13]);
-  d.light_i = (const i4 *)(base + L.off[14]);
-  d.light_f = (const f4 *)(base + L.off[15]);
-  d.n_nodes = (int32_t)H.node_lo.size();
-  d.n_leaves = (int32_t)H.leaf_hdr.size();
-  d.n_items = (int32_t)H.items.size();
-  d.n_mats = (int32_t)H.mat_i.size();
-  d.n_texs = (int32_t)H.tex_i.size();
-  d.n_lights = (int32_t)H.light_i.size();
-  d.light_is_list = H.light_is_list;
-  d.has_lights = H.has_lights;
+  DevScene d = dev_scene_at(H, L, base);
   d.flat_max = p->flat_nodes > 0 ? p->flat_nodes : DEFAULT_FLAT_MAX;
-  d.cam = H.cam;
 
   // the scratch keeps the previous call's contents: clear accumulators and counters
   float4 *accum = (float4 *)scratch;

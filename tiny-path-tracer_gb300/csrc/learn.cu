@@ -330,6 +330,10 @@ struct LossVmf {
     }
     p = fmaxf(p, 1e-30f);
     const float wn = wsum ? tg.w / fmaxf(*wsum, 1e-30f) : tg.w;
+    if (wn == 0.f) {  // no contribution, no gradient (whatever the outputs)
+      for (int o = 0; o < OUT; o++) dy[o] = 0.f;
+      return 0.f;
+    }
     float n2 = 0.f;
     for (int i = 0; i < GUIDE_LOBES; i++) {
       const float r = logit[i] * f[i] / p;
@@ -353,6 +357,10 @@ struct LossVmf {
   }
 };
 
+__device__ __forceinline__ bool finite4(float4 v) {
+  return isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(v.w);
+}
+
 // Training rows: a random record per row (with replacement), encoded.
 __global__ void k_guide_encode_records(const float4 *__restrict__ rec, int count, int rows, uint2 key, uint32_t step,
                                        float3 lo, float3 inv_ext, __half *__restrict__ X, float4 *__restrict__ target,
@@ -362,7 +370,11 @@ __global__ void k_guide_encode_records(const float4 *__restrict__ rec, int count
     uint32_t h = (uint32_t)r * 0x9E3779B1u ^ (step * 0x85EBCA77u) ^ key.x;
     h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12; h *= 0x297A2D39u; h ^= h >> 15;
     const int idx = (int)(h % (uint32_t)count);
-    const float4 xw = rec[3 * idx], nn = rec[3 * idx + 1], dd = rec[3 * idx + 2];
+    float4 xw = rec[3 * idx], nn = rec[3 * idx + 1], dd = rec[3 * idx + 2];
+    if (!(finite4(xw) && finite4(nn) && finite4(dd) && xw.w >= 0.f)) {  // an unusable record: zero weight
+      xw = make_float4(lo.x, lo.y, lo.z, 0.f);
+      nn = dd = make_float4(0.f, 0.f, 1.f, 0.f);
+    }
     const float3 xn = make_float3((xw.x - lo.x) * inv_ext.x, (xw.y - lo.y) * inv_ext.y, (xw.z - lo.z) * inv_ext.z);
     guide_encode(xn, make_float3(nn.x, nn.y, nn.z), X + (size_t)r * GUIDE_IN);
     target[r] = make_float4(dd.x, dd.y, dd.z, xw.w);
@@ -432,23 +444,27 @@ __global__ void k_guide_post(const float *__restrict__ Y, int rows_valid, float4
 // (albedo, 0); training targets float4 (rgb, 0).
 constexpr int NRC_IN = 64, NRC_NH = 5, NRC_OUT = 16, NRC_BINS = 16;
 
+__device__ __forceinline__ __half fin16(float v) {  // non-finite features encode as 0
+  return __float2half_rn(isfinite(v) ? fminf(fmaxf(v, -65504.f), 65504.f) : 0.f);
+}
+
 __device__ __forceinline__ void nrc_encode(const float4 *f, float3 lo, float3 inv_ext, __half *out) {
   const float c[3] = {(f[0].x - lo.x) * inv_ext.x, (f[0].y - lo.y) * inv_ext.y, (f[0].z - lo.z) * inv_ext.z};
 #pragma unroll
   for (int a = 0; a < 3; a++) {
-    const float u = fminf(fmaxf(c[a], 0.f), 1.f) * NRC_BINS;
+    const float u = fminf(fmaxf(c[a], 0.f), 1.f) * NRC_BINS;  // NaN -> 0
     for (int b = 0; b < NRC_BINS; b++) out[a * NRC_BINS + b] = __float2half_rn(fmaxf(0.f, 1.f - fabsf(u - (b + 0.5f))));
   }
-  out[48] = __float2half_rn(f[1].x);
-  out[49] = __float2half_rn(f[1].y);
-  out[50] = __float2half_rn(f[1].z);
-  out[51] = __float2half_rn(f[2].x);
-  out[52] = __float2half_rn(f[2].y);
-  out[53] = __float2half_rn(f[2].z);
-  out[54] = __float2half_rn(f[3].x);
-  out[55] = __float2half_rn(f[3].y);
-  out[56] = __float2half_rn(f[3].z);
-  out[57] = __float2half_rn(f[0].w);
+  out[48] = fin16(f[1].x);
+  out[49] = fin16(f[1].y);
+  out[50] = fin16(f[1].z);
+  out[51] = fin16(f[2].x);
+  out[52] = fin16(f[2].y);
+  out[53] = fin16(f[2].z);
+  out[54] = fin16(f[3].x);
+  out[55] = fin16(f[3].y);
+  out[56] = fin16(f[3].z);
+  out[57] = fin16(f[0].w);
   for (int i = 58; i < NRC_IN; i++) out[i] = __float2half_rn(0.f);
 }
 
@@ -481,7 +497,8 @@ __global__ void k_nrc_encode_records(const float4 *__restrict__ rec, int count, 
     h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12; h *= 0x297A2D39u; h ^= h >> 15;
     const int idx = (int)(h % (uint32_t)count);
     nrc_encode(rec + 5 * (size_t)idx, lo, inv_ext, X + (size_t)r * NRC_IN);
-    target[r] = rec[5 * (size_t)idx + 4];
+    const float4 t = rec[5 * (size_t)idx + 4];
+    target[r] = finite4(t) ? t : make_float4(0.f, 0.f, 0.f, 0.f);
   }
 }
 

@@ -908,6 +908,24 @@ struct Compiler {
         S.items.push_back(i2{ITEM_LEAF, leaf});
       }
     }
+    // child boxes of every node, for the stack walk: one 64-byte load per
+    // popped node gives both children's boxes and references
+    S.node_kids.assign(4 * S.node_lo.size(), f4{0, 0, 0, 0});
+    for (size_t i = 0; i < S.node_lo.size(); i++) {
+      int32_t ref[2];
+      std::memcpy(&ref[0], &S.node_lo[i].w, 4);
+      std::memcpy(&ref[1], &S.node_hi[i].w, 4);
+      for (int c = 0; c < 2; c++) {
+        f4 lo{0, 0, 0, 0}, hi{0, 0, 0, 0};
+        if (ref[c] >= 0) {
+          lo = S.node_lo[ref[c]];
+          hi = S.node_hi[ref[c]];
+        }
+        std::memcpy(&lo.w, &ref[c], 4);
+        S.node_kids[4 * i + 2 * c] = lo;
+        S.node_kids[4 * i + 2 * c + 1] = hi;
+      }
+    }
     // stack bound: both children of every level plus the instance marker
     S.max_stack = top_depth + 2 + (S.n_blas ? S.blas_depth + 2 : 0);
     if (S.max_stack > TRAVERSAL_STACK)

@@ -14,6 +14,7 @@ namespace tpt {
 struct HostScene {
   std::vector<f4> node_lo, node_hi;
   std::vector<int32_t> node_skip;  // pre-order index just past each node's subtree
+  std::vector<f4> node_kids;       // per node: {left lo, ref}, {left hi}, {right lo, ref}, {right hi}
   std::vector<i4> leaf_hdr;
   std::vector<int32_t> leaf_user;
   std::vector<f4> leaf_data;
@@ -34,7 +35,7 @@ struct HostScene {
 };
 
 // Sections of the device arena, each 256-byte aligned, in DevScene order.
-enum { ARENA_SECTIONS = 16 };
+enum { ARENA_SECTIONS = 17 };
 struct ArenaSection {
   const void *data;
   size_t bytes;
@@ -56,7 +57,8 @@ inline void arena_sections(const HostScene &S, ArenaSection out[ARENA_SECTIONS])
       {S.perlin_grad.data(), S.perlin_grad.size() * sizeof(f4)},
       {S.perlin_perm.data(), S.perlin_perm.size() * sizeof(int32_t)},
       {S.light_i.data(), S.light_i.size() * sizeof(i4)},
-      {S.light_f.data(), S.light_f.size() * sizeof(f4)}};
+      {S.light_f.data(), S.light_f.size() * sizeof(f4)},
+      {S.node_kids.data(), S.node_kids.size() * sizeof(f4)}};
   for (int i = 0; i < ARENA_SECTIONS; i++) out[i] = t[i];
 }
 

@@ -166,6 +166,7 @@ _SIGS = {
     "tpt_guide_params_default": (None, [C.POINTER(GuideParams)]),
     "tpt_render_guided": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.POINTER(GuideParams),
                                       C.c_void_p, C.c_int32, C.POINTER(RenderStats), C.POINTER(GuideStats)]),
+    "tpt_guide_records": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     "tpt_nrc_params_default": (None, [C.POINTER(NrcParams)]),
     "tpt_render_nrc": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.POINTER(NrcParams),
                                    C.c_void_p, C.c_int32, C.POINTER(RenderStats), C.POINTER(NrcStats)]),
@@ -314,6 +315,18 @@ def render_guided(ctx: "Context", slot: int, width: int, height: int, spp: int, 
     check(lib().tpt_render_guided(ctx._h, slot, C.byref(p), C.byref(g), _ptr(img), TPT_MEM_HOST, C.byref(st),
                                   C.byref(gs)), "render_guided")
     return img, st.as_dict(), gs.as_dict()
+
+
+def guide_records(ctx: "Context", cap: int = 1 << 22) -> np.ndarray:
+    """Training records of the last guided pass: (n, 12) float32 rows of
+    (position, weight, normal, 0, direction, 0)."""
+    n = C.c_int64()
+    check(lib().tpt_guide_records(ctx._h, None, 0, C.byref(n)), "guide_records")
+    k = min(int(n.value), cap)
+    out = np.zeros((k, 12), np.float32)
+    if k:
+        check(lib().tpt_guide_records(ctx._h, _ptr(out), k, C.byref(n)), "guide_records")
+    return out
 
 
 def render_nrc(ctx: "Context", slot: int, width: int, height: int, spp: int, max_depth: int = 50,
