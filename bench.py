@@ -16,6 +16,11 @@ e2e:    the same frame through the C ABI with host buffers: scene-arena upload
 cpu_baseline / --impl reference: the reference algorithm on the host cores
         (oracle/_ref linked from the reference sources when it was built here,
         else the CPU oracle port), on a bounded band of image rows.
+learned_equal_time: the second half of the metric - relMSE against an FP64
+        high-spp render of the learned renderers (path guiding on the small-
+        light Cornell box, the radiance cache on the next-week scene) next to
+        the plain tracer at equal spp and at equal wall time (skip with
+        --no-learned).
 Multi-GPU: N independent replicas (one frame each per step), scaling "weak".
 """
 from __future__ import annotations
@@ -231,6 +236,69 @@ def batch_bench(args) -> None:
     ctx.close()
 
 
+def _relmse(x, ref, eps=1e-2) -> float:
+    """mean over pixels and channels of (x - ref)^2 / (ref^2 + eps), eps 1e-2"""
+    return float(np.mean((x.astype(np.float64) - ref) ** 2 / (ref.astype(np.float64) ** 2 + eps)))
+
+
+def learned_equal_time(ctx, which: str) -> dict:
+    """Equal-time comparison of a learned renderer against the plain tracer,
+    both scored by relMSE against an FP64-accumulated high-spp plain render
+    (physical semantics).  Times are wall-clock milliseconds of the whole
+    call (training, table refresh / cache inference included), images left
+    on the device.
+
+    guided: Cornell box with the 40x40 light and the second box, 600x600,
+            plain at 1024 spp against guided at the spp that takes the same
+            time (alpha 0.5, the 50/50 MIS of the configuration); FP64
+            reference 16384 spp.
+    nrc:    the seeded next-week scene, 800x800, plain at 256 spp against the
+            cached renderer (paths terminated into the cache after 2 bounces)
+            at the spp that takes the same time; FP64 reference 4096 spp.
+    The reference's own noise adds ~spp/ref_spp of the plain relMSE to both."""
+    import torch
+    import tpt
+    from tpt import scenes
+
+    if which == "guided":
+        sd, w, h, spp, ref_spp = scenes.cornell_guiding(), 600, 600, 1024, 16384
+        run = lambda n, out: tpt.render_guided(ctx, slot, w, h, n, seed=5, out=out)
+    else:
+        sd, w, h, spp, ref_spp = scenes.next_week(), 800, 800, 256, 4096
+        run = lambda n, out: tpt.render_nrc(ctx, slot, w, h, n, seed=5, out=out)
+    slot = ctx.upload(tpt.Scene(sd.text()))
+    dev = torch.empty((h, w, 3), dtype=torch.float32, device="cuda")
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) * 1e3, r
+
+    ref, _ = ctx.render(slot, w, h, ref_spp, semantics=tpt.SEMANTICS_PHYSICAL, seed=999, fp64=True)
+    plain = lambda n: ctx.render(slot, w, h, n, semantics=tpt.SEMANTICS_PHYSICAL, seed=5, out=dev.data_ptr())
+    plain(spp)  # warm-up
+    t_plain, _ = timed(lambda: plain(spp))
+    e_plain = _relmse(dev.cpu().numpy(), ref)
+    run(spp, dev.data_ptr())  # warm-up
+    t_eq, r = timed(lambda: run(spp, dev.data_ptr()))
+    e_eq = _relmse(dev.cpu().numpy(), ref)
+    passes = 8
+    spp_et = max(passes, int(round(spp * t_plain / t_eq / passes)) * passes)
+    t_et, r2 = timed(lambda: run(spp_et, dev.data_ptr()))
+    e_et = _relmse(dev.cpu().numpy(), ref)
+    ctx.release(slot)
+    name = "cornell_40x40_light_two_boxes" if which == "guided" else "next_week_final_seeded"
+    return {"scene": name, "width": w, "height": h, "ref_spp_fp64": ref_spp,
+            "plain": {"spp": spp, "ms": t_plain, "relmse": e_plain},
+            which: {"spp": spp, "ms": t_eq, "relmse": e_eq, "stats": r[2]},
+            which + "_equal_time": {"spp": spp_et, "ms": t_et, "relmse": e_et},
+            "equal_spp_relmse_ratio": e_eq / e_plain,
+            "equal_time_relmse_ratio": e_et / e_plain,
+            "time_ratio_at_equal_spp": t_eq / t_plain}
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -241,6 +309,8 @@ def main() -> None:
     ap.add_argument("--wave", type=int, default=0)
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the equal-time guided / cached comparisons of the default line")
     ap.add_argument("--spp", type=int, default=SPP, help="smaller cases for profiling only")
     ap.add_argument("--workload", default="cornell", choices=["cornell", "batch"],
                     help="cornell: the headline workload; batch: 64 seeded random-sphere scenes in one launch")
@@ -330,6 +400,15 @@ def main() -> None:
         e2e_times.append(time.perf_counter() - t0)
     e2e_value = W * H * args.spp / float(np.mean(e2e_times)) / 1e6
 
+    learned = None
+    if rank == 0 and not args.no_learned and args.spp == SPP:
+        learned = {}
+        for which in ("guided", "nrc"):
+            try:
+                learned[which] = learned_equal_time(ctx, which)
+            except Exception as e:  # reported, never fatal to the throughput line
+                learned[which] = {"error": str(e)}
+
     peaks = _peaks()
     roof = None
     if tr_n > 0 and tr_ms > 0:
@@ -362,7 +441,8 @@ def main() -> None:
                           "segments_per_step": segs / args.steps},
                "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": int(arena_bytes),
                        "d2h_bytes_per_step": int(W * H * 3 * 4)},
-               "gpu_launches": int(launches), "clocks": clk, "roofline": roof, "cpu_baseline": cpu}
+               "gpu_launches": int(launches), "clocks": clk, "roofline": roof, "cpu_baseline": cpu,
+               "learned_equal_time": learned}
         print(json.dumps(out))
     ctx.close()
     if dist is not None:

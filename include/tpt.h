@@ -348,10 +348,10 @@ tpt_status tpt_guide_records(tpt_context *ctx, float *out, int64_t cap, int64_t 
  * The estimator is biased by the cache's error; the plain tracer is its
  * fallback and its judge. */
 typedef struct {
-  int32_t passes;
-  int32_t train_steps;
-  int32_t batch;
-  float lr;
+  int32_t passes;           /* >= 1 (8) */
+  int32_t train_steps;      /* Adam steps after each pass (128) */
+  int32_t batch;            /* training rows per step (16384) */
+  float lr;                 /* Adam learning rate (1e-3) */
   int32_t terminate_depth;  /* 2: two bounces, then the cache */
   int32_t train_stride;     /* every n-th path trains the cache (16) */
   int32_t record_cap;       /* training records per pass */

@@ -50,7 +50,7 @@ enum { MAX_INSTANCE_OPS = 4 };
 enum ItemKind : int32_t { ITEM_BVH = 0, ITEM_LEAF = 1 };
 
 enum MatType : int32_t { MT_LAMBERTIAN = 1, MT_METAL = 2, MT_DIELECTRIC = 3, MT_LIGHT = 4, MT_ISOTROPIC = 5 };
-// mat_i = {type, tex, 0, 0}; mat_f = {albedo.xyz, fuzz} (metal) | {ior,0,0,0}
+// mat_i = {type, tex, 0, reads_uv (1 if the texture tree holds an image)}; mat_f = {albedo.xyz, fuzz} (metal) | {ior,0,0,0}
 
 enum TexType : int32_t { TT_CONST = 1, TT_CHECKER = 2, TT_PERLIN = 3, TT_IMAGE = 4 };
 // tex_i = {type, a, b, c}: checker {odd, even}; image {w, h, byte offset}
@@ -92,6 +92,9 @@ struct DevScene {
   int32_t flat_max;  // BVH items of at most this many nodes use the stackless walk
   Camera cam;
 };
+
+// float4 per entry of the path-guiding lobe table: 8 lobes + 2 of weight sums.
+enum { GUIDE_ENTRY = 10 };
 
 // Default size limit of the stackless pre-order walk (tuned per render).
 enum { DEFAULT_FLAT_MAX = 48 };

@@ -371,6 +371,8 @@ __device__ __forceinline__ bool beats(float t, int outer, int inner, float bt, i
 // instanced BVH is entered when its leaf is popped).  Leaves go through the
 // stack too, so the primitive tests have a single call site.
 enum { STK_RESTORE = -1 };
+// Stackless walks over at most this many nodes skip the pruning test.
+enum { FLAT_PRUNE_MIN = 32 };
 
 // Closest hit of the world for ray wr over [tmin, FLT_MAX] with the exact
 // semantics of hitable_list::hit across the top-level items (sequential,
@@ -497,10 +499,12 @@ __device__ bool trace_closest(const DevScene &S, const Ray &wr, float tmin, int2
       const int root = item.y;
       const int end = __ldg(S.node_skip + root);
       if (end - root <= S.flat_max) {
+        // pruning pays only on trees with more than a few boxes per path
+        const bool prune = end - root > FLAT_PRUNE_MIN;
         for (int i = root; i < end && !overflow;) {
           const f4 lo = ldg4(S.node_lo + i), hi = ldg4(S.node_hi + i);
           float en;
-          if (slab(W, lo, hi, tmin, tmax, en) && !(prune_key(W, lo, hi, en) > bt)) {
+          if (slab(W, lo, hi, tmin, tmax, en) && !(prune && prune_key(W, lo, hi, en) > bt)) {
             const int left = __float_as_int(lo.w), right = __float_as_int(hi.w);
             if (right < 0) push(-2 - ~right, never_pruned);
             if (left < 0 && left != right) push(-2 - ~left, never_pruned);
@@ -549,7 +553,10 @@ __device__ __forceinline__ void uv_map(float3 q, float &u, float &v) {
 // functions fill in, from the traversal result: the instance's object-space
 // ray is recomputed with the same operations, the primitive's record is
 // formed in object space and carried back to world (rect_box.cc:183-190).
-__device__ void finalize(const DevScene &S, const Ray &wr, const HitRef &h, Surface &s) {
+// all_uv: compute (u, v) for every hit (the closest-hit API reports them);
+// otherwise only where the material's texture reads them (image textures),
+// which spares renders the sphere's atan2/asin and the rect's two divisions.
+__device__ void finalize(const DevScene &S, const Ray &wr, const HitRef &h, Surface &s, bool all_uv = true) {
   Ray r = wr;
   const f4 *idata = nullptr;
   int nops = 0;
@@ -566,12 +573,15 @@ __device__ void finalize(const DevScene &S, const Ray &wr, const HitRef &h, Surf
   const float t = h.t;
   const int type = lh.x & LEAF_TYPE_MASK;
   s.mat = lh.z;
+  const bool uv = all_uv || ldg4(S.mat_i + lh.z).w != 0;
+  s.u = 0.f;
+  s.v = 0.f;
   if (type == LT_SPHERE || type == LT_MSPHERE) {  // sphere.cc:24-28,56-60
     const f4 d0 = ldg4(d);
     float3 c0 = f3(d0), c = c0;
     if (type == LT_MSPHERE) c = msphere_center(d0, ldg4(d + 1), ldg4(d + 2), r.time);
     s.p = at(r, t);
-    uv_map(xdiv3(xsub3(s.p, c0), d0.w), s.u, s.v);
+    if (uv) uv_map(xdiv3(xsub3(s.p, c0), d0.w), s.u, s.v);
     s.n = xdiv3(xsub3(s.p, c), d0.w);
   } else if (type == LT_RECT || type == LT_BOX) {
     int ax;
@@ -591,19 +601,19 @@ __device__ void finalize(const DevScene &S, const Ray &wr, const HitRef &h, Surf
       b0 = ax == 2 ? p0.y : p0.z;
       b1 = ax == 2 ? p1.y : p1.z;
     }
-    const int ia = ax == 0 ? 1 : 0, ib = ax == 2 ? 1 : 2;
-    const float a = xa(comp(r.o, ia), xm(t, comp(r.d, ia)));
-    const float b = xa(comp(r.o, ib), xm(t, comp(r.d, ib)));
-    s.u = xd(xs(a, a0), xs(a1, a0));
-    s.v = xd(xs(b, b0), xs(b1, b0));
+    if (uv) {
+      const int ia = ax == 0 ? 1 : 0, ib = ax == 2 ? 1 : 2;
+      const float a = xa(comp(r.o, ia), xm(t, comp(r.d, ia)));
+      const float b = xa(comp(r.o, ib), xm(t, comp(r.d, ib)));
+      s.u = xd(xs(a, a0), xs(a1, a0));
+      s.v = xd(xs(b, b0), xs(b1, b0));
+    }
     s.p = at(r, t);
     s.n = v3(ax == 0 ? 1.f : 0.f, ax == 1 ? 1.f : 0.f, ax == 2 ? 1.f : 0.f);
     if (fflip) s.n = -s.n;
   } else {  // medium: hitable.cc:118-123 (random normal; uv left untouched)
     s.p = at(r, t);
     s.n = v3(1.f, 0.f, 0.f);
-    s.u = 0.f;
-    s.v = 0.f;
   }
   if (lh.x & LEAF_FLIP) s.n = -s.n;
   if (h.inst >= 0) {
@@ -765,23 +775,19 @@ __device__ float3 light_random(const DevScene &S, float3 o, float pick, float r1
 }
 
 __device__ float3 guide_sample(const float4 *lob, float u_lobe, float u1, float u2) {
-  int pick = 7;
-  float cdf = 0.f;
-  for (int i = 0; i < 8; i++) {
-    cdf += __ldg(reinterpret_cast<const float4 *>(lob) + 2 * i + 1).x;
-    if (u_lobe < cdf) {
-      pick = i;
-      break;
-    }
-  }
-  const float4 a = __ldg(reinterpret_cast<const float4 *>(lob) + 2 * pick);
-  const float e2 = __ldg(reinterpret_cast<const float4 *>(lob) + 2 * pick + 1).z;
-  float w = 1.f + __logf(u1 + (1.f - u1) * e2) / a.w;
+  const float4 c0 = __ldg(lob + 8), c1 = __ldg(lob + 9);
+  const int pick = (u_lobe >= c0.x) + (u_lobe >= c0.y) + (u_lobe >= c0.z) + (u_lobe >= c0.w) + (u_lobe >= c1.x) +
+                   (u_lobe >= c1.y) + (u_lobe >= c1.z);
+  const float4 a = __ldg(lob + pick);
+  const float k = sqrtf(a.x * a.x + a.y * a.y + a.z * a.z);
+  const float ik = 1.f / k;
+  const float e2 = __expf(-2.f * k);
+  float w = 1.f + __logf(u1 + (1.f - u1) * e2) * ik;
   w = fminf(fmaxf(w, -1.f), 1.f);
   const float sw = sqrtf(fmaxf(0.f, 1.f - w * w));
   float sn, cs;
   sincospif(2.f * u2, &sn, &cs);
-  const Onb f(v3(a.x, a.y, a.z));
+  const Onb f(v3(a.x * ik, a.y * ik, a.z * ik));
   return f.local(v3(cs * sw, sn * sw, w));
 }
 
@@ -812,8 +818,10 @@ __device__ __forceinline__ Ray camera_ray(const Camera &c, int i, int j, int nx,
 
 // ---------------------------------------------------------- path guiding --
 // The guiding network, evaluated on a res^3 grid of the scene box x 6 normal
-// bins after each training round, as a table of 8 vMF lobes per entry:
-// {mu.xyz, kappa}, {pi, kappa / (2 pi (1 - exp(-2 kappa))), exp(-2 kappa), 0}.
+// bins after each training round, as a table of GUIDE_ENTRY float4 per
+// entry: 8 lobes {kappa mu.xyz, log(pi kappa / (2 pi (1 - exp(-2 kappa)))) - kappa}
+// (so a lobe's density at w is exp(dot(kappa mu, w) + .w)), then the lobe
+// weights' running sums {c0, c1, c2, c3}, {c4, c5, c6, c7} (GUIDE_ENTRY, arena.h).
 struct GuideView {
   const float4 *lobes;  // nullptr: not guided
   float3 lo, inv_ext;
@@ -833,7 +841,7 @@ __device__ __forceinline__ const float4 *guide_entry(const GuideView &g, float3 
   const int cz = min(max((int)((p.z - g.lo.z) * g.inv_ext.z * r), 0), r - 1);
   const float ax = fabsf(n.x), ay = fabsf(n.y), az = fabsf(n.z);
   const int bin = (ax >= ay && ax >= az) ? (n.x >= 0.f ? 0 : 1) : (ay >= az ? (n.y >= 0.f ? 2 : 3) : (n.z >= 0.f ? 4 : 5));
-  return g.lobes + ((size_t)((cz * r + cy) * r + cx) * 6 + bin) * 16;
+  return g.lobes + ((size_t)((cz * r + cy) * r + cx) * 6 + bin) * GUIDE_ENTRY;
 }
 
 // Mixture density of unit direction w (solid-angle measure).
@@ -841,9 +849,8 @@ __device__ __forceinline__ float guide_pdf(const float4 *lob, float3 w) {
   float p = 0.f;
 #pragma unroll
   for (int i = 0; i < 8; i++) {
-    const float4 a = __ldg(reinterpret_cast<const float4 *>(lob) + 2 * i);
-    const float4 b = __ldg(reinterpret_cast<const float4 *>(lob) + 2 * i + 1);
-    p += b.x * b.y * __expf(a.w * (a.x * w.x + a.y * w.y + a.z * w.z - 1.f));
+    const float4 a = __ldg(lob + i);
+    p += __expf(a.x * w.x + a.y * w.y + a.z * w.z + a.w);
   }
   return p;
 }
@@ -912,7 +919,7 @@ __device__ bool shade_vertex_t(const DevScene &S, const RenderCfg &cfg, Ray &ray
     return false;
   }
   Surface sf;
-  finalize(S, ray, h, sf);
+  finalize(S, ray, h, sf, false);
   const i4 mi = ldg4(S.mat_i + sf.mat);
   if (vi) vertex_info(S, ray, sf, mi, *vi);
   float3 E = v3(0.f, 0.f, 0.f);
@@ -983,15 +990,13 @@ __device__ bool shade_vertex_t(const DevScene &S, const RenderCfg &cfg, Ray &ray
       const float cos_scale = cfg.semantics == 0 ? 1.f : 0.318309886183790671538f;
       float pdf;
       const float4 *lob = nullptr;
-      float4 q = make_float4(1.f, 0.f, 0.f, 0.f);
-      if (GUIDED && gv.lobes) {
-        lob = guide_entry(gv, sf.p, sf.n);
-        q = uniforms(make_uint4(pixel, sample, (uint32_t)depth, RNG_GUIDE), cfg.key);
-      }
-      if (GUIDED && lob && q.x < gv.alpha) {
-        dir = guide_sample(lob, q.y, q.z, q.w);
+      float u = r.x;  // technique choice; rescaled to [0,1) for the technique chosen
+      if (GUIDED && gv.lobes) lob = guide_entry(gv, sf.p, sf.n);
+      if (GUIDED && lob && u < gv.alpha) {
+        dir = guide_sample(lob, u / gv.alpha, r.z, r.w);
       } else if (S.has_lights) {
-        dir = r.x < 0.5f ? light_random(S, sf.p, r.y, r.z, r.w) : uvw.local(cos_hemisphere(r.z, r.w));
+        if (GUIDED && lob) u = (u - gv.alpha) / (1.f - gv.alpha);
+        dir = u < 0.5f ? light_random(S, sf.p, r.y, r.z, r.w) : uvw.local(cos_hemisphere(r.z, r.w));
       } else {
         dir = uvw.local(cos_hemisphere(r.z, r.w));
       }

@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
       segs++;
       if (hit && !training && depth >= term_depth) {
         Surface sf;
-        finalize(S, r, h, sf);
+        finalize(S, r, h, sf, false);
         vertex_info(S, r, sf, ldg4(S.mat_i + sf.mat), vi);
         want_q = true;
         accumulate(F, pixel, L);
@@ -1284,7 +1284,7 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
     c->guide = nullptr;
     if ((st = guide_create(c->device, g->seed, &c->guide)) != TPT_OK) return st;
   }
-  const size_t table_f4 = (size_t)g->grid_res * g->grid_res * g->grid_res * 6 * 16;
+  const size_t table_f4 = (size_t)g->grid_res * g->grid_res * g->grid_res * 6 * GUIDE_ENTRY;
   if ((st = ensure(c->guide_table, table_f4 * sizeof(float4))) != TPT_OK) return st;
   if ((st = ensure(c->guide_records, (size_t)g->record_cap * 3 * sizeof(float4))) != TPT_OK) return st;
   if ((st = ensure(c->guide_count, sizeof(unsigned))) != TPT_OK) return st;
@@ -1407,7 +1407,7 @@ extern "C" tpt_status tpt_guide_records(tpt_context *c, float *out, int64_t cap,
 extern "C" void tpt_nrc_params_default(tpt_nrc_params *n) {
   if (!n) return;
   n->passes = 8;
-  n->train_steps = 32;
+  n->train_steps = 128;
   n->batch = 16384;
   n->lr = 1e-3f;
   n->terminate_depth = 2;

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "../../include/tpt.h"
+#include "arena.h"
 #include "mlp.cuh"
 
 namespace tpt {
@@ -401,8 +402,25 @@ __global__ void k_guide_encode_grid(int res, int rows_valid, int rows, __half *_
   }
 }
 
-// Network outputs -> lobe table: per row 8 lobes x 2 float4:
-// {mu.xyz, kappa}, {pi, kappa / (2 pi (1 - exp(-2 kappa))), exp(-2 kappa), 0}.
+// Network outputs -> lobe table rows of GUIDE_ENTRY float4 (the layout the
+// renderer reads, see guide_pdf / guide_sample).
+__device__ __forceinline__ void guide_row(const float lobe[GUIDE_LOBES][5], float4 *dst) {
+  float cdf = 0.f;
+  float c[GUIDE_LOBES];
+  for (int i = 0; i < GUIDE_LOBES; i++) {
+    const float *L = lobe[i];  // {pi, kappa, mu.x, mu.y, mu.z}
+    const float k = L[1];
+    const float norm = k / (6.28318530717958647692f * -expm1f(-2.f * k));
+    const float lc = L[0] > 0.f ? logf(L[0] * norm) - k : -1e30f;
+    dst[i] = make_float4(k * L[2], k * L[3], k * L[4], lc);
+    cdf += L[0];
+    c[i] = cdf;
+  }
+  c[GUIDE_LOBES - 1] = 1.f;
+  dst[8] = make_float4(c[0] / cdf, c[1] / cdf, c[2] / cdf, c[3] / cdf);
+  dst[9] = make_float4(c[4] / cdf, c[5] / cdf, c[6] / cdf, 1.f);
+}
+
 __global__ void k_guide_post(const float *__restrict__ Y, int rows_valid, float4 *__restrict__ lobes) {
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows_valid; r += gridDim.x * blockDim.x) {
     const float *y = Y + (size_t)r * GUIDE_OUT;
@@ -413,59 +431,84 @@ __global__ void k_guide_post(const float *__restrict__ Y, int rows_valid, float4
       e[i] = __expf(y[5 * i] - lmax);
       z += e[i];
     }
-    float4 out[2 * GUIDE_LOBES];
+    float L[GUIDE_LOBES][5];
     bool ok = z > 0.f && isfinite(z);
     for (int i = 0; i < GUIDE_LOBES; i++) {
       const float kp = y[5 * i + 1];
       const float k = fminf((kp > 20.f ? kp : log1pf(__expf(kp))) + 1e-2f, LossVmf::KAPPA_MAX);
-      float mx = y[5 * i + 2], my = y[5 * i + 3], mz = y[5 * i + 4];
-      const float mnorm = fmaxf(sqrtf(mx * mx + my * my + mz * mz), 1e-12f);
-      const float e2 = __expf(-2.f * k);
-      out[2 * i] = make_float4(mx / mnorm, my / mnorm, mz / mnorm, k);
-      out[2 * i + 1] = make_float4(e[i] / z, k / (6.28318530717958647692f * (1.f - e2)), e2, 0.f);
-      ok = ok && isfinite(out[2 * i].x) && isfinite(out[2 * i].y) && isfinite(out[2 * i].z) && isfinite(k) &&
-           isfinite(out[2 * i + 1].x) && isfinite(out[2 * i + 1].y);
+      const float mx = y[5 * i + 2], my = y[5 * i + 3], mz = y[5 * i + 4];
+      const float mnorm = sqrtf(mx * mx + my * my + mz * mz);
+      L[i][0] = e[i] / z;
+      L[i][1] = k;
+      L[i][2] = mx / mnorm;
+      L[i][3] = my / mnorm;
+      L[i][4] = mz / mnorm;
+      ok = ok && mnorm > 1e-12f && isfinite(L[i][0]) && isfinite(k) && isfinite(L[i][2]) && isfinite(L[i][3]) &&
+           isfinite(L[i][4]);
     }
-    if (!ok) {  // a broad lobe: sampling and density stay consistent
+    if (!ok) {  // one broad lobe: sampling and density stay consistent
       for (int i = 0; i < GUIDE_LOBES; i++) {
-        const float k = 0.01f, e2 = __expf(-2.f * k);
-        out[2 * i] = make_float4(0.f, 0.f, 1.f, k);
-        out[2 * i + 1] = make_float4(i == 0 ? 1.f : 0.f, k / (6.28318530717958647692f * (1.f - e2)), e2, 0.f);
+        L[i][0] = i == 0 ? 1.f : 0.f;
+        L[i][1] = 0.01f;
+        L[i][2] = L[i][3] = 0.f;
+        L[i][4] = 1.f;
       }
     }
-    for (int i = 0; i < 2 * GUIDE_LOBES; i++) lobes[(size_t)r * 2 * GUIDE_LOBES + i] = out[i];
+    float4 out[GUIDE_ENTRY];
+    guide_row(L, out);
+    for (int i = 0; i < GUIDE_ENTRY; i++) lobes[(size_t)r * GUIDE_ENTRY + i] = out[i];
   }
 }
 
 // ------------------------------------------------- neural radiance cache --
-// Input: one-blob position (3 x 16 bins) + outgoing direction + normal +
-// albedo + roughness = 58 values padded to 64; output RGB (3 of 16).
-// Records / queries are 4 float4: (x, roughness), (w_out, 0), (n, 0),
-// (albedo, 0); training targets float4 (rgb, 0).
-constexpr int NRC_IN = 64, NRC_NH = 5, NRC_OUT = 16, NRC_BINS = 16;
+// Records / queries are 5 float4: (x, roughness), (w_out, 0), (n, 0),
+// (albedo, 0), then the training target (rgb, 1) or the query's
+// (throughput, pixel bits).
+constexpr int NRC_IN = 64, NRC_NH = 5, NRC_OUT = 16;
 
 __device__ __forceinline__ __half fin16(float v) {  // non-finite features encode as 0
   return __float2half_rn(isfinite(v) ? fminf(fmaxf(v, -65504.f), 65504.f) : 0.f);
 }
 
+// One-blob encoding (Mueller et al., "Neural Importance Sampling", ACM TOG
+// 2019) of u in [0,1] over `bins` bins with a triangular kernel one bin wide.
+__device__ __forceinline__ void one_blob(float u, int bins, __half *out) {
+  const float x = fminf(fmaxf(u, 0.f), 1.f) * bins;  // NaN -> 0
+  for (int b = 0; b < bins; b++) out[b] = __float2half_rn(fmaxf(0.f, 1.f - fabsf(x - (b + 0.5f))));
+}
+
+// Unit direction -> spherical (theta, phi) in [0,1]^2, one-blob 4 + 4.
+__device__ __forceinline__ void dir_blob(float3 d, __half *out) {
+  const float th = acosf(fminf(fmaxf(d.z, -1.f), 1.f)) * 0.318309886183790671538f;
+  float ph = atan2f(d.y, d.x) * 0.159154943091895335769f;
+  ph = ph < 0.f ? ph + 1.f : ph;
+  one_blob(th, 4, out);
+  one_blob(ph, 4, out + 4);
+}
+
+// Cache input (Mueller et al., "Real-time Neural Radiance Caching for Path
+// Tracing", ACM TOG 2021): position by a triangle-wave frequency encoding,
+// 12 octaves per axis (36); outgoing direction and normal as spherical
+// one-blobs (8 + 8); roughness one-blob (4); albedo (3); padded to 64.
 __device__ __forceinline__ void nrc_encode(const float4 *f, float3 lo, float3 inv_ext, __half *out) {
   const float c[3] = {(f[0].x - lo.x) * inv_ext.x, (f[0].y - lo.y) * inv_ext.y, (f[0].z - lo.z) * inv_ext.z};
 #pragma unroll
   for (int a = 0; a < 3; a++) {
-    const float u = fminf(fmaxf(c[a], 0.f), 1.f) * NRC_BINS;  // NaN -> 0
-    for (int b = 0; b < NRC_BINS; b++) out[a * NRC_BINS + b] = __float2half_rn(fmaxf(0.f, 1.f - fabsf(u - (b + 0.5f))));
+    const float x = isfinite(c[a]) ? fminf(fmaxf(c[a], 0.f), 1.f) : 0.f;
+    float s = x;
+    for (int k = 0; k < 12; k++, s *= 2.f) {
+      const float fr = s - floorf(s);
+      out[a * 12 + k] = __float2half_rn(fabsf(2.f * fr - 1.f));
+    }
   }
-  out[48] = fin16(f[1].x);
-  out[49] = fin16(f[1].y);
-  out[50] = fin16(f[1].z);
-  out[51] = fin16(f[2].x);
-  out[52] = fin16(f[2].y);
-  out[53] = fin16(f[2].z);
-  out[54] = fin16(f[3].x);
-  out[55] = fin16(f[3].y);
-  out[56] = fin16(f[3].z);
-  out[57] = fin16(f[0].w);
-  for (int i = 58; i < NRC_IN; i++) out[i] = __float2half_rn(0.f);
+  const float3 wo = make_float3(f[1].x, f[1].y, f[1].z), n = make_float3(f[2].x, f[2].y, f[2].z);
+  dir_blob(wo, out + 36);
+  dir_blob(n, out + 44);
+  one_blob(f[0].w, 4, out + 52);
+  out[56] = fin16(f[3].x);
+  out[57] = fin16(f[3].y);
+  out[58] = fin16(f[3].z);
+  for (int i = 59; i < NRC_IN; i++) out[i] = __float2half_rn(0.f);
 }
 
 // Relative L2 (Mueller et al., "Real-time Neural Radiance Caching for Path

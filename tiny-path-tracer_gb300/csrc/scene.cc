@@ -635,6 +635,16 @@ struct Compiler {
 
   // Flattens the BVH rooted at builder node h into pre-order nodes; leaves
   // are created in left-to-right order.  in_blas: leaves must be primitives.
+  // Whether texture t (a checker: either of its children) reads (u, v):
+  // only image textures do (texture.cc:27-42).
+  bool tex_reads_uv(int t, int guard = 0) const {
+    if (t < 0 || t >= (int)B.texs.size() || guard > 16) return false;
+    const HTex &x = B.texs[t];
+    if (x.kind == TT_IMAGE) return true;
+    if (x.kind == TT_CHECKER) return tex_reads_uv(x.odd, guard + 1) || tex_reads_uv(x.even, guard + 1);
+    return false;
+  }
+
   int flatten_bvh(int h, bool in_blas, int depth, int &max_depth) {
     if (depth > max_depth) max_depth = depth;
     const HNode &n = B.nodes[h];
@@ -700,7 +710,7 @@ struct Compiler {
         i4 hdr{LT_MEDIUM, (int32_t)S.leaf_data.size(), -1, bnd};
         push_data(f4{n.density, 0, 0, 0});
         // the phase function: isotropic(texture) (hitable.cc:92-96)
-        i4 mi{MT_ISOTROPIC, n.phase_tex, 0, 0};
+        i4 mi{MT_ISOTROPIC, n.phase_tex, 0, tex_reads_uv(n.phase_tex) ? 1 : 0};
         S.mat_i.push_back(mi);
         S.mat_f.push_back(f4{0, 0, 0, 0});
         hdr.z = (int)S.mat_i.size() - 1;
@@ -874,7 +884,7 @@ struct Compiler {
     }
     // materials
     for (const HMat &m : B.mats) {
-      i4 mi{m.kind, m.tex, 0, 0};
+      i4 mi{m.kind, m.tex, 0, tex_reads_uv(m.tex) ? 1 : 0};
       f4 mf{m.albedo[0], m.albedo[1], m.albedo[2], m.fuzz};
       if (m.kind == MT_DIELECTRIC) mf = f4{m.ior, 0, 0, 0};
       S.mat_i.push_back(mi);

@@ -301,19 +301,21 @@ class Context:
 
 
 def render_guided(ctx: "Context", slot: int, width: int, height: int, spp: int, max_depth: int = 50,
-                  background: int = BACKGROUND_BLACK, seed: int = 1, **guide):
+                  background: int = BACKGROUND_BLACK, seed: int = 1, out=None, **guide):
     """Learned path guiding (physical semantics).  guide: fields of
     tpt_guide_params (passes, train_steps, batch, lr, grid_res, alpha,
-    record_cap, seed).  Returns (image, render stats, guide stats)."""
+    record_cap, seed).  out: None (host image returned) or a device pointer.
+    Returns (image or None, render stats, guide stats)."""
     p = make_params(width, height, spp, max_depth, SEMANTICS_PHYSICAL, background, 1.0, seed)
     g = GuideParams()
     lib().tpt_guide_params_default(C.byref(g))
     for k, v in guide.items():
         setattr(g, k, v)
-    img = np.zeros((height, width, 3), np.float32)
+    img = np.zeros((height, width, 3), np.float32) if out is None else None
+    dst, mem = (_ptr(img), TPT_MEM_HOST) if out is None else (C.c_void_p(int(out)), TPT_MEM_DEVICE)
     st, gs = RenderStats(), GuideStats()
-    check(lib().tpt_render_guided(ctx._h, slot, C.byref(p), C.byref(g), _ptr(img), TPT_MEM_HOST, C.byref(st),
-                                  C.byref(gs)), "render_guided")
+    check(lib().tpt_render_guided(ctx._h, slot, C.byref(p), C.byref(g), dst, mem, C.byref(st), C.byref(gs)),
+          "render_guided")
     return img, st.as_dict(), gs.as_dict()
 
 
@@ -330,18 +332,21 @@ def guide_records(ctx: "Context", cap: int = 1 << 22) -> np.ndarray:
 
 
 def render_nrc(ctx: "Context", slot: int, width: int, height: int, spp: int, max_depth: int = 50,
-               semantics: int = SEMANTICS_PHYSICAL, background: int = BACKGROUND_BLACK, seed: int = 1, **nrc):
-    """Neural radiance cache render.  nrc: fields of tpt_nrc_params.
-    Returns (image, render stats, cache stats)."""
+               semantics: int = SEMANTICS_PHYSICAL, background: int = BACKGROUND_BLACK, seed: int = 1, out=None,
+               **nrc):
+    """Neural radiance cache render.  nrc: fields of tpt_nrc_params.  out:
+    None (host image returned) or a device pointer.
+    Returns (image or None, render stats, cache stats)."""
     p = make_params(width, height, spp, max_depth, semantics, background, 1.0, seed)
     n = NrcParams()
     lib().tpt_nrc_params_default(C.byref(n))
     for k, v in nrc.items():
         setattr(n, k, v)
-    img = np.zeros((height, width, 3), np.float32)
+    img = np.zeros((height, width, 3), np.float32) if out is None else None
+    dst, mem = (_ptr(img), TPT_MEM_HOST) if out is None else (C.c_void_p(int(out)), TPT_MEM_DEVICE)
     st, ns = RenderStats(), NrcStats()
-    check(lib().tpt_render_nrc(ctx._h, slot, C.byref(p), C.byref(n), _ptr(img), TPT_MEM_HOST, C.byref(st),
-                               C.byref(ns)), "render_nrc")
+    check(lib().tpt_render_nrc(ctx._h, slot, C.byref(p), C.byref(n), dst, mem, C.byref(st), C.byref(ns)),
+          "render_nrc")
     return img, st.as_dict(), ns.as_dict()
 
 
