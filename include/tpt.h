@@ -336,22 +336,24 @@ tpt_status tpt_render_guided(tpt_context *ctx, int32_t slot, const tpt_render_pa
 tpt_status tpt_guide_records(tpt_context *ctx, float *out, int64_t cap, int64_t *count);
 
 /* Neural radiance cache (no counterpart in the reference).  Rendered in
- * `passes` passes; in every pass after the first, a path that reaches its
- * vertex number terminate_depth (0 = camera hit) stops there and adds
+ * `passes` passes; in every pass after the first, a path stops at its first
+ * diffuse vertex (lambertian, or isotropic in physical semantics) whose
+ * vertex number is at least terminate_depth (0 = camera hit) and adds
  * throughput x cache(position, outgoing direction, normal, albedo,
  * roughness), the cache being an MLP of shape (64, 5, 16) evaluated on the
- * tensor cores for all such vertices at once.  Every train_stride-th path is
- * a training path: it is traced to full depth (contributing its unbiased
- * estimate) and records its first vertices with their measured outgoing
- * radiance; after each pass the cache takes train_steps Adam steps on them
- * (relative L2 loss).  The first pass traces every path to full depth.
+ * tensor cores for all such vertices at once; specular vertices and lights
+ * are traced through.  Every train_stride-th path is a training path: it is
+ * traced to full depth (contributing its unbiased estimate) and records its
+ * first three diffuse vertices with their measured outgoing radiance; after
+ * each pass the cache takes train_steps Adam steps on them (relative L2
+ * loss).  The first pass traces every path to full depth.
  * The estimator is biased by the cache's error; the plain tracer is its
  * fallback and its judge. */
 typedef struct {
   int32_t passes;           /* >= 1 (8) */
   int32_t train_steps;      /* Adam steps after each pass (128) */
   int32_t batch;            /* training rows per step (16384) */
-  float lr;                 /* Adam learning rate (1e-3) */
+  float lr;                 /* Adam learning rate (3e-3) */
   int32_t terminate_depth;  /* 2: two bounces, then the cache */
   int32_t train_stride;     /* every n-th path trains the cache (16) */
   int32_t record_cap;       /* training records per pass */
@@ -366,6 +368,54 @@ typedef struct {
 void tpt_nrc_params_default(tpt_nrc_params *n);
 tpt_status tpt_render_nrc(tpt_context *ctx, int32_t slot, const tpt_render_params *p, const tpt_nrc_params *n,
                           float *out_rgb, int32_t mem, tpt_render_stats *stats, tpt_nrc_stats *nstats);
+
+/* ------------------------------------------------------------------------
+ * The formats on either side of the render loop of main.cpp.
+ * ---------------------------------------------------------------------- */
+/* config.ini (main.cpp:29-56): section/key per field. */
+typedef struct {
+  int32_t width;            /* [DEFAULT] width (400) */
+  int32_t height;           /* [DEFAULT] height (200) */
+  int32_t sample;           /* [DEFAULT] sample: samples per pixel (10) */
+  int32_t recur_depth;      /* [DEFAULT] recur_depth: max depth (50) */
+  float fov;                /* [DEFAULT] fov, degrees (90) */
+  int32_t allow_bonus_pic;  /* [DEFAULT] allow_bonus_pic (0) */
+  int32_t bonus_pic;        /* [DEFAULT] bonus_pic: snapshots (10) */
+  float aperture;           /* [BLUR] aperture (0.2) */
+  float start_time;         /* [CAM_MOTION] start_time (0) */
+  float end_time;           /* [CAM_MOTION] end_time (1) */
+} tpt_config;
+/* The defaults of main.cpp:31-40. */
+void tpt_config_default(tpt_config *c);
+/* Parses INI text with the grammar of the reference's inipp: trimmed lines,
+ * ';' comments, [sections], key = value (the first definition of a key in a
+ * section wins); a field changes only when its key is present and its whole
+ * value converts (else it keeps its current value). */
+tpt_status tpt_config_parse(const char *text, tpt_config *c);
+/* tpt_config_parse of a file; an unreadable file leaves *c unchanged and
+ * returns TPT_OK, as main.cpp:29 never checks its stream. */
+tpt_status tpt_config_load(const char *path, tpt_config *c);
+/* The camera inputs of a compiled scene, tpt_builder_set_camera's arguments
+ * in order: lookfrom[3], lookat[3], vup[3], vfov, aspect, aperture, focus,
+ * time0, time1. */
+tpt_status tpt_scene_get_camera(const tpt_scene *s, float out[15]);
+/* Replaces a compiled scene's camera (main.cpp:86-90 builds it from the
+ * config's fov, aperture and shutter); takes effect at the next upload. */
+tpt_status tpt_scene_set_camera(tpt_scene *s, const float lookfrom[3], const float lookat[3], const float vup[3],
+                                float vfov, float aspect, float aperture, float focus, float time0, float time1);
+/* allow_bonus_pic (main.cpp:111-131,192-216): renders spp samples per pixel
+ * and also the running means after every slice = spp / bonus_pic samples:
+ * snapshots_rgb holds bonus_pic images (width*height*3 floats each), image k
+ * the mean of each pixel's first (k+1)*slice samples, identical to what
+ * tpt_render gives at spp = (k+1)*slice.  out_rgb receives the mean of all
+ * spp samples.  bonus_pic > spp is TPT_ERR_INVALID_ARGUMENT (the reference
+ * divides by zero).  Persistent engine; physical or reference semantics. */
+tpt_status tpt_render_snapshots(tpt_context *ctx, int32_t slot, const tpt_render_params *p, int32_t bonus_pic,
+                                float *out_rgb, float *snapshots_rgb, int32_t mem, tpt_render_stats *stats);
+/* `count` quantised images side by side in one PPM P3 file: the strip
+ * main.cpp:222-243 asks ImageMagick's `convert +append` for. */
+tpt_status tpt_write_ppm_strip(const char *path, const uint8_t *const *images, int32_t count, int32_t width,
+                               int32_t height);
 
 /* Host helpers: reference output quantisation (main.cpp:135-142,176-182) and
  * the PPM P3 writer of main.cpp:69,183-189. */

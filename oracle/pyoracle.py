@@ -95,6 +95,8 @@ def ref_lib():
         L.ref_render.restype = C.c_double
         L.ref_render.argtypes = [C.c_void_p, C.POINTER(RefRenderParams), C.c_void_p]
         L.ref_hardware_concurrency.restype = C.c_int32
+        L.ref_config_parse.restype = None
+        L.ref_config_parse.argtypes = [C.c_char_p, C.c_void_p]
         _ref = L
     return _ref
 
@@ -186,6 +188,13 @@ def procedural_image(w: int, h: int, seed: int) -> np.ndarray:
     out = np.zeros((h, w, 3), np.uint8)
     lib().oracle_procedural_image(w, h, seed, _ptr(out))
     return out
+
+
+def ref_config_parse(text: str) -> list:
+    """config.ini values as the reference's main.cpp reads them (inipp)."""
+    out = (C.c_double * 10)()
+    ref_lib().ref_config_parse(text.encode(), out)
+    return list(out)
 
 
 class RefScene:

@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "camera.h"
+#include "inipp.h"
 #include "hitable.h"
 #include "hitable_list.h"
 #include "material.h"
@@ -432,5 +433,30 @@ double ref_render(void *sp, const ref_render_params *p, float *mean_rgb) {
 }
 
 int32_t ref_hardware_concurrency(void) { return (int32_t)std::thread::hardware_concurrency(); }
+
+// config.ini through the reference's own parser and the extraction calls of
+// main.cpp:42-56, from main.cpp:31-40's defaults.  out: width, height,
+// sample, recur_depth, fov, allow_bonus_pic, bonus_pic, aperture,
+// start_time, end_time.
+void ref_config_parse(const char *text, double out[10]) {
+  int nx = 400, ny = 200, ns = 10, depth = 50, allow = 0, bonus = 10;
+  float aperture = 0.2f, time0 = 0.0f, time1 = 1.0f, fov = 90.0f;
+  std::istringstream is{std::string(text)};
+  inipp::Ini<char> ini;
+  ini.parse(is);
+  inipp::extract(ini.sections["DEFAULT"]["width"], nx);
+  inipp::extract(ini.sections["DEFAULT"]["height"], ny);
+  inipp::extract(ini.sections["DEFAULT"]["sample"], ns);
+  inipp::extract(ini.sections["DEFAULT"]["recur_depth"], depth);
+  inipp::extract(ini.sections["DEFAULT"]["fov"], fov);
+  inipp::extract(ini.sections["DEFAULT"]["bonus_pic"], bonus);
+  inipp::extract(ini.sections["DEFAULT"]["allow_bonus_pic"], allow);
+  inipp::extract(ini.sections["BLUR"]["aperture"], aperture);
+  inipp::extract(ini.sections["CAM_MOTION"]["start_time"], time0);
+  inipp::extract(ini.sections["CAM_MOTION"]["end_time"], time1);
+  const double v[10] = {(double)nx, (double)ny, (double)ns, (double)depth, fov, (double)allow, (double)bonus,
+                        aperture, time0, time1};
+  for (int i = 0; i < 10; i++) out[i] = v[i];
+}
 
 }  // extern "C"

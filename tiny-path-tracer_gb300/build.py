@@ -7,7 +7,8 @@ The translation units compile in parallel: kernels.cu (path tracing) and
 learn.cu (tensor-core MLPs of the learned parts) with nvcc
 (-gencode arch=compute_103a,code=sm_103a; hit arithmetic is written with
 unfused round-to-nearest intrinsics, so FMA contraction stays on for the
-rest), scene.cc with g++ (-ffp-contract=off).
+rest), scene.cc (scene compiler) and config.cc (config.ini, PPM strips) with
+g++ (-ffp-contract=off).
 """
 from __future__ import annotations
 
@@ -57,10 +58,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs.append(obj)
         cmds.append([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
                      "-Xcompiler", "-fPIC", "-c", os.path.join(CSRC, cu), "-o", obj])
-    s_obj = os.path.join(OUT, "scene.o")
-    objs.append(s_obj)
-    cmds.append(["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fPIC", "-Wall", f"-I{cuda}/include", "-c",
-                 os.path.join(CSRC, "scene.cc"), "-o", s_obj])
+    for cc in ("scene.cc", "config.cc"):
+        obj = os.path.join(OUT, cc.replace(".cc", ".o"))
+        objs.append(obj)
+        cmds.append(["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fPIC", "-Wall", f"-I{cuda}/include", "-c",
+                     os.path.join(CSRC, cc), "-o", obj])
     procs = [subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT) for cmd in cmds]
     for cmd, p in zip(cmds, procs):
         out, _ = p.communicate()

@@ -889,6 +889,7 @@ __device__ __forceinline__ bool nonzero(float3 e) { return e.x != 0.f || e.y != 
 struct VertexInfo {
   float3 p, wo, n, albedo;
   float rough;
+  int kind;  // material type (MatType)
 };
 
 __device__ __forceinline__ void vertex_info(const DevScene &S, const Ray &ray, const Surface &sf, const i4 &mi,
@@ -896,6 +897,7 @@ __device__ __forceinline__ void vertex_info(const DevScene &S, const Ray &ray, c
   vi.p = sf.p;
   vi.wo = -unit3(ray.d);
   vi.n = sf.n;
+  vi.kind = mi.x;
   vi.rough = 1.f;
   vi.albedo = v3(0.f, 0.f, 0.f);
   if (mi.x == MT_LAMBERTIAN || mi.x == MT_ISOTROPIC) {
@@ -913,7 +915,8 @@ __device__ __forceinline__ void vertex_info(const DevScene &S, const Ray &ray, c
 template <bool GUIDED>
 __device__ bool shade_vertex_t(const DevScene &S, const RenderCfg &cfg, Ray &ray, bool hit, const HitRef &h,
                                float3 &T, float3 &L, int depth, uint32_t pixel, uint32_t sample, const GuideView &gv,
-                               GuideRec &rec, VertexInfo *vi = nullptr) {
+                               GuideRec &rec, VertexInfo *vi = nullptr, int query_depth = 1 << 30,
+                               bool *queried = nullptr) {
   if (!hit) {
     L = L + T * background(cfg, ray);
     return false;
@@ -926,6 +929,12 @@ __device__ bool shade_vertex_t(const DevScene &S, const RenderCfg &cfg, Ray &ray
   if (mi.x == MT_LIGHT && dot3(sf.n, ray.d) < 0.f) E = tex_value(S, mi.y, sf.u, sf.v, sf.p);  // material.cc:79-86
   if (depth >= cfg.max_depth) {
     L = L + T * E;
+    return false;
+  }
+  // radiance-cache query: the path ends here at a diffuse vertex (no
+  // emission there) and the cache supplies its outgoing radiance
+  if (queried && depth >= query_depth && (mi.x == MT_LAMBERTIAN || (mi.x == MT_ISOTROPIC && cfg.semantics == 1))) {
+    *queried = true;
     return false;
   }
   const float4 r = uniforms(make_uint4(pixel, sample, (uint32_t)depth, RNG_SCATTER), cfg.key);

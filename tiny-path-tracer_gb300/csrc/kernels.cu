@@ -493,19 +493,20 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
       HitRef h;
       const bool hit = trace_closest(S, r, 0.001f, stk, blockDim.x, m, h, e);
       segs++;
-      if (hit && !training && depth >= term_depth) {
-        Surface sf;
-        finalize(S, r, h, sf, false);
-        vertex_info(S, r, sf, ldg4(S.mat_i + sf.mat), vi);
+      const float3 Tb = T, Lb = L;
+      const bool may_query = !training && depth >= term_depth;
+      const bool rec_here = training && hit && nrec < 3;
+      bool queried = false;
+      const bool cont = shade_vertex_t<false>(S, cfg, r, hit, h, T, L, depth, pixel, sample, gv, grec,
+                                              (rec_here || may_query) ? &vi : nullptr,
+                                              may_query ? term_depth : (1 << 30), &queried);
+      if (queried) {  // ends at a diffuse vertex: the cache adds T x radiance
         want_q = true;
         accumulate(F, pixel, L);
         alive = false;
       } else {
-        const float3 Tb = T, Lb = L;
-        const bool rec_here = training && hit && nrec < 3;
-        const bool cont = shade_vertex_t<false>(S, cfg, r, hit, h, T, L, depth, pixel, sample, gv, grec,
-                                                rec_here ? &vi : nullptr);
-        if (rec_here) {
+        // records only where queries happen: diffuse vertices
+        if (rec_here && (vi.kind == MT_LAMBERTIAN || vi.kind == MT_ISOTROPIC)) {
           want_r = true;
           rT[nrec] = Tb;
           rL[nrec] = Lb;
@@ -984,9 +985,13 @@ static PersistentKernel persistent_variant(int v) {
   }
 }
 
+// Samples [begin, F.total) of the frame (sample-major order: sample index
+// s covers pixel s % npix, sample s / npix).
 static tpt_status run_persistent(tpt_context *c, const DevScene &S, const RenderCfg &cfg, const FrameDesc &F, int block,
-                                 int variant, bool profile, tpt_render_stats *stats) {
+                                 int variant, bool profile, tpt_render_stats *stats,
+                                 unsigned long long begin = 0) {
   WfCounters init{};
+  init.issued = begin;
   std::memcpy(c->counters_host, &init, sizeof(init));
   TPT_CUDA(cudaMemcpyAsync(c->counters, c->counters_host, sizeof(WfCounters), cudaMemcpyHostToDevice, c->stream));
   const int smem = stack_smem(block);
@@ -1099,6 +1104,71 @@ static BatchKernel batch_variant(int v) {
     case 8: return k_persistent_batch<8>;
     default: return k_persistent_batch<4>;
   }
+}
+
+extern "C" tpt_status tpt_render_snapshots(tpt_context *c, int32_t slot, const tpt_render_params *p,
+                                           int32_t bonus_pic, float *out_rgb, float *snapshots_rgb, int32_t mem,
+                                           tpt_render_stats *stats) {
+  if (!c || !p || !out_rgb || (bonus_pic > 0 && !snapshots_rgb)) return TPT_ERR_INVALID_ARGUMENT;
+  if (slot < 0 || slot >= (int32_t)c->slots.size() || !c->slots[slot].live) return TPT_ERR_BAD_HANDLE;
+  if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->max_depth < 0 || bonus_pic < 0 || bonus_pic > p->spp)
+    return TPT_ERR_INVALID_ARGUMENT;
+  const unsigned long long npix = (unsigned long long)p->width * p->height;
+  if (npix > 0x7fffffffull) return TPT_ERR_INVALID_ARGUMENT;
+  TPT_CUDA(cudaSetDevice(c->device));
+  tpt_status st;
+  if ((st = ensure(c->accum, npix * sizeof(float4))) != TPT_OK) return st;
+  if (p->accumulate_fp64 && (st = ensure(c->accum64, npix * 3 * sizeof(double))) != TPT_OK) return st;
+  if (mem == TPT_MEM_HOST && (st = ensure(c->staging, npix * 3 * sizeof(float))) != TPT_OK) return st;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  const Slot &sl = c->slots[slot];
+  int block = p->block > 0 ? p->block : 128, variant = p->wave;
+  if (p->engine == TPT_ENGINE_AUTO && sl.tuned && sl.tp.engine == TPT_ENGINE_PERSISTENT) {
+    block = sl.tp.block;
+    variant = sl.tp.wave;
+  }
+  DevScene S = sl.ds;
+  S.flat_max = p->flat_nodes > 0 ? p->flat_nodes : (sl.tuned ? sl.tp.flat_nodes : c->flat_nodes);
+  const RenderCfg cfg{p->max_depth, p->semantics, p->background, p->sky_scale,
+                      make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32))};
+  TPT_CUDA(cudaMemsetAsync(c->accum.p, 0, npix * sizeof(float4), c->stream));
+  if (p->accumulate_fp64) TPT_CUDA(cudaMemsetAsync(c->accum64.p, 0, npix * 3 * sizeof(double), c->stream));
+  const int slice = bonus_pic > 0 ? p->spp / bonus_pic : p->spp;
+  const int rgrid = (int)std::min<unsigned long long>((npix + 255) / 256, (unsigned long long)c->sm_count * 16);
+  // resolves the running mean over the first `spp` samples into host or device image `out`
+  auto emit = [&](int spp, float *out) -> tpt_status {
+    FrameDesc R{p->width, p->height, spp, npix * (unsigned long long)spp, (float4 *)c->accum.p,
+                p->accumulate_fp64 ? (double *)c->accum64.p : nullptr};
+    float *dst = mem == TPT_MEM_HOST ? (float *)c->staging.p : out;
+    k_resolve<<<rgrid, 256, 0, c->stream>>>(R, dst);
+    TPT_CUDA(cudaGetLastError());
+    if (mem == TPT_MEM_HOST) {
+      TPT_CUDA(cudaMemcpyAsync(out, dst, npix * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+      TPT_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    return TPT_OK;
+  };
+  int done = 0;
+  for (int k = 0; k <= bonus_pic; k++) {
+    const int upto = k < bonus_pic ? (k + 1) * slice : p->spp;
+    if (upto > done) {
+      FrameDesc F{p->width, p->height, upto, npix * (unsigned long long)upto, (float4 *)c->accum.p,
+                  p->accumulate_fp64 ? (double *)c->accum64.p : nullptr};
+      tpt_render_stats part{};
+      if ((st = run_persistent(c, S, cfg, F, block, variant, false, &part, npix * (unsigned long long)done)) != TPT_OK)
+        return st;
+      if (stats) {
+        stats->segments += part.segments;
+        stats->kernel_launches += part.kernel_launches;
+        stats->iterations += part.iterations;
+      }
+      done = upto;
+    }
+    if ((st = emit(upto, k < bonus_pic ? snapshots_rgb + (size_t)k * npix * 3 : out_rgb)) != TPT_OK) return st;
+  }
+  TPT_CUDA(cudaStreamSynchronize(c->stream));
+  if (stats) stats->samples = (int64_t)npix * p->spp;
+  return TPT_OK;
 }
 
 extern "C" tpt_status tpt_render_batch(tpt_context *c, const tpt_batch_item *items, int32_t n,
@@ -1409,7 +1479,7 @@ extern "C" void tpt_nrc_params_default(tpt_nrc_params *n) {
   n->passes = 8;
   n->train_steps = 128;
   n->batch = 16384;
-  n->lr = 1e-3f;
+  n->lr = 3e-3f;
   n->terminate_depth = 2;
   n->train_stride = 16;
   n->record_cap = 1 << 20;

@@ -105,6 +105,7 @@ struct tpt_builder {
   int world = -1, lights = -1;
   bool has_cam = false;
   Camera cam{};
+  float cam_in[15] = {};  // tpt_builder_set_camera's arguments
   std::string err;
 
   double drand(double a = 0.0, double b = 1.0) {
@@ -538,11 +539,12 @@ tpt_status tpt_builder_set_light_shape(tpt_builder *b, int32_t ls) {
   b->lights = ls;
   return TPT_OK;
 }
-// camera_with_blur constructor (camera.cc:2-21).
-tpt_status tpt_builder_set_camera(tpt_builder *b, const float lf[3], const float la[3], const float up[3], float vfov,
-                                  float aspect, float aperture, float focus, float t0, float t1) {
-  if (!b || !lf || !la || !up) return TPT_ERR_INVALID_ARGUMENT;
-  Camera &c = b->cam;
+}  // extern "C"
+
+// camera_with_blur::camera_with_blur (camera.cc:2-21), precomputed on the host.
+static Camera make_camera(const float lf[3], const float la[3], const float up[3], float vfov, float aspect,
+                          float aperture, float focus, float t0, float t1) {
+  Camera c{};
   c.t0 = t0;
   c.t1 = t1;
   c.lens_radius = aperture / 2;
@@ -564,6 +566,31 @@ tpt_status tpt_builder_set_camera(tpt_builder *b, const float lf[3], const float
     c.u[i] = u.e[i];
     c.v[i] = v.e[i];
   }
+  return c;
+}
+
+static void camera_inputs(const float lf[3], const float la[3], const float up[3], float vfov, float aspect,
+                          float aperture, float focus, float t0, float t1, float out[15]) {
+  for (int i = 0; i < 3; i++) {
+    out[i] = lf[i];
+    out[3 + i] = la[i];
+    out[6 + i] = up[i];
+  }
+  out[9] = vfov;
+  out[10] = aspect;
+  out[11] = aperture;
+  out[12] = focus;
+  out[13] = t0;
+  out[14] = t1;
+}
+
+extern "C" {
+
+tpt_status tpt_builder_set_camera(tpt_builder *b, const float lf[3], const float la[3], const float up[3], float vfov,
+                                  float aspect, float aperture, float focus, float t0, float t1) {
+  if (!b || !lf || !la || !up) return TPT_ERR_INVALID_ARGUMENT;
+  b->cam = make_camera(lf, la, up, vfov, aspect, aperture, focus, t0, t1);
+  camera_inputs(lf, la, up, vfov, aspect, aperture, focus, t0, t1, b->cam_in);
   b->has_cam = true;
   return TPT_OK;
 }
@@ -963,6 +990,7 @@ struct Compiler {
         }
     }
     S.cam = B.cam;
+    std::memcpy(S.cam_in, B.cam_in, sizeof(S.cam_in));
     // keep the BVH trees for topology dumps
     return st;
   }
@@ -1219,6 +1247,20 @@ void tpt_quantize(const float *mean_rgb, int64_t n_pixels, uint8_t *rgb8) {
     if (q > 255) q = 255;
     rgb8[i] = (uint8_t)q;
   }
+}
+
+tpt_status tpt_scene_get_camera(const tpt_scene *s, float out[15]) {
+  if (!s || !out) return TPT_ERR_INVALID_ARGUMENT;
+  std::memcpy(out, s->S.cam_in, sizeof(s->S.cam_in));
+  return TPT_OK;
+}
+
+tpt_status tpt_scene_set_camera(tpt_scene *s, const float lf[3], const float la[3], const float up[3], float vfov,
+                                float aspect, float aperture, float focus, float t0, float t1) {
+  if (!s || !lf || !la || !up) return TPT_ERR_INVALID_ARGUMENT;
+  s->S.cam = make_camera(lf, la, up, vfov, aspect, aperture, focus, t0, t1);
+  camera_inputs(lf, la, up, vfov, aspect, aperture, focus, t0, t1, s->S.cam_in);
+  return TPT_OK;
 }
 
 tpt_status tpt_write_ppm(const char *path, const uint8_t *rgb8, int32_t w, int32_t h) {

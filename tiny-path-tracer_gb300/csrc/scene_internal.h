@@ -32,6 +32,7 @@ struct HostScene {
   int32_t n_blas = 0, blas_depth = 0, max_stack = 0;
   float world_lo[3] = {0, 0, 0}, world_hi[3] = {0, 0, 0};  // world bounding box (0 if none)
   Camera cam{};
+  float cam_in[15] = {};  // the camera's inputs: lookfrom, lookat, vup, vfov, aspect, aperture, focus, t0, t1
 };
 
 // Sections of the device arena, each 256-byte aligned, in DevScene order.

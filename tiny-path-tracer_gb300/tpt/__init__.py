@@ -47,6 +47,16 @@ class RenderParams(C.Structure):
                 ("accumulate_fp64", C.c_int32), ("profile", C.c_int32), ("flat_nodes", C.c_int32)]
 
 
+class Config(C.Structure):
+    """tpt_config: the config.ini keys of main.cpp:29-56."""
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("sample", C.c_int32), ("recur_depth", C.c_int32),
+                ("fov", C.c_float), ("allow_bonus_pic", C.c_int32), ("bonus_pic", C.c_int32),
+                ("aperture", C.c_float), ("start_time", C.c_float), ("end_time", C.c_float)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class RenderStats(C.Structure):
     _fields_ = [("samples", C.c_int64), ("segments", C.c_int64), ("iterations", C.c_int32),
                 ("kernel_launches", C.c_int32), ("device_ms", C.c_double), ("traverse_ms", C.c_double),
@@ -168,6 +178,16 @@ _SIGS = {
                                       C.c_void_p, C.c_int32, C.POINTER(RenderStats), C.POINTER(GuideStats)]),
     "tpt_guide_records": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     "tpt_nrc_params_default": (None, [C.POINTER(NrcParams)]),
+    "tpt_config_default": (None, [C.POINTER(Config)]),
+    "tpt_config_parse": (C.c_int32, [C.c_char_p, C.POINTER(Config)]),
+    "tpt_config_load": (C.c_int32, [C.c_char_p, C.POINTER(Config)]),
+    "tpt_scene_get_camera": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float)]),
+    "tpt_scene_set_camera": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                         C.POINTER(C.c_float), C.c_float, C.c_float, C.c_float, C.c_float,
+                                         C.c_float, C.c_float]),
+    "tpt_render_snapshots": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.c_int32, C.c_void_p,
+                                         C.c_void_p, C.c_int32, C.POINTER(RenderStats)]),
+    "tpt_write_ppm_strip": (C.c_int32, [C.c_char_p, C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_int32]),
     "tpt_render_nrc": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.POINTER(NrcParams),
                                    C.c_void_p, C.c_int32, C.POINTER(RenderStats), C.POINTER(NrcStats)]),
     "tpt_quantize": (None, [C.c_void_p, C.c_int64, C.c_void_p]),
@@ -223,6 +243,27 @@ class Scene:
         i = SceneInfo()
         check(lib().tpt_scene_get_info(self._h, C.byref(i)))
         return i.as_dict()
+
+    def camera(self) -> dict:
+        """The camera inputs (tpt_scene_get_camera)."""
+        v = (C.c_float * 15)()
+        check(lib().tpt_scene_get_camera(self._h, v), "scene_get_camera")
+        v = list(v)
+        return {"lookfrom": v[0:3], "lookat": v[3:6], "vup": v[6:9], "vfov": v[9], "aspect": v[10],
+                "aperture": v[11], "focus": v[12], "time0": v[13], "time1": v[14]}
+
+    def set_camera(self, lookfrom, lookat, vup, vfov, aspect, aperture, focus, time0, time1) -> None:
+        f3 = lambda x: (C.c_float * 3)(*x)
+        check(lib().tpt_scene_set_camera(self._h, f3(lookfrom), f3(lookat), f3(vup), vfov, aspect, aperture, focus,
+                                         time0, time1), "scene_set_camera")
+
+    def apply_config(self, cfg: dict) -> None:
+        """main.cpp:86-90: the camera takes the config's fov, aspect
+        (width / height), aperture and shutter; the scene keeps its viewpoint
+        and focus distance."""
+        c = self.camera()
+        self.set_camera(c["lookfrom"], c["lookat"], c["vup"], cfg["fov"], cfg["width"] / cfg["height"],
+                        cfg["aperture"], c["focus"], cfg["start_time"], cfg["end_time"])
 
     def bvh_dump(self, user_id: int):
         n = lib().tpt_scene_bvh_dump(self._h, user_id, None, None, 0)
@@ -317,6 +358,37 @@ def render_guided(ctx: "Context", slot: int, width: int, height: int, spp: int, 
     check(lib().tpt_render_guided(ctx._h, slot, C.byref(p), C.byref(g), dst, mem, C.byref(st), C.byref(gs)),
           "render_guided")
     return img, st.as_dict(), gs.as_dict()
+
+
+def config(text: str | None = None, path: str | None = None) -> dict:
+    """main.cpp's configuration: the defaults, then `text` (INI) or the file
+    at `path` on top (tpt_config_parse / tpt_config_load)."""
+    c = Config()
+    lib().tpt_config_default(C.byref(c))
+    if text is not None:
+        check(lib().tpt_config_parse(text.encode(), C.byref(c)), "config_parse")
+    if path is not None:
+        check(lib().tpt_config_load(path.encode(), C.byref(c)), "config_load")
+    return c.as_dict()
+
+
+def render_snapshots(ctx: "Context", slot: int, width: int, height: int, spp: int, bonus_pic: int, **kw):
+    """allow_bonus_pic: (final mean, snapshots [bonus_pic, h, w, 3], stats)."""
+    p = make_params(width, height, spp, **kw)
+    img = np.zeros((height, width, 3), np.float32)
+    snaps = np.zeros((max(bonus_pic, 1), height, width, 3), np.float32)
+    st = RenderStats()
+    check(lib().tpt_render_snapshots(ctx._h, slot, C.byref(p), bonus_pic, _ptr(img), _ptr(snaps), TPT_MEM_HOST,
+                                     C.byref(st)), "render_snapshots")
+    return img, snaps[:bonus_pic], st.as_dict()
+
+
+def write_ppm_strip(path: str, images) -> None:
+    """Quantised uint8 images (h, w, 3), side by side in one PPM P3 file."""
+    imgs = [np.ascontiguousarray(im, np.uint8) for im in images]
+    h, w = imgs[0].shape[:2]
+    arr = (C.c_void_p * len(imgs))(*[im.ctypes.data for im in imgs])
+    check(lib().tpt_write_ppm_strip(path.encode(), arr, len(imgs), w, h), "write_ppm_strip")
 
 
 def guide_records(ctx: "Context", cap: int = 1 << 22) -> np.ndarray:
