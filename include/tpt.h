@@ -412,6 +412,11 @@ tpt_status tpt_scene_set_camera(tpt_scene *s, const float lookfrom[3], const flo
  * divides by zero).  Persistent engine; physical or reference semantics. */
 tpt_status tpt_render_snapshots(tpt_context *ctx, int32_t slot, const tpt_render_params *p, int32_t bonus_pic,
                                 float *out_rgb, float *snapshots_rgb, int32_t mem, tpt_render_stats *stats);
+/* Reads a PPM image (P3 or P6, maxval <= 255, '#' comments) for
+ * tpt_image_texture: the stand-in for the stb_image decode of
+ * utils.cc:236-240.  Call with rgb8 = NULL to get the size; then with a
+ * buffer of cap >= width*height*3 bytes (row 0 = top). */
+tpt_status tpt_read_ppm(const char *path, uint8_t *rgb8, int64_t cap, int32_t *width, int32_t *height);
 /* `count` quantised images side by side in one PPM P3 file: the strip
  * main.cpp:222-243 asks ImageMagick's `convert +append` for. */
 tpt_status tpt_write_ppm_strip(const char *path, const uint8_t *const *images, int32_t count, int32_t width,

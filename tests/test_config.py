@@ -137,3 +137,24 @@ def test_config_matches_reference_parser(built):
         ref = pyoracle.ref_config_parse(case)
         for k, r in zip(KEYS, ref):
             assert ours[k] == pytest.approx(r, nan_ok=True), (k, case)
+
+
+def test_read_ppm_p3_p6_and_errors(built, tmp_path):
+    rng = np.random.default_rng(3)
+    img = rng.integers(0, 256, (5, 7, 3), dtype=np.uint8)
+    p3 = tmp_path / "a.ppm"
+    tpt.write_ppm(str(p3), img)
+    np.testing.assert_array_equal(tpt.read_ppm(str(p3)), img)
+    p6 = tmp_path / "b.ppm"
+    p6.write_bytes(b"P6\n# a comment\n7 5\n255\n" + img.tobytes())
+    np.testing.assert_array_equal(tpt.read_ppm(str(p6)), img)
+    p15 = tmp_path / "c.ppm"  # maxval 15: rescaled to 0..255
+    p15.write_text("P3 2 1 15\n0 7 15 15 0 1\n")
+    np.testing.assert_array_equal(tpt.read_ppm(str(p15)), [[[0, 119, 255], [255, 0, 17]]])
+    bad = tmp_path / "bad.ppm"
+    bad.write_text("P3 2 2 255\n1 2 3\n")   # truncated
+    with pytest.raises(tpt.TptError):
+        tpt.read_ppm(str(bad))
+    bad.write_text("P5 2 2 255\n")           # greyscale: not an RGB image
+    with pytest.raises(tpt.TptError):
+        tpt.read_ppm(str(bad))

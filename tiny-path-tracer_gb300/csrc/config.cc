@@ -143,4 +143,67 @@ tpt_status tpt_write_ppm_strip(const char *path, const uint8_t *const *images, i
   return TPT_OK;
 }
 
+// PPM reader for image textures (the reference decodes earthmap.jpg with
+// stb_image, utils.cc:236-240; PPM is the decoder-free stand-in).
+static bool ppm_token(FILE *f, std::string &tok) {
+  tok.clear();
+  int c = std::fgetc(f);
+  for (;;) {
+    while (c != EOF && is_space((char)c)) c = std::fgetc(f);
+    if (c == '#') {  // comment to the end of the line
+      while (c != EOF && c != '\n') c = std::fgetc(f);
+      continue;
+    }
+    break;
+  }
+  while (c != EOF && !is_space((char)c) && c != '#') {
+    tok.push_back((char)c);
+    c = std::fgetc(f);
+  }
+  if (c == '#') std::ungetc(c, f);
+  return !tok.empty();
+}
+
+static bool ppm_int(FILE *f, long &v) {
+  std::string t;
+  if (!ppm_token(f, t)) return false;
+  char *end = nullptr;
+  v = std::strtol(t.c_str(), &end, 10);
+  return end && *end == 0 && v >= 0;
+}
+
+tpt_status tpt_read_ppm(const char *path, uint8_t *rgb8, int64_t cap, int32_t *w, int32_t *h) {
+  if (!path || !w || !h || cap < 0 || (cap > 0 && !rgb8)) return TPT_ERR_INVALID_ARGUMENT;
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return TPT_ERR_INVALID_ARGUMENT;
+  std::string magic;
+  long W = 0, H = 0, maxv = 0;
+  tpt_status st = TPT_OK;
+  if (!ppm_token(f, magic) || (magic != "P3" && magic != "P6") || !ppm_int(f, W) || !ppm_int(f, H) ||
+      !ppm_int(f, maxv) || W <= 0 || H <= 0 || W > (1 << 16) || H > (1 << 16) || maxv <= 0 || maxv > 255) {
+    st = TPT_ERR_PARSE;
+  } else {
+    *w = (int32_t)W;
+    *h = (int32_t)H;
+    const int64_t n = (int64_t)W * H * 3;
+    if (rgb8 && cap >= n) {
+      for (int64_t i = 0; i < n && st == TPT_OK; i++) {
+        long v = 0;
+        if (magic == "P3") {
+          if (!ppm_int(f, v) || v > maxv) st = TPT_ERR_PARSE;
+        } else {
+          const int c = std::fgetc(f);
+          if (c == EOF || c > maxv) st = TPT_ERR_PARSE;
+          v = c;
+        }
+        rgb8[i] = (uint8_t)(maxv == 255 ? v : (v * 255 + maxv / 2) / maxv);
+      }
+    } else if (rgb8) {
+      st = TPT_ERR_INVALID_ARGUMENT;  // buffer smaller than width*height*3
+    }
+  }
+  std::fclose(f);
+  return st;
+}
+
 }  // extern "C"

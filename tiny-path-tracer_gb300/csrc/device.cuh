@@ -645,7 +645,9 @@ __device__ float perlin_noise(const DevScene &S, float3 p) {
       }
   return fabsf(acc);
 }
-__device__ float perlin_turb(const DevScene &S, float3 p) {  // utils.cc:193-203
+// Out of line: one copy shared by every texture lookup site keeps the fused
+// render loops smaller (instruction-cache pressure), and perlin textures are rare.
+__device__ __noinline__ float perlin_turb(const DevScene &S, float3 p) {  // utils.cc:193-203
   float acc = 0.f, weight = 1.f;
   for (int i = 0; i < 5; i++) {
     acc += weight * perlin_noise(S, p);
@@ -731,7 +733,19 @@ __device__ float light_item_pdf(const DevScene &S, int i, float3 o, float3 d) {
     return d2 / (cosine * area);
   }
   if (li.x == LS_SPHERE) {
-    if (!sphere_t(f3(a), a.w, r, 0.001f, 3.402823466e38f, t)) return 0.f;
+    // sphere::pdf_value (sphere.cc:93-106) only asks whether the ray hits the
+    // sphere in (0.001, FLT_MAX); a float test (not the double-root
+    // reproduction of the closest-hit path) differs only on grazing rays,
+    // a set of measure zero for the estimate
+    {
+      const float3 oc = o - f3(a);
+      const float qa = dot3(d, d), qb = dot3(oc, d), qc = dot3(oc, oc) - a.w * a.w;
+      const float disc = qb * qb - qa * qc;
+      if (!(disc > 0.f)) return 0.f;
+      const float sq = sqrtf(disc);
+      // a root t = (-qb -/+ sq) / qa lies beyond 0.001 (qa > 0)
+      if (!(-qb + sq > 0.001f * qa)) return 0.f;
+    }
     const float3 oc = f3(a) - o;
     const float tmp = (a.w * a.w) / dot3(oc, oc);
     const float cmax = sqrtf(1.f - tmp);

@@ -100,13 +100,11 @@ __global__ void __launch_bounds__(WARPS * 32)
   extern __shared__ __half smem[];
   __half *sw = smem;
   __half *swt = sw + smem_w_halves(n);
-  uint32_t *sh = reinterpret_cast<uint32_t *>(swt + smem_wt_halves(n));  // [warp][layer][16][32] h frags
-  float *sy = reinterpret_cast<float *>(sh + WARPS * NH * 16 * 32);      // [warp][16][OUT]
-  float *sdy = sy + WARPS * 16 * OUT;                                     // [warp][16][OUT]
+  float *sy = reinterpret_cast<float *>(swt + smem_wt_halves(n));  // [warp][16][OUT]
+  float *sdy = sy + WARPS * 16 * OUT;                               // [warp][16][OUT]
   load_weights(n, sw, swt);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  uint32_t *my_h = sh + warp * NH * 16 * 32;
   float *my_y = sy + warp * 16 * OUT, *my_dy = sdy + warp * 16 * OUT;
   // transposed activation / gradient buffers per layer
   size_t ht_off[NH + 1], dz_off[NH + 1];
@@ -130,13 +128,22 @@ __global__ void __launch_bounds__(WARPS * 32)
     layer_mma<IN, HID>(a0, sw + smem_w_offset(n, 0), acc);
     uint32_t h[HID / 16][4];
     relu_to_frag<HID>(acc, h);
+    // ReLU masks: bit (kk*4 + i)*2 + half of mask[l-1] says whether this
+    // lane's value of H_l (the input of layer l) is positive
+    uint32_t mask[NH];
 #pragma unroll
     for (int l = 1; l <= NH; l++) {
-      // h = H_l (input of layer l): keep for the masks and the weight gradient
+      // h = H_l (input of layer l): keep its mask and store it for the weight gradient
+      uint32_t m = 0;
 #pragma unroll
       for (int kk = 0; kk < HID / 16; kk++)
 #pragma unroll
-        for (int i = 0; i < 4; i++) my_h[((l - 1) * 16 + kk * 4 + i) * 32 + lane] = h[kk][i];
+        for (int i = 0; i < 4; i++) {
+          const uint32_t v = h[kk][i];
+          m |= (uint32_t)((v & 0x7fffu) != 0 && !(v & 0x8000u)) << ((kk * 4 + i) * 2);
+          m |= (uint32_t)((v & 0x7fff0000u) != 0 && !(v & 0x80000000u)) << ((kk * 4 + i) * 2 + 1);
+        }
+      mask[l - 1] = m;
       store_frag_t<HID>(h, Ht + ht_off[l], rows, r0);
       if (l < NH) {
         layer_mma<HID, HID>(h, sw + smem_w_offset(n, l), acc);
@@ -173,16 +180,16 @@ __global__ void __launch_bounds__(WARPS * 32)
 #pragma unroll
     for (int l = NH - 1; l >= 0; l--) {
       // mask with H_{l+1} > 0 (the ReLU output of layer l)
+      const uint32_t m = mask[l];
 #pragma unroll
       for (int kk = 0; kk < HID / 16; kk++) {
-        const float2 m0 = unpack2(my_h[(l * 16 + kk * 4 + 0) * 32 + lane]);
-        const float2 m1 = unpack2(my_h[(l * 16 + kk * 4 + 1) * 32 + lane]);
-        const float2 m2 = unpack2(my_h[(l * 16 + kk * 4 + 2) * 32 + lane]);
-        const float2 m3 = unpack2(my_h[(l * 16 + kk * 4 + 3) * 32 + lane]);
-        dz[kk][0] = pack2_sat(m0.x > 0.f ? acc[2 * kk][0] : 0.f, m0.y > 0.f ? acc[2 * kk][1] : 0.f);
-        dz[kk][1] = pack2_sat(m1.x > 0.f ? acc[2 * kk][2] : 0.f, m1.y > 0.f ? acc[2 * kk][3] : 0.f);
-        dz[kk][2] = pack2_sat(m2.x > 0.f ? acc[2 * kk + 1][0] : 0.f, m2.y > 0.f ? acc[2 * kk + 1][1] : 0.f);
-        dz[kk][3] = pack2_sat(m3.x > 0.f ? acc[2 * kk + 1][2] : 0.f, m3.y > 0.f ? acc[2 * kk + 1][3] : 0.f);
+        const int b = kk * 8;
+        dz[kk][0] = pack2_sat((m >> (b + 0)) & 1 ? acc[2 * kk][0] : 0.f, (m >> (b + 1)) & 1 ? acc[2 * kk][1] : 0.f);
+        dz[kk][1] = pack2_sat((m >> (b + 2)) & 1 ? acc[2 * kk][2] : 0.f, (m >> (b + 3)) & 1 ? acc[2 * kk][3] : 0.f);
+        dz[kk][2] = pack2_sat((m >> (b + 4)) & 1 ? acc[2 * kk + 1][0] : 0.f,
+                              (m >> (b + 5)) & 1 ? acc[2 * kk + 1][1] : 0.f);
+        dz[kk][3] = pack2_sat((m >> (b + 6)) & 1 ? acc[2 * kk + 1][2] : 0.f,
+                              (m >> (b + 7)) & 1 ? acc[2 * kk + 1][3] : 0.f);
       }
       store_frag_t<HID>(dz, dZt + dz_off[l], rows, r0);
       if (l > 0) layer_mma<HID, HID>(dz, swt + smem_wt_offset(n, l), acc);
@@ -597,8 +604,7 @@ bool supported(int in, int nh, int out) {
 }
 
 size_t train_smem(const Net &n) {
-  return (size_t)(smem_w_halves(n) + smem_wt_halves(n)) * 2 + (size_t)WARPS * n.n_hidden * 16 * 32 * 4 +
-         (size_t)2 * WARPS * 16 * n.out_dim * 4;
+  return (size_t)(smem_w_halves(n) + smem_wt_halves(n)) * 2 + (size_t)2 * WARPS * 16 * n.out_dim * 4;
 }
 
 template <int IN, int NH, int OUT>
@@ -629,7 +635,7 @@ tpt_status launch_train(tpt_mlp *M, const __half *x, int rows, const Loss &loss,
   MLP_CUDA(cudaMemsetAsync(M->loss, 0, sizeof(float), s));
   k_mlp_train<IN, NH, OUT, Loss><<<grid, WARPS * 32, smem, s>>>(M->net, x, rows, loss, M->ht, M->dzt, M->loss);
   MLP_CUDA(cudaGetLastError());
-  const int chunk = 512;
+  const int chunk = 256;  // rows per weight-gradient warp: ~1000 warps for a 16384-row batch
   const int n_chunks = (rows + chunk - 1) / chunk;
   int units = 0;
   for (int l = 0; l <= NH; l++) units += ((l == NH ? OUT : HID) / 16) * n_chunks;

@@ -188,6 +188,7 @@ _SIGS = {
     "tpt_render_snapshots": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.c_int32, C.c_void_p,
                                          C.c_void_p, C.c_int32, C.POINTER(RenderStats)]),
     "tpt_write_ppm_strip": (C.c_int32, [C.c_char_p, C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_int32]),
+    "tpt_read_ppm": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "tpt_render_nrc": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.POINTER(NrcParams),
                                    C.c_void_p, C.c_int32, C.POINTER(RenderStats), C.POINTER(NrcStats)]),
     "tpt_quantize": (None, [C.c_void_p, C.c_int64, C.c_void_p]),
@@ -389,6 +390,15 @@ def write_ppm_strip(path: str, images) -> None:
     h, w = imgs[0].shape[:2]
     arr = (C.c_void_p * len(imgs))(*[im.ctypes.data for im in imgs])
     check(lib().tpt_write_ppm_strip(path.encode(), arr, len(imgs), w, h), "write_ppm_strip")
+
+
+def read_ppm(path: str) -> np.ndarray:
+    """A PPM image (P3/P6) as uint8 (h, w, 3), row 0 = top."""
+    w, h = C.c_int32(), C.c_int32()
+    check(lib().tpt_read_ppm(path.encode(), None, 0, C.byref(w), C.byref(h)), "read_ppm")
+    img = np.zeros((h.value, w.value, 3), np.uint8)
+    check(lib().tpt_read_ppm(path.encode(), _ptr(img), img.size, C.byref(w), C.byref(h)), "read_ppm")
+    return img
 
 
 def guide_records(ctx: "Context", cap: int = 1 << 22) -> np.ndarray:
