@@ -49,10 +49,15 @@ WORKLOAD = "cornell_box_600x600_1024spp_depth50"
 # written + read, path state 48 B read + written (the dominant kernel pair)
 BYTES_PER_SEGMENT = 192
 TRAVERSE_BYTES_PER_SEGMENT = 64 + 16  # traverse reads the path record, writes the hit
-# k_persistent DRAM read+write bytes per ray segment, from the ncu capture of
-# the 16 spp case (profiles/k_persistent_cornell_600x600_16spp.md):
-# 5.872 MB / 30.42 M segments
-NCU_DRAM_BYTES_PER_SEGMENT = 5.872128e6 / 30416883
+# k_persistent DRAM read+write bytes and warp instructions per ray segment,
+# from the ncu capture of the 16 spp case
+# (profiles/k_persistent_cornell_600x600_16spp.md): 7.634 MB and 3.454 G warp
+# instructions over 30.42 M segments
+NCU_DRAM_BYTES_PER_SEGMENT = 7.633664e6 / 30416883
+NCU_WARP_INST_PER_SEGMENT = 3454032782 / 30416883
+# instruction issue peak: 152 SMs x 4 schedulers x 1 warp instruction per
+# cycle at the maximum SM clock (MEASURED_PEAKS.json sm_max_mhz)
+SMS, SCHEDULERS_PER_SM = 152, 4
 
 
 def _peaks() -> dict:
@@ -60,8 +65,8 @@ def _peaks() -> dict:
     if os.path.exists(p):
         with open(p) as f:
             d = json.load(f)
-        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
-    return {"hbm_gbs": 6800.0, "source": "fallback"}
+        return {"hbm_gbs": float(d["hbm_gbs"]), "sm_mhz": float(d.get("sm_max_mhz", 2070.0)), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "sm_mhz": 2070.0, "source": "fallback"}
 
 
 class ClockSampler:
@@ -202,7 +207,7 @@ def batch_bench(args) -> None:
     ctx.set_stream(stream.cuda_stream)
     sds = scenes.batch_scenes(seed=2, count=64)
     t0 = time.perf_counter()
-    slots = [ctx.upload(tpt.Scene(sd.text())) for sd in sds]
+    slots = [ctx.upload(tpt.Scene(sd.text(), bvh=args.bvh)) for sd in sds]
     build_s = time.perf_counter() - t0
     jobs = [(slot, sd.meta["width"], sd.meta["height"], sd.meta["spp"]) for slot, sd in zip(slots, sds)]
     outs = [torch.empty((h, w, 3), dtype=torch.float32, device="cuda") for _, w, h, _ in jobs]
@@ -229,6 +234,7 @@ def batch_bench(args) -> None:
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": "batch_64_random_sphere_scenes", "scenes": len(jobs), "samples_per_step": samples,
+                      "bvh": args.bvh,
                       "spheres": [sd.meta["n_spheres"] for sd in sds][:8] + ["..."],
                       "segments_per_step": st["segments"], "scene_build_and_upload_s": build_s},
            "gpu_launches": st["kernel_launches"] * args.steps, "clocks": clk}
@@ -309,6 +315,8 @@ def main() -> None:
     ap.add_argument("--wave", type=int, default=0)
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--bvh", default="reference", choices=["reference", "sah"],
+                    help="batch workload: the reference's BVH topology or the SAH rebuild")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the equal-time guided / cached comparisons of the default line")
     ap.add_argument("--spp", type=int, default=SPP, help="smaller cases for profiling only")
@@ -428,7 +436,16 @@ def main() -> None:
                 "kernel_share": tr_ms / ms,
                 "note": ("algorithmic bytes = the wavefront traffic floor per ray segment (ray, hit and path "
                          "state written and read); the kernel keeps that state in registers and the scene in "
-                         "L1/L2, so it is issue-bound, not HBM-bound (ncu: issue active 45% of peak)")}
+                         "L1/L2, so it is issue-bound, not HBM-bound: see issue_roofline")}
+        if not wavefront:
+            peak_issue = SMS * SCHEDULERS_PER_SM * peaks["sm_mhz"] / 1e3  # G warp instructions / s
+            ach_issue = seg_per_launch * NCU_WARP_INST_PER_SEGMENT / (tr_ms / tr_n / 1e3) / 1e9
+            roof["issue_roofline"] = {
+                "bound": "issue", "achieved": ach_issue, "peak": peak_issue, "unit": "G warp-inst/s",
+                "frac": ach_issue / peak_issue, "warp_inst_per_segment": NCU_WARP_INST_PER_SEGMENT,
+                "note": ("the binding roof: instructions per segment from the ncu capture of the same kernel "
+                         "(16 spp case) x segments per second measured here; peak = 152 SMs x 4 schedulers x "
+                         "1 instruction per cycle at the maximum SM clock")}
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,

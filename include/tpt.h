@@ -121,6 +121,18 @@ tpt_status tpt_scene_compile(const tpt_builder *b, tpt_scene **out);
 /* Parse scene-description text (the statement format documented in
  * docs of the package loader) into a builder and compile it. */
 tpt_status tpt_scene_from_text(const char *sd_text, tpt_scene **out, char *err, size_t errlen);
+/* BVH topology the compiler flattens for every bvh_node.  REFERENCE (the
+ * default) is the reference's own tree (random axis, median split,
+ * hitable.cc:32-56), required for closest-hit parity.  SAH rebuilds each
+ * bvh_node's primitives with a binned surface-area heuristic (no
+ * counterpart in the reference): the same closest hits except which of
+ * several primitives at exactly equal t wins, and renders that agree
+ * statistically, usually faster on large scenes.  tpt_scene_bvh_dump always
+ * reports the reference tree. */
+enum { TPT_BVH_REFERENCE = 0, TPT_BVH_SAH = 1 };
+tpt_status tpt_builder_set_bvh_build(tpt_builder *b, int32_t mode);
+tpt_status tpt_scene_from_text_opt(const char *sd_text, int32_t bvh_build, tpt_scene **out, char *err,
+                                   size_t errlen);
 void tpt_scene_destroy(tpt_scene *s);
 
 typedef struct {

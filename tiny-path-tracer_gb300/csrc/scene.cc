@@ -106,6 +106,7 @@ struct tpt_builder {
   bool has_cam = false;
   Camera cam{};
   float cam_in[15] = {};  // tpt_builder_set_camera's arguments
+  int bvh_build = TPT_BVH_REFERENCE;  // topology the compiler flattens
   std::string err;
 
   double drand(double a = 0.0, double b = 1.0) {
@@ -521,10 +522,19 @@ int32_t tpt_bvh_node(tpt_builder *b, const int32_t *items, int32_t n, float t0, 
     if (!b->valid_node(h)) return -TPT_ERR_BAD_HANDLE;
   int root = build_bvh(*b, l.data(), n, t0, t1);
   if (root < 0) return root;
-  // the root becomes a user-visible hitable
+  // the root becomes a user-visible hitable; it keeps the shutter interval
+  // for rebuilds of its topology (TPT_BVH_SAH)
   b->nodes[root].internal = false;
+  b->nodes[root].t0 = t0;
+  b->nodes[root].t1 = t1;
   if (b->auto_user) b->set_user(root, root);
   return root;
+}
+
+tpt_status tpt_builder_set_bvh_build(tpt_builder *b, int32_t mode) {
+  if (!b || (mode != TPT_BVH_REFERENCE && mode != TPT_BVH_SAH)) return TPT_ERR_INVALID_ARGUMENT;
+  b->bvh_build = mode;
+  return TPT_OK;
 }
 
 tpt_status tpt_builder_set_world(tpt_builder *b, int32_t world) {
@@ -673,6 +683,7 @@ struct Compiler {
   }
 
   int flatten_bvh(int h, bool in_blas, int depth, int &max_depth) {
+    if (B.bvh_build == TPT_BVH_SAH) return flatten_sah(h, in_blas, depth, max_depth);
     if (depth > max_depth) max_depth = depth;
     const HNode &n = B.nodes[h];
     int me = (int)S.node_lo.size();
@@ -700,6 +711,142 @@ struct Compiler {
     std::memcpy(&S.node_lo[me].w, &lref, 4);
     std::memcpy(&S.node_hi[me].w, &rref, 4);
     S.node_skip[me] = (int32_t)S.node_lo.size();  // subtree = [me, skip)
+    return me;
+  }
+
+  // ---- alternative topology: binned surface-area-heuristic rebuild of a
+  // bvh_node's primitives (Wald 2007, "On fast Construction of SAH-based
+  // Bounding Volume Hierarchies"), flattened in the same pre-order layout.
+  struct SahLeaf {
+    int h;
+    box3 box;
+    float c[3];
+  };
+
+  void sah_collect(int h, float t0, float t1, std::vector<SahLeaf> &out) {
+    const HNode &n = B.nodes[h];
+    if (n.kind == H_BVH) {
+      sah_collect(n.left, t0, t1, out);
+      if (n.right != n.left) sah_collect(n.right, t0, t1, out);
+      return;
+    }
+    SahLeaf l;
+    l.h = h;
+    if (!hbox(B, h, t0, t1, l.box)) {
+      fail(TPT_ERR_NO_BOUNDING_BOX, "primitive without a bounding box under bvh_node");
+      return;
+    }
+    for (int a = 0; a < 3; a++) l.c[a] = 0.5f * (l.box.mn.e[a] + l.box.mx.e[a]);
+    out.push_back(l);
+  }
+
+  static float half_area(const box3 &b) {
+    const float x = b.mx.e[0] - b.mn.e[0], y = b.mx.e[1] - b.mn.e[1], z = b.mx.e[2] - b.mn.e[2];
+    return x * y + y * z + z * x;
+  }
+
+  int sah_leaf_ref(const SahLeaf &l, bool in_blas) {
+    const int leaf = in_blas ? blas_leaf(l.h) : any_leaf(l.h, 0);
+    return leaf < 0 ? INT32_MIN : ~leaf;
+  }
+
+  int flatten_sah(int h, bool in_blas, int depth, int &max_depth) {
+    std::vector<SahLeaf> leaves;
+    sah_collect(h, B.nodes[h].t0, B.nodes[h].t1, leaves);
+    if (st != TPT_OK || leaves.empty()) return -1;
+    return sah_emit(leaves, 0, (int)leaves.size(), in_blas, depth, max_depth);
+  }
+
+  // SAH splits down to depth 16, then halving by count: a 5000-primitive
+  // tree stays within the device traversal stack.
+  int sah_emit(std::vector<SahLeaf> &sah_leaves, int b, int e, bool in_blas, int depth, int &max_depth) {
+    if (depth > max_depth) max_depth = depth;
+    box3 bb = sah_leaves[b].box, cb{};
+    for (int a = 0; a < 3; a++) cb.mn.e[a] = cb.mx.e[a] = sah_leaves[b].c[a];
+    for (int i = b + 1; i < e; i++) {
+      bb = surround(bb, sah_leaves[i].box);
+      for (int a = 0; a < 3; a++) {
+        cb.mn.e[a] = std::min(cb.mn.e[a], sah_leaves[i].c[a]);
+        cb.mx.e[a] = std::max(cb.mx.e[a], sah_leaves[i].c[a]);
+      }
+    }
+    const int me = (int)S.node_lo.size();
+    S.node_lo.push_back(f4{bb.mn.e[0], bb.mn.e[1], bb.mn.e[2], 0});
+    S.node_hi.push_back(f4{bb.mx.e[0], bb.mx.e[1], bb.mx.e[2], 0});
+    S.node_skip.push_back(0);
+    int mid = b + 1;
+    if (e - b > 1) {
+      // 16 bins per axis on the centroid bounds; cost = A_l N_l + A_r N_r
+      enum { BINS = 16 };
+      float best = std::numeric_limits<float>::infinity();
+      int best_axis = -1, best_bin = 0;
+      for (int a = 0; a < 3 && depth < 16; a++) {
+        const float lo = cb.mn.e[a], ext = cb.mx.e[a] - lo;
+        if (!(ext > 0.f)) continue;
+        int cnt[BINS] = {};
+        box3 bx[BINS];
+        for (int i = b; i < e; i++) {
+          int k = (int)((sah_leaves[i].c[a] - lo) / ext * BINS);
+          k = std::min(std::max(k, 0), BINS - 1);
+          bx[k] = cnt[k] ? surround(bx[k], sah_leaves[i].box) : sah_leaves[i].box;
+          cnt[k]++;
+        }
+        float right_area[BINS];
+        int right_n[BINS];
+        box3 acc{};
+        int n = 0;
+        for (int k = BINS - 1; k > 0; k--) {
+          if (cnt[k]) acc = n ? surround(acc, bx[k]) : bx[k];
+          n += cnt[k];
+          right_area[k] = n ? half_area(acc) : 0.f;
+          right_n[k] = n;
+        }
+        acc = box3{};
+        n = 0;
+        for (int k = 0; k < BINS - 1; k++) {
+          if (cnt[k]) acc = n ? surround(acc, bx[k]) : bx[k];
+          n += cnt[k];
+          if (n == 0 || right_n[k + 1] == 0) continue;
+          const float cost = half_area(acc) * n + right_area[k + 1] * right_n[k + 1];
+          if (cost < best) {
+            best = cost;
+            best_axis = a;
+            best_bin = k;
+          }
+        }
+      }
+      if (best_axis >= 0) {
+        const float lo = cb.mn.e[best_axis], ext = cb.mx.e[best_axis] - lo;
+        auto it = std::stable_partition(sah_leaves.begin() + b, sah_leaves.begin() + e, [&](const SahLeaf &l) {
+          int k = (int)((l.c[best_axis] - lo) / ext * BINS);
+          return std::min(std::max(k, 0), (int)BINS - 1) <= best_bin;
+        });
+        mid = (int)(it - sah_leaves.begin());
+      }
+      if (best_axis < 0 || mid <= b || mid >= e) {  // coincident centroids or too deep: halve by count
+        int a = 0;
+        for (int k = 1; k < 3; k++)
+          if (cb.mx.e[k] - cb.mn.e[k] > cb.mx.e[a] - cb.mn.e[a]) a = k;
+        std::stable_sort(sah_leaves.begin() + b, sah_leaves.begin() + e,
+                         [a](const SahLeaf &x, const SahLeaf &y) { return x.c[a] < y.c[a]; });
+        mid = b + (e - b) / 2;
+      }
+    }
+    int refs[2];
+    const int rb[2] = {b, mid}, re[2] = {mid, e};
+    for (int c = 0; c < 2; c++) {
+      if (e - b == 1) {  // a single primitive: left == right, as bvh_node with n == 1
+        refs[1] = refs[0] = sah_leaf_ref(sah_leaves[b], in_blas);
+        break;
+      }
+      refs[c] = re[c] - rb[c] == 1 ? sah_leaf_ref(sah_leaves[rb[c]], in_blas)
+                                   : sah_emit(sah_leaves, rb[c], re[c], in_blas, depth + 1, max_depth);
+      if (st != TPT_OK) return -1;
+    }
+    if (st != TPT_OK) return -1;
+    std::memcpy(&S.node_lo[me].w, &refs[0], 4);
+    std::memcpy(&S.node_hi[me].w, &refs[1], 4);
+    S.node_skip[me] = (int32_t)S.node_lo.size();
     return me;
   }
 
@@ -1081,10 +1228,15 @@ int32_t tpt_scene_bvh_dump(const tpt_scene *s, int32_t user, float *boxes, int32
 // loader documentation): builder calls in file order, SD ids kept as the
 // user ids reported for hits and dumps.
 tpt_status tpt_scene_from_text(const char *text, tpt_scene **out, char *err, size_t errlen) {
+  return tpt_scene_from_text_opt(text, TPT_BVH_REFERENCE, out, err, errlen);
+}
+
+tpt_status tpt_scene_from_text_opt(const char *text, int32_t bvh_build, tpt_scene **out, char *err, size_t errlen) {
   if (!text || !out) return TPT_ERR_INVALID_ARGUMENT;
   tpt_builder *b = nullptr;
   tpt_builder_create(&b);
   std::unique_ptr<tpt_builder> guard(b);
+  if (tpt_builder_set_bvh_build(b, bvh_build) != TPT_OK) return TPT_ERR_INVALID_ARGUMENT;
   b->perlin_draws = false;  // scene text carries explicit perlin tables
   b->auto_user = false;     // hits and dumps report SD ids
   std::unordered_map<int, int> tex, mat, node;

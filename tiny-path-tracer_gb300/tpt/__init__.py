@@ -27,6 +27,7 @@ BACKGROUND_SKY = 1
 ENGINE_AUTO = 0
 ENGINE_WAVEFRONT = 1
 ENGINE_PERSISTENT = 2
+BVH_REFERENCE, BVH_SAH = 0, 1
 
 STATUS = {0: "TPT_OK", 1: "TPT_ERR_INVALID_ARGUMENT", 2: "TPT_ERR_PARSE", 3: "TPT_ERR_UNSUPPORTED",
           4: "TPT_ERR_NO_BOUNDING_BOX", 5: "TPT_ERR_CUDA", 6: "TPT_ERR_OUT_OF_MEMORY",
@@ -179,6 +180,8 @@ _SIGS = {
     "tpt_guide_records": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     "tpt_nrc_params_default": (None, [C.POINTER(NrcParams)]),
     "tpt_config_default": (None, [C.POINTER(Config)]),
+    "tpt_builder_set_bvh_build": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "tpt_scene_from_text_opt": (C.c_int32, [C.c_char_p, C.c_int32, C.POINTER(C.c_void_p), C.c_char_p, C.c_size_t]),
     "tpt_config_parse": (C.c_int32, [C.c_char_p, C.POINTER(Config)]),
     "tpt_config_load": (C.c_int32, [C.c_char_p, C.POINTER(Config)]),
     "tpt_scene_get_camera": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float)]),
@@ -228,10 +231,13 @@ def _ptr(a):
 class Scene:
     """A compiled scene (host arena) built from scene-description text."""
 
-    def __init__(self, sd_text: str):
+    def __init__(self, sd_text: str, bvh: str = "reference"):
+        """bvh: "reference" (the reference's tree, closest-hit parity) or
+        "sah" (binned SAH rebuild of every bvh_node, TPT_BVH_SAH)."""
         h = C.c_void_p()
         err = C.create_string_buffer(512)
-        st = lib().tpt_scene_from_text(sd_text.encode(), C.byref(h), err, 512)
+        mode = {"reference": BVH_REFERENCE, "sah": BVH_SAH}[bvh]
+        st = lib().tpt_scene_from_text_opt(sd_text.encode(), mode, C.byref(h), err, 512)
         if st != 0:
             raise TptError(st, err.value.decode())
         self._h = h
