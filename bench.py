@@ -252,7 +252,8 @@ def learned_equal_time(ctx, which: str) -> dict:
     both scored by relMSE against an FP64-accumulated high-spp plain render
     (physical semantics).  Times are wall-clock milliseconds of the whole
     call (training, table refresh / cache inference included), images left
-    on the device.
+    on the device; both sides run on the engine the autotuner picks for the
+    scene, so the plain baseline is the tracer's best configuration.
 
     guided: Cornell box with the 40x40 light and the second box, 600x600,
             plain at 1024 spp against guided at the spp that takes the same
@@ -273,6 +274,9 @@ def learned_equal_time(ctx, which: str) -> dict:
         sd, w, h, spp, ref_spp = scenes.next_week(), 800, 800, 256, 4096
         run = lambda n, out: tpt.render_nrc(ctx, slot, w, h, n, seed=5, out=out)
     slot = ctx.upload(tpt.Scene(sd.text()))
+    # both sides use the engine the autotuner picks for this scene (physical
+    # semantics): the plain baseline is the tracer's best configuration
+    tuned = tpt.autotune(ctx, slot, w, h, 4, semantics=tpt.SEMANTICS_PHYSICAL)
     dev = torch.empty((h, w, 3), dtype=torch.float32, device="cuda")
 
     def timed(fn):
@@ -297,6 +301,7 @@ def learned_equal_time(ctx, which: str) -> dict:
     ctx.release(slot)
     name = "cornell_40x40_light_two_boxes" if which == "guided" else "next_week_final_seeded"
     return {"scene": name, "width": w, "height": h, "ref_spp_fp64": ref_spp,
+            "engine": ["auto", "wavefront", "persistent"][tuned[0]],
             "plain": {"spp": spp, "ms": t_plain, "relmse": e_plain},
             which: {"spp": spp, "ms": t_eq, "relmse": e_eq, "stats": r[2]},
             which + "_equal_time": {"spp": spp_et, "ms": t_et, "relmse": e_et},

@@ -203,6 +203,8 @@ typedef struct {
   int32_t accumulate_fp64;  /* 1: also accumulate in double (out_rgb is the FP64 mean) */
   int32_t profile;          /* 1: time each traverse/shade launch with CUDA events */
   int32_t flat_nodes;       /* stackless-walk size limit; 0 = the context option */
+  int32_t refill;           /* persistent engines: a warp's finished lanes take new camera
+                               samples once at least this many are idle (1..32; 0 = 1) */
 } tpt_render_params;
 
 typedef struct {

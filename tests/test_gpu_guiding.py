@@ -1,8 +1,9 @@
 """Learned path guiding on the GPU: the guided estimator is unbiased (its
 per-pixel means agree with the plain tracer's, physical semantics), online
 training lowers the guiding loss, and on the small-light Cornell box the
-trained guide does not lose to the plain tracer at equal spp (relMSE against
-a high-spp FP64-accumulated plain render)."""
+trained guide lowers the error of the plain tracer at equal spp (relMSE
+against a high-spp FP64-accumulated plain render).  Both engines (wavefront,
+persistent) carry the guided renderer."""
 import numpy as np
 import pytest
 
@@ -18,12 +19,14 @@ def relmse(x, ref):
     return float(np.mean((x - ref) ** 2 / (ref * ref + EPS)))
 
 
-def test_guided_is_unbiased(ctx):
+@pytest.mark.parametrize("engine", [tpt.ENGINE_WAVEFRONT, tpt.ENGINE_PERSISTENT], ids=["wavefront", "persistent"])
+def test_guided_is_unbiased(ctx, engine):
     slot = ctx.upload(tpt.Scene(scenes.cornell_guiding().text()))
     w = h = 32
     k = 8
     guided = np.stack([tpt.render_guided(ctx, slot, w, h, 64, seed=10 + i, passes=4, train_steps=16, batch=4096,
-                                         grid_res=8, record_cap=1 << 16)[0] for i in range(k)]).astype(np.float64)
+                                         grid_res=8, record_cap=1 << 16, engine=engine)[0]
+                       for i in range(k)]).astype(np.float64)
     plain = np.stack([ctx.render(slot, w, h, 64, semantics=tpt.SEMANTICS_PHYSICAL, seed=100 + i)[0]
                       for i in range(k)]).astype(np.float64)
     ma, mb = guided.mean(axis=(1, 2, 3)), plain.mean(axis=(1, 2, 3))
@@ -42,15 +45,20 @@ def test_guided_is_unbiased(ctx):
     ctx.release(slot)
 
 
-def test_training_lowers_the_loss(ctx):
+@pytest.mark.parametrize("engine", [tpt.ENGINE_WAVEFRONT, tpt.ENGINE_PERSISTENT], ids=["wavefront", "persistent"])
+def test_training_lowers_the_loss(ctx, engine):
     slot = ctx.upload(tpt.Scene(scenes.cornell_guiding().text()))
-    _, _, g1 = tpt.render_guided(ctx, slot, 48, 48, 16, passes=2, train_steps=1, batch=8192, seed=3)
-    _, _, g2 = tpt.render_guided(ctx, slot, 48, 48, 16, passes=2, train_steps=300, batch=8192, seed=3)
+    _, _, g1 = tpt.render_guided(ctx, slot, 48, 48, 16, passes=2, train_steps=1, batch=8192, seed=3, engine=engine)
+    _, _, g2 = tpt.render_guided(ctx, slot, 48, 48, 16, passes=2, train_steps=300, batch=8192, seed=3,
+                                 engine=engine)
+    rec = tpt.guide_records(ctx)
+    assert np.isfinite(rec).all() and (rec[:, 3] >= 0).all()
+    assert np.allclose(np.linalg.norm(rec[:, 8:11], axis=1), 1.0, atol=1e-3)
     assert g1["records"] > 1000 and g2["final_loss"] < g1["final_loss"], (g1, g2)
     ctx.release(slot)
 
 
-def test_guided_does_not_lose_at_equal_spp(ctx):
+def test_guided_gains_at_equal_spp(ctx):
     slot = ctx.upload(tpt.Scene(scenes.cornell_guiding().text()))
     w = h = 64
     ref, _ = ctx.render(slot, w, h, 16384, semantics=tpt.SEMANTICS_PHYSICAL, seed=999, fp64=True)
@@ -59,5 +67,6 @@ def test_guided_does_not_lose_at_equal_spp(ctx):
     guided = [relmse(tpt.render_guided(ctx, slot, w, h, 256, seed=40 + i, passes=8, train_steps=32)[0], ref)
               for i in range(3)]
     print("relMSE plain", np.mean(plain), "guided", np.mean(guided))
-    assert np.mean(guided) < 1.1 * np.mean(plain)
+    # what the trained guide gains over the plain mixture: lower error per sample
+    assert np.mean(guided) < 0.95 * np.mean(plain)
     ctx.release(slot)

@@ -1,8 +1,9 @@
 """Neural radiance cache on the GPU: with the cache never queried the
 renderer is the plain tracer (statistically identical images); online
-training lowers the cache loss; a cached render is finite and its relMSE
-against a high-spp FP64 plain render stays within a bound of the plain
-tracer's at equal spp (the cache trades bias for shorter paths)."""
+training lowers the cache loss; and the cached render's relMSE against a
+high-spp FP64 plain render is below the plain tracer's at equal spp (the
+cache trades a small bias for much less variance and shorter paths).  Both
+engines (wavefront, persistent) carry the cached renderer."""
 import numpy as np
 import pytest
 
@@ -21,12 +22,13 @@ def _slot(ctx):
     return ctx.upload(tpt.Scene(scenes.next_week(image_size=(256, 128)).text()))
 
 
-def test_uncached_nrc_render_equals_plain_tracer(ctx):
+@pytest.mark.parametrize("engine", [tpt.ENGINE_WAVEFRONT, tpt.ENGINE_PERSISTENT], ids=["wavefront", "persistent"])
+def test_uncached_nrc_render_equals_plain_tracer(ctx, engine):
     slot = _slot(ctx)
     w = h = 24
     k = 6
     a = np.stack([tpt.render_nrc(ctx, slot, w, h, 32, seed=10 + i, passes=2, terminate_depth=1 << 20,
-                                 train_steps=4, batch=1024)[0] for i in range(k)]).astype(np.float64)
+                                 train_steps=4, batch=1024, engine=engine)[0] for i in range(k)]).astype(np.float64)
     b = np.stack([ctx.render(slot, w, h, 32, semantics=tpt.SEMANTICS_PHYSICAL, seed=200 + i)[0]
                   for i in range(k)]).astype(np.float64)
     ma, mb = a.mean(axis=(1, 2, 3)), b.mean(axis=(1, 2, 3))
@@ -35,17 +37,19 @@ def test_uncached_nrc_render_equals_plain_tracer(ctx):
     ctx.release(slot)
 
 
-def test_cache_training_lowers_loss_and_renders(ctx):
+@pytest.mark.parametrize("engine", [tpt.ENGINE_WAVEFRONT, tpt.ENGINE_PERSISTENT], ids=["wavefront", "persistent"])
+def test_cache_training_lowers_loss_and_renders(ctx, engine):
     slot = _slot(ctx)
-    _, _, n1 = tpt.render_nrc(ctx, slot, 64, 64, 16, passes=2, train_steps=1, batch=8192, seed=3)
-    img, st, n2 = tpt.render_nrc(ctx, slot, 64, 64, 16, passes=2, train_steps=300, batch=8192, seed=3)
+    _, _, n1 = tpt.render_nrc(ctx, slot, 64, 64, 16, passes=2, train_steps=1, batch=8192, seed=3, engine=engine)
+    img, st, n2 = tpt.render_nrc(ctx, slot, 64, 64, 16, passes=2, train_steps=300, batch=8192, seed=3,
+                                 engine=engine)
     assert n1["records"] > 1000 and n2["queries"] > 0
     assert n2["final_loss"] < n1["final_loss"], (n1, n2)
     assert np.isfinite(img).all() and img.mean() > 0
     ctx.release(slot)
 
 
-def test_cached_render_error_is_bounded(ctx):
+def test_cached_render_gains_at_equal_spp(ctx):
     slot = _slot(ctx)
     w = h = 48
     ref, _ = ctx.render(slot, w, h, 4096, semantics=tpt.SEMANTICS_PHYSICAL, seed=999, fp64=True)
@@ -53,5 +57,6 @@ def test_cached_render_error_is_bounded(ctx):
     cached, st, ns = tpt.render_nrc(ctx, slot, w, h, 64, passes=4, train_steps=64, seed=5)
     r = relmse(cached, ref)
     print("relMSE plain", plain, "nrc", r, ns)
-    assert r < 5 * plain + 0.05
+    # what the trained cache gains: lower error than the plain tracer at equal spp
+    assert r < plain
     ctx.release(slot)

@@ -1,8 +1,8 @@
 """The SAH topology option (TPT_BVH_SAH): the closest hit of every ray is the
 reference's (checked against the CPU oracle, which builds the reference's
-own tree) except where several primitives tie at exactly equal t - the one
-scene built from coincident primitives ("ties") is left out - and renders
-agree statistically with the reference topology's."""
+own tree) except which primitive wins where several report exactly the same
+t - the scene built from coincident primitives ("ties") is left out - and
+renders agree with the reference topology's."""
 import numpy as np
 import pytest
 
@@ -27,9 +27,15 @@ def test_sah_closest_hits_match_oracle(ctx, name, flat):
     ctx.set_flat_nodes(48)
     ctx.release(slot)
     # media draw their free flight from (ray, medium id): independent of the visit order
-    assert np.array_equal(i, oi), f"{(i != oi).any(axis=1).sum()} rays differ"
+    assert np.array_equal(i[:, 0], oi[:, 0]), "hit / miss differs"
     hit = oi[:, 0] == 1
     np.testing.assert_allclose(f[hit, 0], of[hit, 0], rtol=1e-5, atol=1e-6)
+    # a different primitive only where two primitives report the very same t
+    # (boxes standing on the floor, adjacent ground boxes sharing a face):
+    # which one wins such a tie is a property of the tree
+    differ = hit & (i[:, 1] != oi[:, 1])
+    assert (f[differ, 0] == of[differ, 0]).all(), "a primitive differs without a tie in t"
+    assert differ.mean() < 1e-2, differ.sum()
 
 
 def test_sah_render_matches_reference_topology(ctx):

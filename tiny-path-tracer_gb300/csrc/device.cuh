@@ -145,9 +145,12 @@ __device__ __forceinline__ RayPre precompute(const Ray &r) {
 // (disc = b*b - 4ac cancels near tangency), so a hit can lie outside the
 // primitive's box.  The bound subtracts 2^-8 (entry + box diagonal / |d|),
 // four times that error, plus a term for rounding of a transformed origin.
+__device__ __forceinline__ float prune_key_ext(const RayPre &r, float ext, float entry) {
+  return entry * 0.99609375f - ext * 0.00390625f * r.inv_len - r.slack;
+}
 __device__ __forceinline__ float prune_key(const RayPre &r, const f4 &lo, const f4 &hi, float entry) {
   const float ext = (hi.x - lo.x) + (hi.y - lo.y) + (hi.z - lo.z);  // >= box diagonal
-  return entry * 0.99609375f - ext * 0.00390625f * r.inv_len - r.slack;
+  return prune_key_ext(r, ext, entry);
 }
 
 // AABB::hit (aabb.cc:3-19) evaluated without the early exit: the interval
@@ -479,7 +482,7 @@ __device__ bool trace_closest(const DevScene &S, const Ray &wr, float tmin, int2
             const f4 clo = c == 0 ? k0 : k2, chi = c == 0 ? k1 : k3;
             if (slab(curp, clo, chi, tmin, tmax, en)) {
               ent[nq] = en;
-              q[nq++] = make_int2(ref, __float_as_int(prune_key(curp, clo, chi, en)));
+              q[nq++] = make_int2(ref, __float_as_int(prune_key_ext(curp, chi.w, en)));  // chi.w: box size term
             }
           } else {
             push(-2 - ~ref, never_pruned);
@@ -658,7 +661,17 @@ __device__ __noinline__ float perlin_turb(const DevScene &S, float3 p) {  // uti
 }
 
 // texture::value (texture.h:15-51, texture.cc:4-42)
-__device__ float3 tex_value(const DevScene &S, int t, float u, float v, float3 p) {
+__device__ __noinline__ float3 tex_value_any(const DevScene &S, int t, float u, float v, float3 p);
+
+// Constant textures inline (the common case); the others in one out-of-line
+// copy shared by every call site.
+__device__ __forceinline__ float3 tex_value(const DevScene &S, int t, float u, float v, float3 p) {
+  const i4 ti = ldg4(S.tex_i + t);
+  if (ti.x == TT_CONST) return f3(ldg4(S.tex_f + t));
+  return tex_value_any(S, t, u, v, p);
+}
+
+__device__ __noinline__ float3 tex_value_any(const DevScene &S, int t, float u, float v, float3 p) {
   for (int guard = 0; guard < 16; guard++) {
     const i4 ti = ldg4(S.tex_i + t);
     if (ti.x == TT_CONST) return f3(ldg4(S.tex_f + t));
@@ -880,6 +893,7 @@ struct RenderCfg {
   int background;  // 0 black, 1 sky
   float sky_scale;
   uint2 key;
+  int refill;      // persistent engines: idle lanes per warp that trigger new camera samples
 };
 
 __device__ __forceinline__ float3 background(const RenderCfg &cfg, const Ray &r) {  // utils.cc:85-90

@@ -45,6 +45,7 @@ struct PathBuf {
   float4 *d_depth;  // direction, bounce depth (int bits)
   float4 *thr_pix;  // throughput, pixel (int bits)
   float4 *rad_smp;  // radiance so far, sample index (int bits)
+  int4 *aux;        // learned renders: training-record slots of the path (else unused)
 };
 
 __device__ __forceinline__ void warp_claim(bool want, unsigned long long *counter, unsigned long long &base,
@@ -56,6 +57,15 @@ __device__ __forceinline__ void warp_claim(bool want, unsigned long long *counte
   const int leader = mask ? __ffs(mask) - 1 : 0;
   if (want && lane == leader) b = atomicAdd(counter, (unsigned long long)__popc(mask));
   base = __shfl_sync(0xffffffffu, b, leader);
+}
+
+// Whether the warp's idle lanes take new camera samples now: when at least
+// `refill` of them are idle (1: at once, each lane on its own; 32: only when
+// the whole warp is idle, so a warp's paths stay at the same depth over
+// neighbouring pixels, as in a wavefront), or when no lane is left tracing.
+__device__ __forceinline__ bool refill_now(bool want, bool alive, int refill) {
+  const unsigned m = __ballot_sync(0xffffffffu, want);
+  return m && ((int)__popc(m) >= refill || !__any_sync(0xffffffffu, alive));
 }
 
 __device__ __forceinline__ unsigned warp_append(bool want, unsigned int *counter) {
@@ -233,6 +243,208 @@ __global__ void k_wf_shade(DevScene S, RenderCfg cfg, FrameDesc F, PathBuf in, P
   }
 }
 
+// Learned renders on the wavefront engine: the per-pass sample mapping, the
+// training-record buffers and the cache queries (one struct for both modes).
+struct WfLearn {
+  GuideView gv;                       // guided: lobe table (lobes == nullptr: plain mixture)
+  unsigned long long sample_offset;   // claimed index s -> sample_coords(F, s + sample_offset)
+  uint32_t sample_add;                // added to the sample number (guided passes)
+  uint32_t stride;                    // guided: every stride-th sample records; cache: trains
+  float4 *records;                    // guided: 3 float4 per record (ring); cache: 5 float4 (capped)
+  unsigned *rec_count;
+  unsigned rec_cap;
+  float4 *pend;                       // guided: 5 float4 per recording path; cache: T_k, L_k per record
+  unsigned *pend_count;
+  int term_depth;                     // cache
+  float4 *queries;                    // cache: 6 float4 per query
+  unsigned *q_count;
+  unsigned q_cap;
+};
+
+__device__ __forceinline__ bool wf_training(const FrameDesc &F, const WfLearn &W, uint32_t pixel, uint32_t sample) {
+  const unsigned long long npix = (unsigned long long)F.nx * F.ny;
+  return ((unsigned long long)(sample - W.sample_add) * npix + pixel) % W.stride == 0;
+}
+
+// Fills slots [0, count) with camera samples first..first+count of a learned pass.
+__global__ void k_wf_generate_learn(DevScene S, FrameDesc F, PathBuf out, unsigned count, uint2 key, WfLearn W) {
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+    uint32_t pixel, sample;
+    int i, j;
+    sample_coords(F, k + W.sample_offset, pixel, sample, i, j);
+    sample += W.sample_add;
+    const Ray r = camera_ray(S.cam, i, j, F.nx, F.ny, pixel, sample, key);
+    write_path(out, k, r, 0, v3(1.f, 1.f, 1.f), v3(0.f, 0.f, 0.f), pixel, sample);
+    out.aux[k] = make_int4(-1, -1, -1, 0);
+  }
+}
+
+// k_wf_shade for the learned renders.  MODE 1: path guiding (guided sampling
+// at diffuse vertices; a recording path keeps its first diffuse vertex in
+// `pend` and emits the finished record when it ends).  MODE 2: radiance
+// cache (paths end at the first diffuse vertex past term_depth and leave a
+// query; training paths record their first three diffuse vertices and fill
+// in the targets when they end).  Same per-vertex arithmetic as the
+// persistent engines (shade_vertex_t).
+template <int MODE>
+__global__ void k_wf_shade_learn(DevScene S, RenderCfg cfg, FrameDesc F, PathBuf in, PathBuf out, int cur,
+                                 WfCounters *C, const int4 *__restrict__ hits, WfLearn W) {
+  const unsigned n = C->count[cur];
+  const unsigned stride = gridDim.x * blockDim.x;
+  const unsigned n_round = (n + 31u) & ~31u;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n_round; k += stride) {
+    const bool live = k < n;
+    bool cont = false;
+    Ray r{};
+    int depth = 0;
+    float3 T = v3(0.f, 0.f, 0.f), L = v3(0.f, 0.f, 0.f);
+    uint32_t pixel = 0, sample = 0;
+    int4 aux = make_int4(-1, -1, -1, 0);
+    bool new_rec = false, want_q = false, want_r = false;
+    GuideRec grec{};
+    VertexInfo vi{};
+    float3 Tb = T, Lb = L;
+    if (live) {
+      const float4 ot = in.o_time[k], dd = in.d_depth[k];
+      const float4 tp = in.thr_pix[k], rs = in.rad_smp[k];
+      r = Ray{v3(ot.x, ot.y, ot.z), v3(dd.x, dd.y, dd.z), ot.w};
+      depth = __float_as_int(dd.w);
+      T = v3(tp.x, tp.y, tp.z);
+      L = v3(rs.x, rs.y, rs.z);
+      pixel = (uint32_t)__float_as_int(tp.w);
+      sample = (uint32_t)__float_as_int(rs.w);
+      aux = in.aux[k];
+      Tb = T;
+      Lb = L;
+      const int4 hv = hits[k];
+      const HitRef h{__int_as_float(hv.x), hv.y, hv.z, hv.w};
+      const bool training = wf_training(F, W, pixel, sample);
+      if (MODE == 1) {
+        grec.valid = aux.x >= 0 || !training;  // only recording paths without a record yet take one
+        const bool had = grec.valid;
+        cont = shade_vertex_t<true>(S, cfg, r, hv.y >= 0, h, T, L, depth, pixel, sample, W.gv, grec);
+        new_rec = !had && grec.valid && finite3(grec.x) && finite3(grec.n) && finite3(grec.d);
+      } else {
+        const bool may_query = !training && depth >= W.term_depth;
+        const bool rec_here = training && hv.y >= 0 && aux.w < 3;
+        bool queried = false;
+        cont = shade_vertex_t<false>(S, cfg, r, hv.y >= 0, h, T, L, depth, pixel, sample, W.gv, grec,
+                                     (rec_here || may_query) ? &vi : nullptr, may_query ? W.term_depth : (1 << 30),
+                                     &queried);
+        want_q = queried;
+        want_r = !queried && rec_here && (vi.kind == MT_LAMBERTIAN || vi.kind == MT_ISOTROPIC);
+      }
+      if (cont) depth++;
+    }
+    // warp-wide appends (every lane takes part in the ballots)
+    if (MODE == 1) {
+      const unsigned ps = warp_append(new_rec, W.pend_count);
+      if (new_rec && ps < W.rec_cap) {
+        float4 *q = W.pend + 5 * (size_t)ps;
+        q[0] = make_float4(grec.x.x, grec.x.y, grec.x.z, 0.f);
+        q[1] = make_float4(grec.n.x, grec.n.y, grec.n.z, 0.f);
+        q[2] = make_float4(grec.d.x, grec.d.y, grec.d.z, 0.f);
+        q[3] = make_float4(grec.T.x, grec.T.y, grec.T.z, 0.f);
+        q[4] = make_float4(grec.L.x, grec.L.y, grec.L.z, 0.f);
+        aux.x = (int)ps;
+      }
+    } else {
+      const unsigned qs = warp_append(want_q, W.q_count);
+      if (want_q && qs < W.q_cap) {
+        float4 *q = W.queries + 6 * (size_t)qs;
+        q[0] = make_float4(vi.p.x, vi.p.y, vi.p.z, vi.rough);
+        q[1] = make_float4(vi.wo.x, vi.wo.y, vi.wo.z, 0.f);
+        q[2] = make_float4(vi.n.x, vi.n.y, vi.n.z, 0.f);
+        q[3] = make_float4(vi.albedo.x, vi.albedo.y, vi.albedo.z, 0.f);
+        q[4] = make_float4(Tb.x, Tb.y, Tb.z, __int_as_float((int)pixel));
+      }
+      const unsigned rs = warp_append(want_r, W.rec_count);
+      if (want_r) {
+        if (rs < W.rec_cap) {
+          float4 *q = W.records + 5 * (size_t)rs;
+          q[0] = make_float4(vi.p.x, vi.p.y, vi.p.z, vi.rough);
+          q[1] = make_float4(vi.wo.x, vi.wo.y, vi.wo.z, 0.f);
+          q[2] = make_float4(vi.n.x, vi.n.y, vi.n.z, 0.f);
+          q[3] = make_float4(vi.albedo.x, vi.albedo.y, vi.albedo.z, 0.f);
+          q[4] = make_float4(0.f, 0.f, 0.f, 0.f);
+          W.pend[2 * (size_t)rs] = make_float4(Tb.x, Tb.y, Tb.z, 0.f);
+          W.pend[2 * (size_t)rs + 1] = make_float4(Lb.x, Lb.y, Lb.z, 0.f);
+        }
+        const int slot = rs < W.rec_cap ? (int)rs : -1;
+        if (aux.w == 0) aux.x = slot;
+        else if (aux.w == 1) aux.y = slot;
+        else aux.z = slot;
+        aux.w++;
+      }
+    }
+    // finished paths: accumulate, complete their records
+    const bool ended = live && !cont;
+    bool emit_rec = false;
+    float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0;
+    if (ended) {
+      accumulate(F, pixel, L);
+      const float3 Lf = de_nan(L);
+      if (MODE == 1 && aux.x >= 0 && aux.x < (int)W.rec_cap) {
+        const float4 *q = W.pend + 5 * (size_t)aux.x;
+        const float4 qT = q[3], qL = q[4];
+        const float3 c = v3((L.x - qL.x) / qT.x, (L.y - qL.y) / qT.y, (L.z - qL.z) / qT.z);
+        float wgt = (c.x + c.y + c.z) * (1.f / 3.f);
+        if (!(wgt >= 0.f) || !(wgt < 1e6f)) wgt = 0.f;
+        const float4 x = q[0];
+        r0 = make_float4(x.x, x.y, x.z, wgt);
+        r1 = q[1];
+        r2 = q[2];
+        emit_rec = true;
+      }
+      if (MODE == 2) {
+        const int slots[3] = {aux.x, aux.y, aux.z};
+        for (int j = 0; j < aux.w && j < 3; j++) {
+          const int sl = slots[j];
+          if (sl < 0) continue;
+          const float4 pT = W.pend[2 * (size_t)sl], pL = W.pend[2 * (size_t)sl + 1];
+          float3 tg = v3((Lf.x - pL.x) / pT.x, (Lf.y - pL.y) / pT.y, (Lf.z - pL.z) / pT.z);
+          tg = v3(isfinite(tg.x) ? fmaxf(tg.x, 0.f) : 0.f, isfinite(tg.y) ? fmaxf(tg.y, 0.f) : 0.f,
+                  isfinite(tg.z) ? fmaxf(tg.z, 0.f) : 0.f);
+          W.records[5 * (size_t)sl + 4] = make_float4(tg.x, tg.y, tg.z, 1.f);
+        }
+      }
+    }
+    if (MODE == 1) {
+      const unsigned rs = warp_append(emit_rec, W.rec_count) % W.rec_cap;  // ring: the newest records win
+      if (emit_rec) {
+        W.records[3 * (size_t)rs] = r0;
+        W.records[3 * (size_t)rs + 1] = r1;
+        W.records[3 * (size_t)rs + 2] = r2;
+      }
+    }
+    // regenerate finished paths from the global sample counter
+    unsigned long long base;
+    int rank;
+    warp_claim(ended, &C->issued, base, rank);
+    bool fresh = false;
+    if (ended) {
+      const unsigned long long s = base + (unsigned long long)rank;
+      if (s < F.total) {
+        int i, j;
+        sample_coords(F, s + W.sample_offset, pixel, sample, i, j);
+        sample += W.sample_add;
+        r = camera_ray(S.cam, i, j, F.nx, F.ny, pixel, sample, cfg.key);
+        depth = 0;
+        T = v3(1.f, 1.f, 1.f);
+        L = v3(0.f, 0.f, 0.f);
+        aux = make_int4(-1, -1, -1, 0);
+        fresh = true;
+      }
+    }
+    const bool emit = cont || fresh;
+    const unsigned slot = warp_append(emit, &C->count[cur ^ 1]);
+    if (emit) {
+      write_path(out, slot, r, depth, T, L, pixel, sample);
+      out.aux[slot] = aux;
+    }
+  }
+}
+
 // Persistent engine: every lane carries one path in registers; when its
 // path ends it accumulates and claims the next camera sample (one atomic per
 // warp for all lanes that need one), so lanes do not idle behind the longest
@@ -250,7 +462,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS) k_persistent(DevScene S, Rend
   int depth = 0;
   for (;;) {
     const bool want = !alive && !done;
-    if (__any_sync(0xffffffffu, want)) {
+    if (refill_now(want, alive, cfg.refill)) {
       unsigned long long base;
       int rank;
       warp_claim(want, &C->issued, base, rank);
@@ -315,7 +527,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
   int depth = 0, item = 0;
   for (;;) {
     const bool want = !alive && !done;
-    if (__any_sync(0xffffffffu, want)) {
+    if (refill_now(want, alive, cfg.refill)) {
       unsigned long long base;
       int rank;
       warp_claim(want, &C->issued, base, rank);
@@ -379,7 +591,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
   bool want_rec = false;
   for (;;) {
     const bool want = !alive && !done;
-    if (__any_sync(0xffffffffu, want)) {
+    if (refill_now(want, alive, cfg.refill)) {
       unsigned long long base;
       int rank;
       warp_claim(want, &C->issued, base, rank);
@@ -463,7 +675,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
   GuideRec grec{};
   for (;;) {
     const bool want = !alive && !done;
-    if (__any_sync(0xffffffffu, want)) {
+    if (refill_now(want, alive, cfg.refill)) {
       unsigned long long base;
       int rank;
       warp_claim(want, &C->issued, base, rank);
@@ -617,7 +829,8 @@ struct tpt_context {
   cudaStream_t own = nullptr;
   int sm_count = 0;
   std::vector<Slot> slots;
-  DevBuf path[2], hits, accum, accum64, staging, rays, hitf, hiti;
+  DevBuf path[2], path_aux[2], hits, accum, accum64, staging, rays, hitf, hiti;
+  DevBuf learn_pend;  // wavefront learned renders: pending record state
   DevBuf batch_table, batch_accum, batch_staging;
   DevBuf guide_table, guide_records, guide_count;
   long long guide_last_count = 0;  // records of the last guided pass
@@ -717,7 +930,7 @@ void tpt_context_destroy(tpt_context *c) {
     if (b->p) cudaFree(b->p);
   if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
   DevBuf *gb[] = {&c->guide_table, &c->guide_records, &c->guide_count, &c->nrc_records, &c->nrc_queries,
-                  &c->nrc_counts};
+                  &c->nrc_counts, &c->path_aux[0], &c->path_aux[1], &c->learn_pend};
   for (DevBuf *b : gb)
     if (b->p) cudaFree(b->p);
   guide_destroy(c->guide);
@@ -887,19 +1100,27 @@ void tpt_render_params_default(tpt_render_params *p) {
 
 }  // extern "C"
 
-static PathBuf path_view(DevBuf &b, size_t wave) {
+static PathBuf path_view(DevBuf &b, size_t wave, DevBuf *aux = nullptr) {
   float4 *base = (float4 *)b.p;
-  return PathBuf{base, base + wave, base + 2 * wave, base + 3 * wave};
+  return PathBuf{base, base + wave, base + 2 * wave, base + 3 * wave, aux ? (int4 *)aux->p : nullptr};
 }
 
-// Wavefront render; returns after all samples are accumulated.
-static tpt_status run_wavefront(tpt_context *c, const DevScene &S, const RenderCfg &cfg, const FrameDesc &F, int block,
-                                size_t wave, bool profile, tpt_render_stats *stats) {
+// Wavefront render; returns after all samples are accumulated.  MODE 0: the
+// plain tracer; 1 / 2: a pass of the guided / cached renderer (W).
+template <int MODE>
+static tpt_status run_wavefront_t(tpt_context *c, const DevScene &S, const RenderCfg &cfg, const FrameDesc &F,
+                                  int block, size_t wave, bool profile, tpt_render_stats *stats,
+                                  const WfLearn *W = nullptr) {
   tpt_status st;
   if ((st = ensure(c->path[0], wave * 4 * sizeof(float4))) != TPT_OK) return st;
   if ((st = ensure(c->path[1], wave * 4 * sizeof(float4))) != TPT_OK) return st;
   if ((st = ensure(c->hits, wave * sizeof(int4))) != TPT_OK) return st;
-  PathBuf P[2] = {path_view(c->path[0], wave), path_view(c->path[1], wave)};
+  if (MODE > 0) {
+    if ((st = ensure(c->path_aux[0], wave * sizeof(int4))) != TPT_OK) return st;
+    if ((st = ensure(c->path_aux[1], wave * sizeof(int4))) != TPT_OK) return st;
+  }
+  PathBuf P[2] = {path_view(c->path[0], wave, MODE > 0 ? &c->path_aux[0] : nullptr),
+                  path_view(c->path[1], wave, MODE > 0 ? &c->path_aux[1] : nullptr)};
   const unsigned first = (unsigned)std::min<unsigned long long>(wave, F.total);
   WfCounters init{};
   init.count[0] = first;
@@ -909,11 +1130,14 @@ static tpt_status run_wavefront(tpt_context *c, const DevScene &S, const RenderC
   const int smem = stack_smem(block);
   TPT_CUDA(smem_optin(k_wf_traverse, smem));
   const int g_gen = std::max(1, std::min<int>((int)((first + block - 1) / block), c->sm_count * 8));
-  k_wf_generate<<<g_gen, block, 0, c->stream>>>(S, F, P[0], 0ull, first, cfg.key);
+  if constexpr (MODE == 0)
+    k_wf_generate<<<g_gen, block, 0, c->stream>>>(S, F, P[0], 0ull, first, cfg.key);
+  else
+    k_wf_generate_learn<<<g_gen, block, 0, c->stream>>>(S, F, P[0], first, cfg.key, *W);
   TPT_CUDA(cudaGetLastError());
   int launches = 1;
   const int g_tr = grid_for(c, k_wf_traverse, block, smem);
-  const int g_sh = grid_for(c, k_wf_shade, block, 0);
+  const int g_sh = MODE == 0 ? grid_for(c, k_wf_shade, block, 0) : grid_for(c, k_wf_shade_learn<MODE == 0 ? 1 : MODE>, block, 0);
   // iteration bound: every sample lives at most max_depth+1 segments
   const unsigned long long max_iters = (F.total * (unsigned long long)(cfg.max_depth + 1)) / wave + 64;
   // capture an even number of iterations (buffer parity returns) as a graph;
@@ -931,8 +1155,12 @@ static tpt_status run_wavefront(tpt_context *c, const DevScene &S, const RenderC
     if (profile) cudaEventRecordWithFlags(c->prof_ev[3 * it], c->stream, cudaEventRecordExternal);
     k_wf_traverse<<<g_tr, block, smem, c->stream>>>(S, P[cur], cur, c->counters, (int4 *)c->hits.p, cfg.key);
     if (profile) cudaEventRecordWithFlags(c->prof_ev[3 * it + 1], c->stream, cudaEventRecordExternal);
-    k_wf_shade<<<g_sh, block, 0, c->stream>>>(S, cfg, F, P[cur], P[cur ^ 1], cur, c->counters,
-                                              (const int4 *)c->hits.p);
+    if constexpr (MODE == 0)
+      k_wf_shade<<<g_sh, block, 0, c->stream>>>(S, cfg, F, P[cur], P[cur ^ 1], cur, c->counters,
+                                                (const int4 *)c->hits.p);
+    else
+      k_wf_shade_learn<MODE><<<g_sh, block, 0, c->stream>>>(S, cfg, F, P[cur], P[cur ^ 1], cur, c->counters,
+                                                            (const int4 *)c->hits.p, *W);
     if (profile) cudaEventRecordWithFlags(c->prof_ev[3 * it + 2], c->stream, cudaEventRecordExternal);
   }
   cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
@@ -972,6 +1200,11 @@ static tpt_status run_wavefront(tpt_context *c, const DevScene &S, const RenderC
     stats->segments = (int64_t)c->counters_host->segments;
   }
   return result;
+}
+
+static tpt_status run_wavefront(tpt_context *c, const DevScene &S, const RenderCfg &cfg, const FrameDesc &F, int block,
+                                size_t wave, bool profile, tpt_render_stats *stats) {
+  return run_wavefront_t<0>(c, S, cfg, F, block, wave, profile, stats);
 }
 
 // Register-capped variants of the persistent kernel (occupancy vs spills),
@@ -1039,7 +1272,7 @@ extern "C" tpt_status tpt_render(tpt_context *c, int32_t slot, const tpt_render_
   FrameDesc F{p->width, p->height, p->spp, total, (float4 *)c->accum.p,
               p->accumulate_fp64 ? (double *)c->accum64.p : nullptr};
   RenderCfg cfg{p->max_depth, p->semantics, p->background, p->sky_scale,
-                make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32))};
+                make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32)), p->refill > 0 ? p->refill : 1};
   tpt_render_params tuned;
   if (p->engine == TPT_ENGINE_AUTO && c->slots[slot].tuned) {
     tuned = *p;
@@ -1130,7 +1363,7 @@ extern "C" tpt_status tpt_render_snapshots(tpt_context *c, int32_t slot, const t
   DevScene S = sl.ds;
   S.flat_max = p->flat_nodes > 0 ? p->flat_nodes : (sl.tuned ? sl.tp.flat_nodes : c->flat_nodes);
   const RenderCfg cfg{p->max_depth, p->semantics, p->background, p->sky_scale,
-                      make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32))};
+                      make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32)), p->refill > 0 ? p->refill : 1};
   TPT_CUDA(cudaMemsetAsync(c->accum.p, 0, npix * sizeof(float4), c->stream));
   if (p->accumulate_fp64) TPT_CUDA(cudaMemsetAsync(c->accum64.p, 0, npix * 3 * sizeof(double), c->stream));
   const int slice = bonus_pic > 0 ? p->spp / bonus_pic : p->spp;
@@ -1203,7 +1436,7 @@ extern "C" tpt_status tpt_render_batch(tpt_context *c, const tpt_batch_item *ite
                                acc + pix_off[k], nullptr};
   }
   const RenderCfg cfg{p->max_depth, p->semantics, p->background, p->sky_scale,
-                      make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32))};
+                      make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32)), p->refill > 0 ? p->refill : 1};
   uint64_t key = 1469598103934665603ull;
   key = fnv1a(key, table.data(), table.size() * sizeof(BatchItem));
   key = fnv1a(key, &cfg, sizeof(cfg));
@@ -1333,6 +1566,20 @@ extern "C" void tpt_guide_params_default(tpt_guide_params *g) {
   g->seed = 1;
 }
 
+// Engine of a learned render: as asked, else the slot's tuned one, else the
+// wavefront engine (faster than the persistent one in physical semantics on
+// the measured scenes: Cornell with the small light 684 vs 570, next week
+// 159 vs 98 Msamples/s).
+static int learned_engine(const tpt_render_params *p, const Slot &sl) {
+  if (p->engine == TPT_ENGINE_WAVEFRONT || p->engine == TPT_ENGINE_PERSISTENT) return p->engine;
+  return sl.tuned ? sl.tp.engine : TPT_ENGINE_WAVEFRONT;
+}
+static size_t wf_wave(const tpt_render_params *p, const Slot &sl) {
+  if (p->wave > 0) return (size_t)p->wave;
+  if (sl.tuned && sl.tp.engine == TPT_ENGINE_WAVEFRONT && sl.tp.wave > 0) return (size_t)sl.tp.wave;
+  return (size_t)1 << 20;
+}
+
 extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_render_params *p,
                                         const tpt_guide_params *g, float *out_rgb, int32_t mem,
                                         tpt_render_stats *stats, tpt_guide_stats *gstats) {
@@ -1357,7 +1604,7 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
   const size_t table_f4 = (size_t)g->grid_res * g->grid_res * g->grid_res * 6 * GUIDE_ENTRY;
   if ((st = ensure(c->guide_table, table_f4 * sizeof(float4))) != TPT_OK) return st;
   if ((st = ensure(c->guide_records, (size_t)g->record_cap * 3 * sizeof(float4))) != TPT_OK) return st;
-  if ((st = ensure(c->guide_count, sizeof(unsigned))) != TPT_OK) return st;
+  if ((st = ensure(c->guide_count, 2 * sizeof(unsigned))) != TPT_OK) return st;  // [0] records, [1] pending
   if ((st = ensure(c->accum, npix * sizeof(float4))) != TPT_OK) return st;
   const float3 lo = make_float3(sl.world_lo[0], sl.world_lo[1], sl.world_lo[2]);
   const float3 ext = make_float3(fmaxf(sl.world_hi[0] - sl.world_lo[0], 1e-6f),
@@ -1366,12 +1613,20 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
   DevScene S = sl.ds;
   S.flat_max = p->flat_nodes > 0 ? p->flat_nodes : c->flat_nodes;
   const RenderCfg cfg{p->max_depth, p->semantics, p->background, p->sky_scale,
-                      make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32))};
+                      make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32)), p->refill > 0 ? p->refill : 1};
   FrameDesc F{p->width, p->height, spp_pass, npix * (unsigned long long)spp_pass, (float4 *)c->accum.p, nullptr};
-  const int block = 128, smem = stack_smem(block);
+  // engine: as asked, else the slot's tuned one, else the wavefront (faster in
+  // physical semantics on the measured scenes)
+  const int engine = learned_engine(p, sl);
+  const bool wf = engine == TPT_ENGINE_WAVEFRONT;
+  const int block = wf ? (p->block > 0 ? p->block : (sl.tuned && sl.tp.engine == TPT_ENGINE_WAVEFRONT ? sl.tp.block : 128))
+                       : 128;
+  const size_t wave = wf_wave(p, sl);
+  const int smem = stack_smem(block);
   auto kern = k_persistent_guided<4>;
   TPT_CUDA(smem_optin(kern, smem));
-  const int grid = grid_for(c, kern, block, smem);
+  const int grid = grid_for(c, kern, 128, stack_smem(128));
+  if (wf && ((st = ensure(c->learn_pend, (size_t)g->record_cap * 5 * sizeof(float4))) != TPT_OK)) return st;
   const unsigned long long per_pass = F.total;
   const uint32_t stride = (uint32_t)std::max<unsigned long long>(1ull, per_pass / (unsigned long long)g->record_cap);
   cudaEvent_t e[4];
@@ -1387,13 +1642,29 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
   for (int pass = 0; pass < g->passes && result == TPT_OK; pass++) {
     GuideView gv{have_table ? (const float4 *)c->guide_table.p : nullptr, lo,
                  make_float3(1.f / ext.x, 1.f / ext.y, 1.f / ext.z), g->grid_res, g->alpha};
-    WfCounters init{};
-    std::memcpy(c->counters_host, &init, sizeof(init));
-    cudaMemcpyAsync(c->counters, c->counters_host, sizeof(WfCounters), cudaMemcpyHostToDevice, c->stream);
     cudaEventRecord(e[0], c->stream);
-    kern<<<grid, block, smem, c->stream>>>(S, cfg, F, c->counters, gv, (uint32_t)(pass * spp_pass),
-                                          (float4 *)c->guide_records.p, (unsigned *)c->guide_count.p,
-                                          (unsigned)g->record_cap, stride);
+    if (wf) {
+      WfLearn W{};
+      W.gv = gv;
+      W.sample_add = (uint32_t)(pass * spp_pass);
+      W.stride = stride;
+      W.records = (float4 *)c->guide_records.p;
+      W.rec_count = (unsigned *)c->guide_count.p;
+      W.rec_cap = (unsigned)g->record_cap;
+      W.pend = (float4 *)c->learn_pend.p;
+      W.pend_count = (unsigned *)c->guide_count.p + 1;
+      cudaMemsetAsync(W.pend_count, 0, sizeof(unsigned), c->stream);
+      tpt_render_stats part{};
+      result = run_wavefront_t<1>(c, S, cfg, F, block, wave, false, &part, &W);
+      if (result != TPT_OK) break;
+    } else {
+      WfCounters init{};
+      std::memcpy(c->counters_host, &init, sizeof(init));
+      cudaMemcpyAsync(c->counters, c->counters_host, sizeof(WfCounters), cudaMemcpyHostToDevice, c->stream);
+      kern<<<grid, 128, stack_smem(128), c->stream>>>(S, cfg, F, c->counters, gv, (uint32_t)(pass * spp_pass),
+                                                     (float4 *)c->guide_records.p, (unsigned *)c->guide_count.p,
+                                                     (unsigned)g->record_cap, stride);
+    }
     cudaEventRecord(e[1], c->stream);
     unsigned count = 0;
     cudaMemcpyAsync(&count, c->guide_count.p, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
@@ -1515,11 +1786,17 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
   DevScene S = sl.ds;
   S.flat_max = p->flat_nodes > 0 ? p->flat_nodes : c->flat_nodes;
   const RenderCfg cfg{p->max_depth, p->semantics, p->background, p->sky_scale,
-                      make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32))};
+                      make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32)), p->refill > 0 ? p->refill : 1};
+  const int engine = learned_engine(p, sl);
+  const bool wf = engine == TPT_ENGINE_WAVEFRONT;
+  const int wf_block =
+      p->block > 0 ? p->block : (sl.tuned && sl.tp.engine == TPT_ENGINE_WAVEFRONT ? sl.tp.block : 128);
+  const size_t wave = wf_wave(p, sl);
   const int block = 128, smem = stack_smem(block);
   auto kern = k_persistent_nrc<4>;
   TPT_CUDA(smem_optin(kern, smem));
   const int grid = grid_for(c, kern, block, smem);
+  if (wf && ((st = ensure(c->learn_pend, (size_t)n->record_cap * 2 * sizeof(float4))) != TPT_OK)) return st;
   unsigned *counts = (unsigned *)c->nrc_counts.p;  // [0] records, [1] queries
   cudaEvent_t ev[6];
   for (auto &x : ev) TPT_CUDA(cudaEventCreate(&x));
@@ -1539,15 +1816,32 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
       const unsigned long long cnt = std::min(chunk, pass_total - off);
       FrameDesc Fc = F;
       Fc.total = cnt;
-      WfCounters init{};
-      std::memcpy(c->counters_host, &init, sizeof(init));
-      cudaMemcpyAsync(c->counters, c->counters_host, sizeof(WfCounters), cudaMemcpyHostToDevice, c->stream);
       cudaMemsetAsync(counts + 1, 0, sizeof(unsigned), c->stream);
       cudaEventRecord(ev[0], c->stream);
-      kern<<<grid, block, smem, c->stream>>>(S, cfg, Fc, c->counters, pass_begin + off, term,
-                                            (uint32_t)n->train_stride, (float4 *)c->nrc_records.p, counts,
-                                            (unsigned)n->record_cap, (float4 *)c->nrc_queries.p, counts + 1,
-                                            (unsigned)n->query_cap);
+      if (wf) {
+        WfLearn W{};
+        W.sample_offset = pass_begin + off;
+        W.stride = (uint32_t)n->train_stride;
+        W.records = (float4 *)c->nrc_records.p;
+        W.rec_count = counts;
+        W.rec_cap = (unsigned)n->record_cap;
+        W.pend = (float4 *)c->learn_pend.p;
+        W.term_depth = term;
+        W.queries = (float4 *)c->nrc_queries.p;
+        W.q_count = counts + 1;
+        W.q_cap = (unsigned)n->query_cap;
+        tpt_render_stats part{};
+        result = run_wavefront_t<2>(c, S, cfg, Fc, wf_block, wave, false, &part, &W);
+        if (result != TPT_OK) break;
+      } else {
+        WfCounters init{};
+        std::memcpy(c->counters_host, &init, sizeof(init));
+        cudaMemcpyAsync(c->counters, c->counters_host, sizeof(WfCounters), cudaMemcpyHostToDevice, c->stream);
+        kern<<<grid, block, smem, c->stream>>>(S, cfg, Fc, c->counters, pass_begin + off, term,
+                                              (uint32_t)n->train_stride, (float4 *)c->nrc_records.p, counts,
+                                              (unsigned)n->record_cap, (float4 *)c->nrc_queries.p, counts + 1,
+                                              (unsigned)n->query_cap);
+      }
       cudaEventRecord(ev[1], c->stream);
       unsigned q = 0;
       cudaMemcpyAsync(&q, counts + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
@@ -1700,7 +1994,7 @@ extern "C" tpt_status tpt_render_noalloc(const tpt_scene *scene, void *arena_dev
   TPT_CUDA(cudaMemsetAsync(counters, 0, sizeof(WfCounters), stream));
   const FrameDesc F{p->width, p->height, p->spp, npix * (unsigned long long)p->spp, accum, nullptr};
   const RenderCfg cfg{p->max_depth, p->semantics, p->background, p->sky_scale,
-                      make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32))};
+                      make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32)), p->refill > 0 ? p->refill : 1};
   const PersistentKernel kern = persistent_variant(p->wave);
   const int smem = stack_smem(block);
   TPT_CUDA(smem_optin(kern, smem));

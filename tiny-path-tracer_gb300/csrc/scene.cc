@@ -1104,6 +1104,9 @@ struct Compiler {
         if (ref[c] >= 0) {
           lo = S.node_lo[ref[c]];
           hi = S.node_hi[ref[c]];
+          // the box's size term of the pruning bound, in the device's order
+          // of float operations (prune_key)
+          hi.w = ((hi.x - lo.x) + (hi.y - lo.y)) + (hi.z - lo.z);
         }
         std::memcpy(&lo.w, &ref[c], 4);
         S.node_kids[4 * i + 2 * c] = lo;

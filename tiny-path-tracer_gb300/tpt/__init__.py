@@ -45,7 +45,8 @@ class RenderParams(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("max_depth", C.c_int32),
                 ("semantics", C.c_int32), ("background", C.c_int32), ("sky_scale", C.c_float),
                 ("seed", C.c_uint64), ("engine", C.c_int32), ("block", C.c_int32), ("wave", C.c_int32),
-                ("accumulate_fp64", C.c_int32), ("profile", C.c_int32), ("flat_nodes", C.c_int32)]
+                ("accumulate_fp64", C.c_int32), ("profile", C.c_int32), ("flat_nodes", C.c_int32),
+                ("refill", C.c_int32)]
 
 
 class Config(C.Structure):
@@ -335,9 +336,9 @@ class Context:
     def render(self, slot: int, width: int, height: int, spp: int, max_depth: int = 50,
                semantics: int = SEMANTICS_REFERENCE, background: int = BACKGROUND_BLACK, sky_scale: float = 1.0,
                seed: int = 1, engine: int = ENGINE_AUTO, block: int = 0, wave: int = 0, fp64: bool = False,
-               profile: bool = False, flat_nodes: int = 0, out=None):
+               profile: bool = False, flat_nodes: int = 0, out=None, refill: int = 0):
         p = make_params(width, height, spp, max_depth, semantics, background, sky_scale, seed, engine, block,
-                        wave, fp64, profile, flat_nodes)
+                        wave, fp64, profile, flat_nodes, refill)
         st = RenderStats()
         if out is None:
             img = np.zeros((height, width, 3), np.float32)
@@ -349,12 +350,14 @@ class Context:
 
 
 def render_guided(ctx: "Context", slot: int, width: int, height: int, spp: int, max_depth: int = 50,
-                  background: int = BACKGROUND_BLACK, seed: int = 1, out=None, **guide):
+                  background: int = BACKGROUND_BLACK, seed: int = 1, out=None, refill: int = 0, engine: int = 0,
+                  **guide):
     """Learned path guiding (physical semantics).  guide: fields of
     tpt_guide_params (passes, train_steps, batch, lr, grid_res, alpha,
     record_cap, seed).  out: None (host image returned) or a device pointer.
     Returns (image or None, render stats, guide stats)."""
-    p = make_params(width, height, spp, max_depth, SEMANTICS_PHYSICAL, background, 1.0, seed)
+    p = make_params(width, height, spp, max_depth, SEMANTICS_PHYSICAL, background, 1.0, seed, engine=engine,
+                    refill=refill)
     g = GuideParams()
     lib().tpt_guide_params_default(C.byref(g))
     for k, v in guide.items():
@@ -421,11 +424,11 @@ def guide_records(ctx: "Context", cap: int = 1 << 22) -> np.ndarray:
 
 def render_nrc(ctx: "Context", slot: int, width: int, height: int, spp: int, max_depth: int = 50,
                semantics: int = SEMANTICS_PHYSICAL, background: int = BACKGROUND_BLACK, seed: int = 1, out=None,
-               **nrc):
+               refill: int = 0, engine: int = 0, **nrc):
     """Neural radiance cache render.  nrc: fields of tpt_nrc_params.  out:
     None (host image returned) or a device pointer.
     Returns (image or None, render stats, cache stats)."""
-    p = make_params(width, height, spp, max_depth, semantics, background, 1.0, seed)
+    p = make_params(width, height, spp, max_depth, semantics, background, 1.0, seed, engine=engine, refill=refill)
     n = NrcParams()
     lib().tpt_nrc_params_default(C.byref(n))
     for k, v in nrc.items():
@@ -471,7 +474,7 @@ def autotune(ctx: "Context", slot: int, width: int, height: int, probe_spp: int 
 
 
 def make_params(width, height, spp, max_depth=50, semantics=0, background=0, sky_scale=1.0, seed=1, engine=0,
-                block=0, wave=0, fp64=False, profile=False, flat_nodes=0) -> RenderParams:
+                block=0, wave=0, fp64=False, profile=False, flat_nodes=0, refill=0) -> RenderParams:
     p = RenderParams()
     lib().tpt_render_params_default(C.byref(p))
     p.width, p.height, p.spp, p.max_depth = width, height, spp, max_depth
@@ -479,6 +482,7 @@ def make_params(width, height, spp, max_depth=50, semantics=0, background=0, sky
     p.engine, p.block, p.wave, p.accumulate_fp64 = engine, block, wave, int(bool(fp64))
     p.profile = int(bool(profile))
     p.flat_nodes = flat_nodes
+    p.refill = refill
     return p
 
 
