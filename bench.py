@@ -53,10 +53,10 @@ BYTES_PER_SEGMENT = 192
 TRAVERSE_BYTES_PER_SEGMENT = 64 + 16  # traverse reads the path record, writes the hit
 # k_persistent DRAM read+write bytes and warp instructions per ray segment,
 # from the ncu capture of the 16 spp case
-# (profiles/k_persistent_cornell_600x600_16spp.md): 7.634 MB and 3.454 G warp
+# (profiles/k_persistent_cornell_600x600_16spp.md): 5.865 MB and 3.167 G warp
 # instructions over 30.42 M segments
-NCU_DRAM_BYTES_PER_SEGMENT = 7.633664e6 / 30416883
-NCU_WARP_INST_PER_SEGMENT = 3454032782 / 30416883
+NCU_DRAM_BYTES_PER_SEGMENT = 5.864704e6 / 30416883
+NCU_WARP_INST_PER_SEGMENT = 3167059649 / 30416883
 # instruction issue peak: 152 SMs x 4 schedulers x 1 warp instruction per
 # cycle at the maximum SM clock (MEASURED_PEAKS.json sm_max_mhz)
 SMS, SCHEDULERS_PER_SM = 152, 4

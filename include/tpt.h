@@ -199,7 +199,7 @@ typedef struct {
   int32_t engine;           /* TPT_ENGINE_* */
   int32_t block;            /* threads per block, 0 = tuned (persistent engine: <= 128) */
   int32_t wave;             /* wavefront: path slots (0 = 1M); persistent: register
-                               variant, minimum resident blocks 4 (default), 6 or 8 */
+                               variant, minimum resident blocks 4 (default), 5, 6 or 8 */
   int32_t accumulate_fp64;  /* 1: also accumulate in double (out_rgb is the FP64 mean) */
   int32_t profile;          /* 1: time each traverse/shade launch with CUDA events */
   int32_t flat_nodes;       /* stackless-walk size limit; 0 = the context option */

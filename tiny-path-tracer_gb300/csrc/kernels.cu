@@ -1212,6 +1212,7 @@ static tpt_status run_wavefront(tpt_context *c, const DevScene &S, const RenderC
 typedef void (*PersistentKernel)(DevScene, RenderCfg, FrameDesc, WfCounters *);
 static PersistentKernel persistent_variant(int v) {
   switch (v) {
+    case 5: return k_persistent<5>;
     case 6: return k_persistent<6>;
     case 8: return k_persistent<8>;
     default: return k_persistent<4>;
@@ -1512,7 +1513,7 @@ extern "C" tpt_status tpt_autotune(tpt_context *c, int32_t slot, tpt_render_para
   };
   std::vector<Cand> cands;
   for (int block : {64, 128})
-    for (int var : {4, 6})
+    for (int var : {4, 5, 6})
       for (int flat : {16, 48, 1 << 20}) cands.push_back({TPT_ENGINE_PERSISTENT, block, var, flat});
   for (int block : {128, 256})
     for (int wave : {1 << 19, 1 << 20}) cands.push_back({TPT_ENGINE_WAVEFRONT, block, wave, 48});
