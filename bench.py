@@ -380,9 +380,14 @@ def main() -> None:
     scene = tpt.Scene(text)
     slot = ctx.upload(scene)
     arena_bytes = scene.info()["arena_bytes"]
+    tuned = None
+    if args.engine == 0:  # engine choice, block, register variant by the autotuner (untimed)
+        tuned = tpt.autotune(ctx, slot, W, H, 16, max_depth=DEPTH)
     img = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     kw = dict(max_depth=DEPTH, engine=args.engine, wave=args.wave, block=args.block, seed=1)
+    if tuned:  # the e2e frames (fresh uploads) render with the same configuration
+        kw.update(engine=tuned[0], block=tuned[1], wave=tuned[2], flat_nodes=tuned[3])
 
     def barrier():
         if dist is not None:
@@ -444,7 +449,7 @@ def main() -> None:
     roof = None
     if tr_n > 0 and tr_ms > 0:
         seg_per_launch = segs / tr_n
-        wavefront = args.engine == 1
+        wavefront = kw["engine"] == 1
         per_seg = TRAVERSE_BYTES_PER_SEGMENT if wavefront else BYTES_PER_SEGMENT
         algo_bytes = seg_per_launch * per_seg
         achieved = algo_bytes / (tr_ms / tr_n / 1e3) / 1e9
@@ -476,7 +481,9 @@ def main() -> None:
                "config": {"workload": WORKLOAD if args.spp == SPP else f"{WORKLOAD} (profiling case: {args.spp} spp)",
                           "width": W, "height": H, "spp": args.spp, "max_depth": DEPTH,
                           "semantics": "reference",
-                          "engine": ["auto (persistent)", "wavefront", "persistent"][args.engine],
+                          "engine": (["auto", "wavefront", "persistent"][tuned[0]] + " (autotuned: block %d, %s %d)" % (
+                              tuned[1], "variant" if tuned[0] == 2 else "queue", tuned[2]) if tuned else
+                              ["auto", "wavefront", "persistent"][args.engine]),
                           "l2": "flushed between timed steps (256 MB write)",
                           "segments_per_step": segs / args.steps},
                "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": int(arena_bytes),

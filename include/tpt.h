@@ -103,6 +103,12 @@ int32_t tpt_hitable_list(tpt_builder *b, const int32_t *items, int32_t n);      
  * Returns TPT_ERR_NO_BOUNDING_BOX (negated) where the reference would exit. */
 int32_t tpt_bvh_node(tpt_builder *b, const int32_t *items, int32_t n, float t0, float t1);
 
+/* drand_r(min, max) (utils.cc:28-32) on the builder's stream: scene code that
+ * draws its random layout through this shares one mt19937 stream with
+ * bvh_node, exactly as the reference's scene functions share drand_r with
+ * the bvh_node constructor on their thread. */
+double tpt_builder_drand(tpt_builder *b, double min, double max);
+
 tpt_status tpt_builder_set_world(tpt_builder *b, int32_t world);
 /* light_shape argument of color() (utils.h:26-27); -1 = none (pure cosine). */
 tpt_status tpt_builder_set_light_shape(tpt_builder *b, int32_t light_shape);
@@ -271,7 +277,8 @@ enum { TPT_MAX_BATCH = 256 };
 tpt_status tpt_render_batch(tpt_context *ctx, const tpt_batch_item *items, int32_t n, const tpt_render_params *common,
                             int32_t mem, tpt_render_stats *stats);
 
-/* Autotuner: renders `probe_spp` samples per pixel with each candidate
+/* Autotuner: renders `probe_spp` samples per pixel (raised so that a probe
+ * has at least 16 M samples: smaller probes measure launch tails) with each candidate
  * configuration - engine, threads per block, register variant, wavefront
  * queue size, stackless-walk threshold - times them with CUDA events, writes
  * the fastest into *p (engine, block, wave, flat_nodes; the other fields are

@@ -95,6 +95,8 @@ def ref_lib():
         L.ref_render.restype = C.c_double
         L.ref_render.argtypes = [C.c_void_p, C.POINTER(RefRenderParams), C.c_void_p]
         L.ref_hardware_concurrency.restype = C.c_int32
+        L.ref_frontend_bvh.restype = C.c_int32
+        L.ref_frontend_bvh.argtypes = [C.c_int32, C.c_void_p, C.c_int32]
         L.ref_config_parse.restype = None
         L.ref_config_parse.argtypes = [C.c_char_p, C.c_void_p]
         _ref = L
@@ -188,6 +190,15 @@ def procedural_image(w: int, h: int, seed: int) -> np.ndarray:
     out = np.zeros((h, w, 3), np.uint8)
     lib().oracle_procedural_image(w, h, seed, _ptr(out))
     return out
+
+
+def ref_frontend_bvh(n: int):
+    """Pre-order node boxes of the reference's bvh_node over n spheres laid
+    out with its drand_r (the sequence of tests/frontend/random_bvh.cc)."""
+    cap = 2 * n + 2
+    out = np.zeros((cap, 6), np.float32)
+    k = ref_lib().ref_frontend_bvh(n, out.ctypes.data_as(C.c_void_p), cap)
+    return out[:k]
 
 
 def ref_config_parse(text: str) -> list:

@@ -434,6 +434,39 @@ double ref_render(void *sp, const ref_render_params *p, float *mean_rgb) {
 
 int32_t ref_hardware_concurrency(void) { return (int32_t)std::thread::hardware_concurrency(); }
 
+static void frontend_boxes(const bvh_node *bn, std::vector<float> &out) {
+  for (int i = 0; i < 3; i++) out.push_back(bn->box_.min()[i]);
+  for (int i = 0; i < 3; i++) out.push_back(bn->box_.max()[i]);
+  const hitable *ch[2] = {bn->left_, bn->right_};
+  for (int c = 0; c < 2; c++) {
+    if (c == 1 && ch[1] == ch[0]) break;
+    if (auto *cb = dynamic_cast<const bvh_node *>(ch[c])) frontend_boxes(cb, out);
+  }
+}
+
+// The reference side of tests/frontend/random_bvh.cc: the same n spheres
+// drawn with the reference's drand_r, then bvh_node, on a fresh thread
+// (default drand_r stream); writes the pre-order node boxes (6 floats each)
+// and returns the node count.
+int32_t ref_frontend_bvh(int32_t n, float *boxes, int32_t cap) {
+  std::vector<float> out;
+  std::thread th([&]() {
+    material *m = new lambertian(new constant_texture(vec3(0.5f, 0.5f, 0.5f)));
+    std::vector<hitable *> list;
+    for (int i = 0; i < n; i++) {
+      const float x = (float)drand_r(-10, 10);
+      const float z = (float)drand_r(-10, 10);
+      const float r = (float)(0.1 + 0.3 * drand_r(0, 1));
+      list.push_back(new sphere(vec3(x, r, z), r, m));
+    }
+    frontend_boxes(new bvh_node(list.data(), n, 0.0f, 1.0f), out);
+  });
+  th.join();
+  const int nodes = (int)out.size() / 6;
+  for (int i = 0; i < 6 * nodes && i < 6 * cap; i++) boxes[i] = out[i];
+  return nodes;
+}
+
 // config.ini through the reference's own parser and the extraction calls of
 // main.cpp:42-56, from main.cpp:31-40's defaults.  out: width, height,
 // sample, recur_depth, fov, allow_bonus_pic, bonus_pic, aperture,

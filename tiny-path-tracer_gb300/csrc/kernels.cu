@@ -1518,6 +1518,9 @@ extern "C" tpt_status tpt_autotune(tpt_context *c, int32_t slot, tpt_render_para
   for (int block : {128, 256})
     for (int wave : {1 << 19, 1 << 20}) cands.push_back({TPT_ENGINE_WAVEFRONT, block, wave, 48});
   const size_t npix = (size_t)p->width * p->height;
+  // a probe of a few M samples is dominated by the launch tail of the
+  // persistent kernels: probe at least 16 M samples
+  probe_spp = std::max<int32_t>(probe_spp, (int32_t)((16ull << 20) / npix) + 1);
   tpt_status st;
   if ((st = ensure(c->staging, npix * 3 * sizeof(float))) != TPT_OK) return st;
   double best = -1.0;

@@ -537,6 +537,8 @@ tpt_status tpt_builder_set_bvh_build(tpt_builder *b, int32_t mode) {
   return TPT_OK;
 }
 
+double tpt_builder_drand(tpt_builder *b, double min, double max) { return b ? b->drand(min, max) : 0.0; }
+
 tpt_status tpt_builder_set_world(tpt_builder *b, int32_t world) {
   if (!b) return TPT_ERR_INVALID_ARGUMENT;
   if (!b->valid_node(world)) return TPT_ERR_BAD_HANDLE;
