@@ -215,6 +215,10 @@ def batch_bench(args) -> None:
     outs = [torch.empty((h, w, 3), dtype=torch.float32, device="cuda") for _, w, h, _ in jobs]
     ptrs = [o.data_ptr() for o in outs]
     kw = dict(max_depth=50, background=tpt.BACKGROUND_SKY, seed=1, block=args.block, variant=args.wave)
+    tuned = None
+    if args.block == 0 and args.wave == 0:  # block, register variant, walk threshold by the autotuner (untimed)
+        tuned = tpt.autotune_batch(ctx, jobs, ptrs, 8, max_depth=50, background=tpt.BACKGROUND_SKY, seed=1)
+        kw.update(block=tuned[0], variant=tuned[1], flat_nodes=tuned[2])
     for _ in range(args.warmup):
         tpt.render_batch(ctx, jobs, outs=ptrs, **kw)
     torch.cuda.synchronize()
@@ -237,6 +241,8 @@ def batch_bench(args) -> None:
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": "batch_64_random_sphere_scenes", "scenes": len(jobs), "samples_per_step": samples,
                       "bvh": args.bvh,
+                      "launch": {"block": kw["block"], "variant": kw["variant"], "flat_nodes": kw.get("flat_nodes", 0),
+                                 "autotuned": tuned is not None},
                       "spheres": [sd.meta["n_spheres"] for sd in sds][:8] + ["..."],
                       "segments_per_step": st["segments"], "scene_build_and_upload_s": build_s},
            "gpu_launches": st["kernel_launches"] * args.steps, "clocks": clk}

@@ -286,6 +286,13 @@ tpt_status tpt_render_batch(tpt_context *ctx, const tpt_batch_item *items, int32
  * engine = TPT_ENGINE_AUTO use it.  best_msps (may be NULL) receives the
  * winner's Msamples/s. */
 tpt_status tpt_autotune(tpt_context *ctx, int32_t slot, tpt_render_params *p, int32_t probe_spp, double *best_msps);
+/* Autotuner of a batch: renders the batch with every item's spp divided by
+ * spp_divisor (at least 1) for each candidate block size, register variant
+ * and stackless-walk threshold of the batched persistent launch, times them
+ * with CUDA events and writes the fastest into p (block, wave, flat_nodes)
+ * for tpt_render_batch.  best_msps (may be NULL) receives its Msamples/s. */
+tpt_status tpt_autotune_batch(tpt_context *ctx, const tpt_batch_item *items, int32_t n, tpt_render_params *p,
+                              int32_t spp_divisor, double *best_msps);
 
 /* ------------------------------------------------------------------------
  * Learned parts: fully fused FP16 MLPs on the tensor cores (FP32

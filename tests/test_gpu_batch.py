@@ -62,3 +62,21 @@ def test_autotune_picks_a_config_that_auto_renders_use(ctx):
     b, _ = ctx.render(slot, 40, 40, 8, seed=5, fp64=True, engine=eng, block=block, wave=wave, flat_nodes=flat)
     np.testing.assert_allclose(a, b, rtol=1e-6, atol=1e-7)
     ctx.release(slot)
+
+
+def test_batch_autotuner_and_variant_5(ctx):
+    import torch
+
+    slots = _slots(ctx)
+    jobs = [(slots[0], 40, 30, 16), (slots[1], 17, 23, 16), (slots[3], 24, 24, 8)]
+    outs = [torch.empty((h, w, 3), dtype=torch.float32, device="cuda") for _, w, h, _ in jobs]
+    block, variant, flat, msps = tpt.autotune_batch(ctx, jobs, [o.data_ptr() for o in outs], spp_divisor=4,
+                                                    background=tpt.BACKGROUND_SKY, seed=3)
+    assert block in (64, 128) and variant in (4, 5, 6) and flat in (16, 48) and msps > 0
+    # every variant renders the same images (register caps change spills, not arithmetic)
+    ref, _ = tpt.render_batch(ctx, jobs, background=tpt.BACKGROUND_SKY, seed=3, block=128, variant=4)
+    got, _ = tpt.render_batch(ctx, jobs, background=tpt.BACKGROUND_SKY, seed=3, block=64, variant=5)
+    for a, b in zip(ref, got):
+        np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-6)
+    for s in set(slots):
+        ctx.release(s)

@@ -1334,6 +1334,7 @@ static uint64_t fnv1a(uint64_t h, const void *data, size_t n) {
 typedef void (*BatchKernel)(const BatchItem *, int, unsigned long long, RenderCfg, WfCounters *);
 static BatchKernel batch_variant(int v) {
   switch (v) {
+    case 5: return k_persistent_batch<5>;
     case 6: return k_persistent_batch<6>;
     case 8: return k_persistent_batch<8>;
     default: return k_persistent_batch<4>;
@@ -1504,6 +1505,56 @@ extern "C" tpt_status tpt_render_batch(tpt_context *c, const tpt_batch_item *ite
 }
 
 // ============================================================= autotuner ==
+extern "C" tpt_status tpt_autotune_batch(tpt_context *c, const tpt_batch_item *items, int32_t n,
+                                         tpt_render_params *p, int32_t spp_divisor, double *best_msps) {
+  if (!c || !items || !p || n < 1 || n > TPT_MAX_BATCH || spp_divisor < 1) return TPT_ERR_INVALID_ARGUMENT;
+  std::vector<tpt_batch_item> probe(items, items + n);
+  for (auto &it : probe) it.spp = std::max(1, it.spp / spp_divisor);
+  struct Cand {
+    int block, variant, flat;
+  };
+  std::vector<Cand> cands;
+  for (int block : {64, 128})
+    for (int var : {4, 5, 6})
+      for (int flat : {16, 48}) cands.push_back({block, var, flat});
+  cudaEvent_t e0, e1;
+  TPT_CUDA(cudaEventCreate(&e0));
+  TPT_CUDA(cudaEventCreate(&e1));
+  double best = -1.0;
+  Cand win = cands[0];
+  tpt_status st = TPT_OK;
+  for (const Cand &cd : cands) {
+    tpt_render_params q = *p;
+    q.block = cd.block;
+    q.wave = cd.variant;
+    q.flat_nodes = cd.flat;
+    q.profile = 0;
+    tpt_render_stats rs{};
+    float ms = 0.f;
+    for (int rep = 0; rep < 2 && st == TPT_OK; rep++) {  // the first run captures the graph
+      cudaEventRecord(e0, c->stream);
+      st = tpt_render_batch(c, probe.data(), n, &q, TPT_MEM_DEVICE, &rs);
+      cudaEventRecord(e1, c->stream);
+      cudaEventSynchronize(e1);
+      cudaEventElapsedTime(&ms, e0, e1);
+    }
+    if (st != TPT_OK) break;
+    const double msps = (double)rs.samples / (ms * 1e3);
+    if (msps > best) {
+      best = msps;
+      win = cd;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != TPT_OK) return st;
+  p->block = win.block;
+  p->wave = win.variant;
+  p->flat_nodes = win.flat;
+  if (best_msps) *best_msps = best;
+  return TPT_OK;
+}
+
 extern "C" tpt_status tpt_autotune(tpt_context *c, int32_t slot, tpt_render_params *p, int32_t probe_spp,
                                    double *best_msps) {
   if (!c || !p || probe_spp <= 0 || p->width <= 0 || p->height <= 0) return TPT_ERR_INVALID_ARGUMENT;

@@ -180,6 +180,8 @@ _SIGS = {
                                       C.c_void_p, C.c_int32, C.POINTER(RenderStats), C.POINTER(GuideStats)]),
     "tpt_guide_records": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
     "tpt_nrc_params_default": (None, [C.POINTER(NrcParams)]),
+    "tpt_autotune_batch": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.c_int32,
+                                       C.POINTER(C.c_double)]),
     "tpt_config_default": (None, [C.POINTER(Config)]),
     "tpt_builder_set_bvh_build": (C.c_int32, [C.c_void_p, C.c_int32]),
     "tpt_scene_from_text_opt": (C.c_int32, [C.c_char_p, C.c_int32, C.POINTER(C.c_void_p), C.c_char_p, C.c_size_t]),
@@ -439,6 +441,20 @@ def render_nrc(ctx: "Context", slot: int, width: int, height: int, spp: int, max
     check(lib().tpt_render_nrc(ctx._h, slot, C.byref(p), C.byref(n), dst, mem, C.byref(st), C.byref(ns)),
           "render_nrc")
     return img, st.as_dict(), ns.as_dict()
+
+
+def autotune_batch(ctx: "Context", jobs, outs, spp_divisor=8, max_depth=50, semantics=SEMANTICS_REFERENCE,
+                   background=BACKGROUND_BLACK, sky_scale=1.0, seed=1):
+    """tpt_autotune_batch over jobs (slot, width, height, spp) rendering into
+    the device pointers outs; returns (block, variant, flat_nodes, Msamples/s)."""
+    n = len(jobs)
+    arr = (BatchItem * n)()
+    for k, (slot, w, h, spp) in enumerate(jobs):
+        arr[k] = BatchItem(slot, w, h, spp, int(outs[k]))
+    p = make_params(1, 1, 1, max_depth, semantics, background, sky_scale, seed, ENGINE_PERSISTENT)
+    best = C.c_double()
+    check(lib().tpt_autotune_batch(ctx._h, arr, n, C.byref(p), spp_divisor, C.byref(best)), "autotune_batch")
+    return p.block, p.wave, p.flat_nodes, best.value
 
 
 def render_batch(ctx: "Context", jobs, max_depth=50, semantics=SEMANTICS_REFERENCE, background=BACKGROUND_BLACK,
