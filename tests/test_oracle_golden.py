@@ -93,3 +93,18 @@ def test_oracle_render_matches_reference_statistics(built, name):
     ok = s > 0
     z = d[ok] / s[ok]
     assert abs(z.mean()) < 0.1 and 0.5 < z.std() < 1.6, (z.mean(), z.std())
+
+
+@pytest.mark.parametrize("name", ["cornell", "one_weekend", "instances", "next_week"])
+def test_oracle_edge_rays_match_reference(built, name):
+    """Known-answer rays at the edges of the primitives' arithmetic
+    (tangent and near-tangent to spheres, from sphere surfaces, at rect and
+    box edges and corners, axis-parallel through rect edges - where the
+    reference's 0/0 gives t = NaN), frozen from the reference itself: the
+    oracle reproduces every result bit for bit."""
+    g = np.load(os.path.join(GOLDEN, f"{name}_edge.npz"))
+    ora = pyoracle.Scene(_sd(name))
+    f, i = ora.trace(g["rays"], media_mode=1, nthreads=1)  # the reference's drand_r order for media
+    assert np.array_equal(i, g["hit_i"])
+    hit = g["hit_i"][:, 0] == 1
+    assert np.array_equal(f[hit], g["hit_f"][hit], equal_nan=True)

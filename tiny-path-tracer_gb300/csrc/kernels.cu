@@ -574,10 +574,14 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
 
 // Guided persistent engine: as k_persistent, with guided diffuse vertices
 // and one training record per recorded path (every `rec_stride`-th sample).
+// A recording path parks the state of its first diffuse vertex in `pend`
+// (5 float4 per slot) and emits the finished record into the ring when it
+// ends, so non-recording lanes carry no record state in registers.
 template <int MIN_BLOCKS>
 __global__ void __launch_bounds__(128, MIN_BLOCKS)
     k_persistent_guided(DevScene S, RenderCfg cfg, FrameDesc F, WfCounters *C, GuideView gv, uint32_t sample_base,
-                        float4 *__restrict__ records, unsigned *rec_count, unsigned rec_cap, uint32_t rec_stride) {
+                        float4 *__restrict__ records, unsigned *rec_count, unsigned rec_cap, uint32_t rec_stride,
+                        float4 *__restrict__ pend, unsigned *pend_count) {
   extern __shared__ int2 stack_smem[];
   int2 *stk = stack_smem + threadIdx.x;
   int e = 0;
@@ -587,8 +591,8 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
   float3 T = v3(0.f, 0.f, 0.f), L = v3(0.f, 0.f, 0.f);
   uint32_t pixel = 0, sample = 0;
   int depth = 0;
-  GuideRec rec{};
   bool want_rec = false;
+  int ps = -1;  // pending-record slot of this path
   for (;;) {
     const bool want = !alive && !done;
     if (refill_now(want, alive, cfg.refill)) {
@@ -605,8 +609,8 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
           T = v3(1.f, 1.f, 1.f);
           L = v3(0.f, 0.f, 0.f);
           depth = 0;
-          rec.valid = false;
           want_rec = (s % rec_stride) == 0;
+          ps = -1;
           alive = true;
         } else {
           done = true;
@@ -614,31 +618,49 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
       }
     }
     if (__all_sync(0xffffffffu, done)) break;
-    bool emit = false;
-    float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0;
+    bool new_rec = false, ended = false;
+    GuideRec rec{};
     if (alive) {
       MediumRng m{make_uint4(pixel, sample, (uint32_t)depth, 0u), cfg.key, 1};
       HitRef h;
       const bool hit = trace_closest(S, r, 0.001f, stk, blockDim.x, m, h, e);
       segs++;
+      rec.valid = !want_rec || ps >= 0;  // only a recording path without a record takes one
       if (shade_vertex_t<true>(S, cfg, r, hit, h, T, L, depth, pixel, sample, gv, rec)) {
         depth++;
       } else {
         accumulate(F, pixel, L);
         alive = false;
-        if (want_rec && rec.valid) {
-          // contribution of the sampled direction: (L_final - L_k) / T_k
-          const float3 c = v3((L.x - rec.L.x) / rec.T.x, (L.y - rec.L.y) / rec.T.y, (L.z - rec.L.z) / rec.T.z);
-          float wgt = (c.x + c.y + c.z) * (1.f / 3.f);
-          if (!(wgt >= 0.f) || !(wgt < 1e6f)) wgt = 0.f;
-          // a NaN direction (the reference's sphere cone sampling from inside
-          // the sphere) or position would poison a whole training batch
-          emit = finite3(rec.x) && finite3(rec.n) && finite3(rec.d);
-          r0 = make_float4(rec.x.x, rec.x.y, rec.x.z, wgt);
-          r1 = make_float4(rec.n.x, rec.n.y, rec.n.z, 0.f);
-          r2 = make_float4(rec.d.x, rec.d.y, rec.d.z, 0.f);
-        }
+        ended = true;
       }
+      // a NaN direction (the reference's sphere cone sampling from inside
+      // the sphere) or position would poison a whole training batch
+      new_rec = want_rec && ps < 0 && rec.valid && finite3(rec.x) && finite3(rec.n) && finite3(rec.d);
+    }
+    const unsigned np = warp_append(new_rec, pend_count);
+    if (new_rec && np < rec_cap) {
+      float4 *q = pend + 5 * (size_t)np;
+      q[0] = make_float4(rec.x.x, rec.x.y, rec.x.z, 0.f);
+      q[1] = make_float4(rec.n.x, rec.n.y, rec.n.z, 0.f);
+      q[2] = make_float4(rec.d.x, rec.d.y, rec.d.z, 0.f);
+      q[3] = make_float4(rec.T.x, rec.T.y, rec.T.z, 0.f);
+      q[4] = make_float4(rec.L.x, rec.L.y, rec.L.z, 0.f);
+      ps = (int)np;
+    }
+    bool emit = false;
+    float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0;
+    if (ended && ps >= 0) {  // contribution of the sampled direction: (L_final - L_k) / T_k
+      const float4 *q = pend + 5 * (size_t)ps;
+      const float4 qT = q[3], qL = q[4];
+      const float3 c = v3((L.x - qL.x) / qT.x, (L.y - qL.y) / qT.y, (L.z - qL.z) / qT.z);
+      float wgt = (c.x + c.y + c.z) * (1.f / 3.f);
+      if (!(wgt >= 0.f) || !(wgt < 1e6f)) wgt = 0.f;
+      const float4 x = q[0];
+      r0 = make_float4(x.x, x.y, x.z, wgt);
+      r1 = q[1];
+      r2 = q[2];
+      emit = true;
+      ps = -1;
     }
     const unsigned slot = warp_append(emit, rec_count) % rec_cap;  // ring: the newest records win
     if (emit) {
@@ -1678,10 +1700,14 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
                        : 128;
   const size_t wave = wf_wave(p, sl);
   const int smem = stack_smem(block);
-  auto kern = k_persistent_guided<4>;
-  TPT_CUDA(smem_optin(kern, smem));
-  const int grid = grid_for(c, kern, 128, stack_smem(128));
-  if (wf && ((st = ensure(c->learn_pend, (size_t)g->record_cap * 5 * sizeof(float4))) != TPT_OK)) return st;
+  // persistent: the slot's tuned register variant (4 or 5 blocks per SM) and block size
+  const bool tuned_p = sl.tuned && sl.tp.engine == TPT_ENGINE_PERSISTENT;
+  const int pvar = p->wave > 0 ? p->wave : (tuned_p ? sl.tp.wave : 4);
+  const int pblock = p->block > 0 && p->block <= 128 ? p->block : (tuned_p ? sl.tp.block : 128);
+  auto kern = pvar == 5 ? k_persistent_guided<5> : k_persistent_guided<4>;
+  TPT_CUDA(smem_optin(kern, stack_smem(pblock)));
+  const int grid = grid_for(c, kern, pblock, stack_smem(pblock));
+  if ((st = ensure(c->learn_pend, (size_t)g->record_cap * 5 * sizeof(float4))) != TPT_OK) return st;
   const unsigned long long per_pass = F.total;
   const uint32_t stride = (uint32_t)std::max<unsigned long long>(1ull, per_pass / (unsigned long long)g->record_cap);
   cudaEvent_t e[4];
@@ -1716,9 +1742,11 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
       WfCounters init{};
       std::memcpy(c->counters_host, &init, sizeof(init));
       cudaMemcpyAsync(c->counters, c->counters_host, sizeof(WfCounters), cudaMemcpyHostToDevice, c->stream);
-      kern<<<grid, 128, stack_smem(128), c->stream>>>(S, cfg, F, c->counters, gv, (uint32_t)(pass * spp_pass),
-                                                     (float4 *)c->guide_records.p, (unsigned *)c->guide_count.p,
-                                                     (unsigned)g->record_cap, stride);
+      cudaMemsetAsync((unsigned *)c->guide_count.p + 1, 0, sizeof(unsigned), c->stream);
+      kern<<<grid, pblock, stack_smem(pblock), c->stream>>>(
+          S, cfg, F, c->counters, gv, (uint32_t)(pass * spp_pass), (float4 *)c->guide_records.p,
+          (unsigned *)c->guide_count.p, (unsigned)g->record_cap, stride, (float4 *)c->learn_pend.p,
+          (unsigned *)c->guide_count.p + 1);
     }
     cudaEventRecord(e[1], c->stream);
     unsigned count = 0;
