@@ -376,7 +376,7 @@ tpt_status tpt_guide_records(tpt_context *ctx, float *out, int64_t cap, int64_t 
  * each pass the cache takes train_steps Adam steps on them (relative L2
  * loss).  The first pass traces every path to full depth.
  * The estimator is biased by the cache's error; the plain tracer is its
- * fallback and its judge. */
+ * fallback and the yardstick for that error. */
 typedef struct {
   int32_t passes;           /* >= 1 (8) */
   int32_t train_steps;      /* Adam steps after each pass (128) */

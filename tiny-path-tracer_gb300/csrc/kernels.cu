@@ -673,14 +673,17 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
   if (e) atomicExch(&C->err, e);
 }
 
-// Radiance-cache engine.  Paths stop at vertex `term_depth` and leave a
-// query; every `train_stride`-th path is traced to full depth and records its
-// vertices 0..2 (features now, target (L_final - L_k) / T_k at its end).
+// Radiance-cache engine.  Paths stop at their first diffuse vertex at or
+// past `term_depth` and leave a query; every `train_stride`-th path is traced
+// to full depth and records its first three diffuse vertices (features now;
+// T_k, L_k parked in `pend` under the record's slot; target (L_final - L_k) /
+// T_k at its end).
 template <int MIN_BLOCKS>
 __global__ void __launch_bounds__(128, MIN_BLOCKS)
     k_persistent_nrc(DevScene S, RenderCfg cfg, FrameDesc F, WfCounters *C, unsigned long long sample_offset,
                      int term_depth, uint32_t train_stride, float4 *__restrict__ records, unsigned *rec_count,
-                     unsigned rec_cap, float4 *__restrict__ queries, unsigned *q_count, unsigned q_cap) {
+                     unsigned rec_cap, float4 *__restrict__ queries, unsigned *q_count, unsigned q_cap,
+                     float4 *__restrict__ pend) {
   extern __shared__ int2 stack_smem[];
   int2 *stk = stack_smem + threadIdx.x;
   int e = 0;
@@ -690,9 +693,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
   float3 T = v3(0.f, 0.f, 0.f), L = v3(0.f, 0.f, 0.f);
   uint32_t pixel = 0, sample = 0;
   int depth = 0;
-  unsigned rslot[3];
-  float3 rT[3], rL[3];
-  int nrec = 0;
+  int4 rslot = make_int4(-1, -1, -1, 0);  // record slots, count in .w
   GuideView gv{};
   GuideRec grec{};
   for (;;) {
@@ -711,7 +712,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
           L = v3(0.f, 0.f, 0.f);
           depth = 0;
           training = ((s + sample_offset) % train_stride) == 0;
-          nrec = 0;
+          rslot = make_int4(-1, -1, -1, 0);
           alive = true;
         } else {
           done = true;
@@ -721,15 +722,14 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
     if (__all_sync(0xffffffffu, done)) break;
     bool want_q = false, want_r = false;
     VertexInfo vi{};
-    float3 qT = T;
+    float3 qT = T, Tb = T, Lb = L;
     if (alive) {
       MediumRng m{make_uint4(pixel, sample, (uint32_t)depth, 0u), cfg.key, 1};
       HitRef h;
       const bool hit = trace_closest(S, r, 0.001f, stk, blockDim.x, m, h, e);
       segs++;
-      const float3 Tb = T, Lb = L;
       const bool may_query = !training && depth >= term_depth;
-      const bool rec_here = training && hit && nrec < 3;
+      const bool rec_here = training && hit && rslot.w < 3;
       bool queried = false;
       const bool cont = shade_vertex_t<false>(S, cfg, r, hit, h, T, L, depth, pixel, sample, gv, grec,
                                               (rec_here || may_query) ? &vi : nullptr,
@@ -740,11 +740,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
         alive = false;
       } else {
         // records only where queries happen: diffuse vertices
-        if (rec_here && (vi.kind == MT_LAMBERTIAN || vi.kind == MT_ISOTROPIC)) {
-          want_r = true;
-          rT[nrec] = Tb;
-          rL[nrec] = Lb;
-        }
+        want_r = rec_here && (vi.kind == MT_LAMBERTIAN || vi.kind == MT_ISOTROPIC);
         if (cont) {
           depth++;
         } else {
@@ -764,27 +760,34 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
     }
     const unsigned rs = warp_append(want_r, rec_count);
     if (want_r) {
-      rslot[nrec] = rs;
-      if (rs < rec_cap) {
-        float4 *q = records + 5 * (size_t)rs;
+      const int sl = rs < rec_cap ? (int)rs : -1;
+      if (sl >= 0) {
+        float4 *q = records + 5 * (size_t)sl;
         q[0] = make_float4(vi.p.x, vi.p.y, vi.p.z, vi.rough);
         q[1] = make_float4(vi.wo.x, vi.wo.y, vi.wo.z, 0.f);
         q[2] = make_float4(vi.n.x, vi.n.y, vi.n.z, 0.f);
         q[3] = make_float4(vi.albedo.x, vi.albedo.y, vi.albedo.z, 0.f);
         q[4] = make_float4(0.f, 0.f, 0.f, 0.f);
+        pend[2 * (size_t)sl] = make_float4(Tb.x, Tb.y, Tb.z, 0.f);
+        pend[2 * (size_t)sl + 1] = make_float4(Lb.x, Lb.y, Lb.z, 0.f);
       }
-      nrec++;
+      if (rslot.w == 0) rslot.x = sl;
+      else if (rslot.w == 1) rslot.y = sl;
+      else rslot.z = sl;
+      rslot.w++;
     }
-    if (training && !alive && nrec > 0) {  // path finished: targets of its records
+    if (training && !alive && rslot.w > 0) {  // path finished: targets of its records
       const float3 Lf = de_nan(L);
-      for (int k = 0; k < nrec; k++) {
-        if (rslot[k] >= rec_cap) continue;
-        float3 tg = v3((Lf.x - rL[k].x) / rT[k].x, (Lf.y - rL[k].y) / rT[k].y, (Lf.z - rL[k].z) / rT[k].z);
+      const int slots[3] = {rslot.x, rslot.y, rslot.z};
+      for (int k = 0; k < rslot.w && k < 3; k++) {
+        if (slots[k] < 0) continue;
+        const float4 pT = pend[2 * (size_t)slots[k]], pL = pend[2 * (size_t)slots[k] + 1];
+        float3 tg = v3((Lf.x - pL.x) / pT.x, (Lf.y - pL.y) / pT.y, (Lf.z - pL.z) / pT.z);
         tg = v3(isfinite(tg.x) ? fmaxf(tg.x, 0.f) : 0.f, isfinite(tg.y) ? fmaxf(tg.y, 0.f) : 0.f,
                 isfinite(tg.z) ? fmaxf(tg.z, 0.f) : 0.f);
-        records[5 * (size_t)rslot[k] + 4] = make_float4(tg.x, tg.y, tg.z, 1.f);
+        records[5 * (size_t)slots[k] + 4] = make_float4(tg.x, tg.y, tg.z, 1.f);
       }
-      nrec = 0;
+      rslot = make_int4(-1, -1, -1, 0);
     }
   }
   if (segs) atomicAdd(&C->segments, segs);
@@ -1879,7 +1882,7 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
   auto kern = k_persistent_nrc<4>;
   TPT_CUDA(smem_optin(kern, smem));
   const int grid = grid_for(c, kern, block, smem);
-  if (wf && ((st = ensure(c->learn_pend, (size_t)n->record_cap * 2 * sizeof(float4))) != TPT_OK)) return st;
+  if ((st = ensure(c->learn_pend, (size_t)n->record_cap * 2 * sizeof(float4))) != TPT_OK) return st;
   unsigned *counts = (unsigned *)c->nrc_counts.p;  // [0] records, [1] queries
   cudaEvent_t ev[6];
   for (auto &x : ev) TPT_CUDA(cudaEventCreate(&x));
@@ -1923,7 +1926,7 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
         kern<<<grid, block, smem, c->stream>>>(S, cfg, Fc, c->counters, pass_begin + off, term,
                                               (uint32_t)n->train_stride, (float4 *)c->nrc_records.p, counts,
                                               (unsigned)n->record_cap, (float4 *)c->nrc_queries.p, counts + 1,
-                                              (unsigned)n->query_cap);
+                                              (unsigned)n->query_cap, (float4 *)c->learn_pend.p);
       }
       cudaEventRecord(ev[1], c->stream);
       unsigned q = 0;
