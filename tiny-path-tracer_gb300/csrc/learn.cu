@@ -201,51 +201,68 @@ __global__ void __launch_bounds__(WARPS * 32)
   }
 }
 
-// dW_l[o][i] += sum over rows r of dZt_l[o][r] * Ht_l[i][r], one warp per
-// (layer, 16-output tile, chunk of `chunk` rows).
+// ldmatrix: four 8x8 b16 matrices from shared memory (lane l gives the
+// address of row l & 7 of matrix l >> 3).
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const __half *p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
+}
+
+// dW_l[o][i] += sum over rows r of dZt_l[o][r] * Ht_l[i][r].  One block per
+// (layer, chunk of WG_ROWS rows): the chunk of Ht_l (all inputs) and of dZt_l
+// (all outputs) is staged in shared memory with 16-byte loads (each read once
+// per block), then warp w forms output rows 16w..16w+15 with ldmatrix-fed
+// m16n8k16 MMAs and adds its tile to the f32 gradient.
+constexpr int WG_ROWS = 256, WG_LD = WG_ROWS + 8;  // shared row stride (halves): conflict-free ldmatrix
+
+__host__ __device__ inline size_t wgrad_smem(int max_in, int max_out) {
+  return (size_t)(max_in + max_out) * WG_LD * sizeof(__half);
+}
+
 template <int IN, int NH, int OUT>
-__global__ void k_mlp_wgrad(Net n, const __half *__restrict__ Ht, const __half *__restrict__ dZt, int rows,
-                            int chunk) {
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  const int warp_global = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int n_chunks = (rows + chunk - 1) / chunk;
-  // enumerate (layer, mtile, chunk)
-  int w = warp_global, layer = -1, mt = 0;
+__global__ void __launch_bounds__(128) k_mlp_wgrad(Net n, const __half *__restrict__ Ht,
+                                                   const __half *__restrict__ dZt, int rows) {
+  extern __shared__ __half wsm[];
+  const int n_chunks = (rows + WG_ROWS - 1) / WG_ROWS;
+  const int layer = blockIdx.x / n_chunks, ck = blockIdx.x - layer * n_chunks;
+  if (layer > NH) return;
+  const int K = layer == 0 ? IN : HID;   // layer inputs
+  const int N = layer == NH ? OUT : HID;  // layer outputs
   size_t ht_off = 0, dz_off = 0;
-  for (int l = 0; l <= NH; l++) {
-    const int N = l == NH ? OUT : HID;
-    const int units = (N / 16) * n_chunks;
-    if (w < units) {
-      layer = l;
-      mt = w / n_chunks;
-      w -= mt * n_chunks;
-      break;
-    }
-    w -= units;
+  for (int l = 0; l < layer; l++) {
     ht_off += (size_t)(l == 0 ? IN : HID) * rows;
-    dz_off += (size_t)N * rows;
+    dz_off += (size_t)(l == NH ? OUT : HID) * rows;
   }
-  if (layer < 0) return;
-  const int K = layer == 0 ? IN : HID;  // layer input width (GEMM N dimension)
-  const int ck = w;
-  const int k_begin = ck * chunk, k_end = min(rows, k_begin + chunk);
-  const __half *A = dZt + dz_off + (size_t)(mt * 16) * rows;
-  const __half *B = Ht + ht_off;
+  const int r0 = ck * WG_ROWS, nr = min(WG_ROWS, rows - r0);  // nr: a multiple of 16
+  __half *sH = wsm, *sZ = wsm + (size_t)K * WG_LD;
+  // stage: row q of (Ht | dZt) holds chunk rows r0 .. r0+nr of input (output) q
+  const int vec = nr / 8;  // 16-byte pieces per row
+  for (int idx = threadIdx.x; idx < (K + N) * vec; idx += blockDim.x) {
+    const int q = idx / vec, v = idx - q * vec;
+    const __half *src = q < K ? Ht + ht_off + (size_t)q * rows + r0 + v * 8
+                              : dZt + dz_off + (size_t)(q - K) * rows + r0 + v * 8;
+    __half *dst = (q < K ? sH + (size_t)q * WG_LD : sZ + (size_t)(q - K) * WG_LD) + v * 8;
+    *reinterpret_cast<uint4 *>(dst) = __ldg(reinterpret_cast<const uint4 *>(src));
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  if (warp * 16 >= N) return;
+  const int o0 = warp * 16;
   float acc[MAX_IN / 8][4];
 #pragma unroll
   for (int j = 0; j < MAX_IN / 8; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-  for (int k0 = k_begin; k0 < k_end; k0 += 16) {
-    const __half *ra = A + (size_t)g * rows + k0 + 2 * t;
-    const uint32_t a0 = *reinterpret_cast<const uint32_t *>(ra);
-    const uint32_t a1 = *reinterpret_cast<const uint32_t *>(ra + 8 * (size_t)rows);
-    const uint32_t a2 = *reinterpret_cast<const uint32_t *>(ra + 8);
-    const uint32_t a3 = *reinterpret_cast<const uint32_t *>(ra + 8 * (size_t)rows + 8);
+  for (int k0 = 0; k0 < nr; k0 += 16) {
+    uint32_t a[4];  // dZ^T tile: rows o0.., columns (chunk rows) k0..
+    ldsm_x4(a, sZ + (size_t)(o0 + (lane & 7) + ((lane >> 3) & 1) * 8) * WG_LD + k0 + (lane >> 4) * 8);
 #pragma unroll
-    for (int j = 0; j < MAX_IN / 8; j++) {
-      if (j < K / 8) {
-        const __half *rb = B + (size_t)(j * 8 + g) * rows + k0 + 2 * t;
-        mma16816(acc[j], a0, a1, a2, a3, *reinterpret_cast<const uint32_t *>(rb),
-                 *reinterpret_cast<const uint32_t *>(rb + 8));
+    for (int j = 0; j < MAX_IN / 8; j += 2) {
+      if (j < K / 8) {  // B fragments of input tiles j, j+1 (rows i of Ht, columns k0..)
+        uint32_t b[4];
+        ldsm_x4(b, sH + (size_t)(j * 8 + (lane & 7) + (lane >> 4) * 8) * WG_LD + k0 + ((lane >> 3) & 1) * 8);
+        mma16816(acc[j], a[0], a[1], a[2], a[3], b[0], b[1]);
+        mma16816(acc[j + 1], a[0], a[1], a[2], a[3], b[2], b[3]);
       }
     }
   }
@@ -253,11 +270,11 @@ __global__ void k_mlp_wgrad(Net n, const __half *__restrict__ Ht, const __half *
 #pragma unroll
   for (int j = 0; j < MAX_IN / 8; j++) {
     if (j < K / 8) {
-      const int o0 = mt * 16 + g, i0 = j * 8 + 2 * t;
-      atomicAdd(G + (size_t)o0 * K + i0, acc[j][0]);
-      atomicAdd(G + (size_t)o0 * K + i0 + 1, acc[j][1]);
-      atomicAdd(G + (size_t)(o0 + 8) * K + i0, acc[j][2]);
-      atomicAdd(G + (size_t)(o0 + 8) * K + i0 + 1, acc[j][3]);
+      const int oo = o0 + g, i0 = j * 8 + 2 * t;
+      atomicAdd(G + (size_t)oo * K + i0, acc[j][0]);
+      atomicAdd(G + (size_t)oo * K + i0 + 1, acc[j][1]);
+      atomicAdd(G + (size_t)(oo + 8) * K + i0, acc[j][2]);
+      atomicAdd(G + (size_t)(oo + 8) * K + i0 + 1, acc[j][3]);
     }
   }
 }
@@ -289,16 +306,27 @@ __global__ void k_adam(int count, float *__restrict__ w32, __half *__restrict__ 
 // pre-activation, mean direction xyz), 40 values padded to 48.
 constexpr int GUIDE_IN = 112, GUIDE_NH = 3, GUIDE_OUT = 48, GUIDE_LOBES = 8, BLOB_BINS = 32;
 
+// A row of N halves built in registers (fully unrolled encoders), written
+// to a 16-byte-aligned row with 16-byte stores.
+template <int N>
+__device__ __forceinline__ void store_row(const __half (&buf)[N], __half *dst) {
+  static_assert(N % 8 == 0, "rows are whole 16-byte chunks");
+#pragma unroll
+  for (int i = 0; i < N / 8; i++) reinterpret_cast<uint4 *>(dst)[i] = reinterpret_cast<const uint4 *>(buf)[i];
+}
+
 __device__ __forceinline__ void guide_encode(float3 xn, float3 n, __half *out) {
   const float c[3] = {xn.x, xn.y, xn.z};
 #pragma unroll
   for (int a = 0; a < 3; a++) {
     const float u = fminf(fmaxf(c[a], 0.f), 1.f) * BLOB_BINS;
+#pragma unroll
     for (int b = 0; b < BLOB_BINS; b++) out[a * BLOB_BINS + b] = __float2half_rn(fmaxf(0.f, 1.f - fabsf(u - (b + 0.5f))));
   }
   out[96] = __float2half_rn(n.x);
   out[97] = __float2half_rn(n.y);
   out[98] = __float2half_rn(n.z);
+#pragma unroll
   for (int i = 99; i < GUIDE_IN; i++) out[i] = __float2half_rn(0.f);
 }
 
@@ -384,7 +412,9 @@ __global__ void k_guide_encode_records(const float4 *__restrict__ rec, int count
       nn = dd = make_float4(0.f, 0.f, 1.f, 0.f);
     }
     const float3 xn = make_float3((xw.x - lo.x) * inv_ext.x, (xw.y - lo.y) * inv_ext.y, (xw.z - lo.z) * inv_ext.z);
-    guide_encode(xn, make_float3(nn.x, nn.y, nn.z), X + (size_t)r * GUIDE_IN);
+    __align__(16) __half row[GUIDE_IN];
+    guide_encode(xn, make_float3(nn.x, nn.y, nn.z), row);
+    store_row(row, X + (size_t)r * GUIDE_IN);
     target[r] = make_float4(dd.x, dd.y, dd.z, xw.w);
     part += xw.w;
   }
@@ -405,7 +435,9 @@ __global__ void k_guide_encode_grid(int res, int rows_valid, int rows, __half *_
     const float3 xn = make_float3((cx + 0.5f) / res, (cy + 0.5f) / res, (cz + 0.5f) / res);
     const float sgn = (bin & 1) ? -1.f : 1.f;
     const float3 n = make_float3(bin / 2 == 0 ? sgn : 0.f, bin / 2 == 1 ? sgn : 0.f, bin / 2 == 2 ? sgn : 0.f);
-    guide_encode(xn, n, out);
+    __align__(16) __half row[GUIDE_IN];
+    guide_encode(xn, n, row);
+    store_row(row, out);
   }
 }
 
@@ -479,9 +511,11 @@ __device__ __forceinline__ __half fin16(float v) {  // non-finite features encod
 
 // One-blob encoding (Mueller et al., "Neural Importance Sampling", ACM TOG
 // 2019) of u in [0,1] over `bins` bins with a triangular kernel one bin wide.
-__device__ __forceinline__ void one_blob(float u, int bins, __half *out) {
-  const float x = fminf(fmaxf(u, 0.f), 1.f) * bins;  // NaN -> 0
-  for (int b = 0; b < bins; b++) out[b] = __float2half_rn(fmaxf(0.f, 1.f - fabsf(x - (b + 0.5f))));
+template <int BINS>
+__device__ __forceinline__ void one_blob(float u, __half *out) {
+  const float x = fminf(fmaxf(u, 0.f), 1.f) * BINS;  // NaN -> 0
+#pragma unroll
+  for (int b = 0; b < BINS; b++) out[b] = __float2half_rn(fmaxf(0.f, 1.f - fabsf(x - (b + 0.5f))));
 }
 
 // Unit direction -> spherical (theta, phi) in [0,1]^2, one-blob 4 + 4.
@@ -489,8 +523,8 @@ __device__ __forceinline__ void dir_blob(float3 d, __half *out) {
   const float th = acosf(fminf(fmaxf(d.z, -1.f), 1.f)) * 0.318309886183790671538f;
   float ph = atan2f(d.y, d.x) * 0.159154943091895335769f;
   ph = ph < 0.f ? ph + 1.f : ph;
-  one_blob(th, 4, out);
-  one_blob(ph, 4, out + 4);
+  one_blob<4>(th, out);
+  one_blob<4>(ph, out + 4);
 }
 
 // Cache input (Mueller et al., "Real-time Neural Radiance Caching for Path
@@ -503,6 +537,7 @@ __device__ __forceinline__ void nrc_encode(const float4 *f, float3 lo, float3 in
   for (int a = 0; a < 3; a++) {
     const float x = isfinite(c[a]) ? fminf(fmaxf(c[a], 0.f), 1.f) : 0.f;
     float s = x;
+#pragma unroll
     for (int k = 0; k < 12; k++, s *= 2.f) {
       const float fr = s - floorf(s);
       out[a * 12 + k] = __float2half_rn(fabsf(2.f * fr - 1.f));
@@ -511,10 +546,11 @@ __device__ __forceinline__ void nrc_encode(const float4 *f, float3 lo, float3 in
   const float3 wo = make_float3(f[1].x, f[1].y, f[1].z), n = make_float3(f[2].x, f[2].y, f[2].z);
   dir_blob(wo, out + 36);
   dir_blob(n, out + 44);
-  one_blob(f[0].w, 4, out + 52);
+  one_blob<4>(f[0].w, out + 52);
   out[56] = fin16(f[3].x);
   out[57] = fin16(f[3].y);
   out[58] = fin16(f[3].z);
+#pragma unroll
   for (int i = 59; i < NRC_IN; i++) out[i] = __float2half_rn(0.f);
 }
 
@@ -546,7 +582,9 @@ __global__ void k_nrc_encode_records(const float4 *__restrict__ rec, int count, 
     uint32_t h = (uint32_t)r * 0x9E3779B1u ^ (step * 0x85EBCA77u) ^ key;
     h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12; h *= 0x297A2D39u; h ^= h >> 15;
     const int idx = (int)(h % (uint32_t)count);
-    nrc_encode(rec + 5 * (size_t)idx, lo, inv_ext, X + (size_t)r * NRC_IN);
+    __align__(16) __half row[NRC_IN];
+    nrc_encode(rec + 5 * (size_t)idx, lo, inv_ext, row);
+    store_row(row, X + (size_t)r * NRC_IN);
     const float4 t = rec[5 * (size_t)idx + 4];
     target[r] = finite4(t) ? t : make_float4(0.f, 0.f, 0.f, 0.f);
   }
@@ -560,7 +598,9 @@ __global__ void k_nrc_encode_queries(const float4 *__restrict__ q, int count, in
       for (int i = 0; i < NRC_IN; i++) out[i] = __float2half_rn(0.f);
       continue;
     }
-    nrc_encode(q + 6 * (size_t)r, lo, inv_ext, out);
+    __align__(16) __half row[NRC_IN];
+    nrc_encode(q + 6 * (size_t)r, lo, inv_ext, row);
+    store_row(row, out);
   }
 }
 
@@ -635,11 +675,10 @@ tpt_status launch_train(tpt_mlp *M, const __half *x, int rows, const Loss &loss,
   MLP_CUDA(cudaMemsetAsync(M->loss, 0, sizeof(float), s));
   k_mlp_train<IN, NH, OUT, Loss><<<grid, WARPS * 32, smem, s>>>(M->net, x, rows, loss, M->ht, M->dzt, M->loss);
   MLP_CUDA(cudaGetLastError());
-  const int chunk = 256;  // rows per weight-gradient warp: ~1000 warps for a 16384-row batch
-  const int n_chunks = (rows + chunk - 1) / chunk;
-  int units = 0;
-  for (int l = 0; l <= NH; l++) units += ((l == NH ? OUT : HID) / 16) * n_chunks;
-  k_mlp_wgrad<IN, NH, OUT><<<(units + 3) / 4, 128, 0, s>>>(M->net, M->ht, M->dzt, rows, chunk);
+  const int n_chunks = (rows + WG_ROWS - 1) / WG_ROWS;
+  const size_t wsm = wgrad_smem(IN > HID ? IN : HID, OUT > HID ? OUT : HID);
+  MLP_CUDA(cudaFuncSetAttribute(k_mlp_wgrad<IN, NH, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
+  k_mlp_wgrad<IN, NH, OUT><<<(NH + 1) * n_chunks, 128, wsm, s>>>(M->net, M->ht, M->dzt, rows);
   return mlp_cuda(cudaGetLastError());
 }
 

@@ -82,17 +82,25 @@ __device__ __forceinline__ float2 unpack2(uint32_t v) {
 }
 
 // Copies all weights into shared memory (row stride in+8) and, if `wt`,
-// the transposed hidden/output layers (row stride out+8).
+// the transposed hidden/output layers (row stride out+8).  16-byte loads:
+// every layer's row length and offset are multiples of 8 halves, and the
+// padded shared rows keep 16-byte alignment.
 __device__ inline void load_weights(const Net &n, __half *sw, __half *swt) {
   for (int l = 0; l < n_layers(n); l++) {
     const int K = layer_in(n, l), N = layer_out(n, l);
-    const __half *g = n.w16 + layer_offset(n, l);
+    const uint4 *g = reinterpret_cast<const uint4 *>(n.w16 + layer_offset(n, l));
     __half *s = sw + smem_w_offset(n, l);
-    for (int i = threadIdx.x; i < N * K; i += blockDim.x) {
-      const int o = i / K, k = i - o * K;
-      const __half v = g[i];
-      s[o * (K + 8) + k] = v;
-      if (swt && l > 0) swt[smem_wt_offset(n, l) + k * (N + 8) + o] = v;
+    const int chunks = N * K / 8;
+    for (int c = threadIdx.x; c < chunks; c += blockDim.x) {
+      const int i = c * 8, o = i / K, k = i - o * K;  // 8 consecutive inputs of output o
+      const uint4 v = __ldg(g + c);
+      *reinterpret_cast<uint4 *>(s + o * (K + 8) + k) = v;
+      if (swt && l > 0) {
+        const __half *h = reinterpret_cast<const __half *>(&v);
+        __half *t = swt + smem_wt_offset(n, l) + o;
+#pragma unroll
+        for (int j = 0; j < 8; j++) t[(k + j) * (N + 8)] = h[j];
+      }
     }
   }
 }
