@@ -379,7 +379,7 @@ tpt_status tpt_guide_records(tpt_context *ctx, float *out, int64_t cap, int64_t 
  * fallback and the yardstick for that error. */
 typedef struct {
   int32_t passes;           /* >= 1 (8) */
-  int32_t train_steps;      /* Adam steps after each pass (128) */
+  int32_t train_steps;      /* Adam steps after each pass (256) */
   int32_t batch;            /* training rows per step (16384) */
   float lr;                 /* Adam learning rate (3e-3) */
   int32_t terminate_depth;  /* 2: two bounces, then the cache */

@@ -70,3 +70,26 @@ def test_guided_gains_at_equal_spp(ctx):
     # what the trained guide gains over the plain mixture: lower error per sample
     assert np.mean(guided) < 0.95 * np.mean(plain)
     ctx.release(slot)
+
+
+def test_guided_argument_errors(built):
+    import ctypes as C
+
+    ctx = tpt.Context(0)
+    assert len(tpt.guide_records(ctx)) == 0  # nothing rendered yet
+    slot = ctx.upload(tpt.Scene(scenes.cornell_guiding().text()))
+    img = np.zeros((8, 8, 3), np.float32)
+    g = tpt.GuideParams()
+    tpt.lib().tpt_guide_params_default(C.byref(g))
+    p = tpt.make_params(8, 8, 4, 50, tpt.SEMANTICS_REFERENCE)  # guiding needs physical semantics
+    st = tpt.lib().tpt_render_guided(ctx._h, slot, C.byref(p), C.byref(g), img.ctypes.data_as(C.c_void_p),
+                                     tpt.TPT_MEM_HOST, None, None)
+    assert st == 1
+    p = tpt.make_params(8, 8, 4, 50, tpt.SEMANTICS_PHYSICAL)
+    for field, bad in (("passes", 0), ("grid_res", 65), ("alpha", 1.5), ("batch", 8)):
+        g2 = tpt.GuideParams()
+        tpt.lib().tpt_guide_params_default(C.byref(g2))
+        setattr(g2, field, bad)
+        assert tpt.lib().tpt_render_guided(ctx._h, slot, C.byref(p), C.byref(g2), img.ctypes.data_as(C.c_void_p),
+                                           tpt.TPT_MEM_HOST, None, None) == 1, field
+    ctx.close()

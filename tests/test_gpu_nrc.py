@@ -60,3 +60,19 @@ def test_cached_render_gains_at_equal_spp(ctx):
     # what the trained cache gains: lower error than the plain tracer at equal spp
     assert r < plain
     ctx.release(slot)
+
+
+def test_nrc_argument_errors(ctx):
+    import ctypes as C
+
+    slot = _slot(ctx)
+    img = np.zeros((8, 8, 3), np.float32)
+    p = tpt.make_params(8, 8, 4, 50, tpt.SEMANTICS_PHYSICAL)
+    for field, bad in (("passes", 0), ("terminate_depth", -1), ("train_stride", 0), ("query_cap", 16),
+                       ("batch", 8)):
+        n = tpt.NrcParams()
+        tpt.lib().tpt_nrc_params_default(C.byref(n))
+        setattr(n, field, bad)
+        assert tpt.lib().tpt_render_nrc(ctx._h, slot, C.byref(p), C.byref(n), img.ctypes.data_as(C.c_void_p),
+                                        tpt.TPT_MEM_HOST, None, None) == 1, field
+    ctx.release(slot)

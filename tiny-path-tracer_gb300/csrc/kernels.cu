@@ -1778,8 +1778,12 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
       result = guide_train(c->guide, (const float4 *)c->guide_records.p, (int)count, g->train_steps, g->batch, g->lr,
                            lo, ext, g->seed + 7919ull * (pass + 1), c->stream);
       if (result == TPT_OK) result = guide_refresh(c->guide, g->grid_res, (float4 *)c->guide_table.p, c->stream);
+      if (result != TPT_OK) break;
       cudaEventRecord(e[3], c->stream);
-      cudaStreamSynchronize(c->stream);
+      if ((ce = cudaStreamSynchronize(c->stream)) != cudaSuccess) {
+        result = cuda_status(ce);
+        break;
+      }
       cudaEventElapsedTime(&ms, e[2], e[3]);
       train_ms += ms;
       have_table = true;
@@ -1834,7 +1838,7 @@ extern "C" tpt_status tpt_guide_records(tpt_context *c, float *out, int64_t cap,
 extern "C" void tpt_nrc_params_default(tpt_nrc_params *n) {
   if (!n) return;
   n->passes = 8;
-  n->train_steps = 128;
+  n->train_steps = 256;
   n->batch = 16384;
   n->lr = 3e-3f;
   n->terminate_depth = 2;
@@ -1956,23 +1960,34 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
         const int g2 = (int)std::min<unsigned>((q + 255) / 256, (unsigned)c->sm_count * 16);
         k_nrc_accumulate<<<g2, 256, 0, c->stream>>>((const float4 *)c->nrc_queries.p, y, (int)q, F);
         cudaEventRecord(ev[3], c->stream);
-        cudaStreamSynchronize(c->stream);
+        if ((ce = cudaStreamSynchronize(c->stream)) != cudaSuccess) {
+          result = cuda_status(ce);
+          break;
+        }
         cudaEventElapsedTime(&ms, ev[2], ev[3]);
         infer_ms += ms;
       }
     }
     if (result != TPT_OK) break;
     unsigned nr = 0;
-    cudaMemcpyAsync(&nr, counts, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
-    cudaStreamSynchronize(c->stream);
+    cudaError_t ce = cudaMemcpyAsync(&nr, counts, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(c->stream);
+    if (ce != cudaSuccess) {
+      result = cuda_status(ce);
+      break;
+    }
     nr = std::min<unsigned>(nr, (unsigned)n->record_cap);
     n_rec += nr;
     if (pass + 1 < n->passes && nr > 0) {
       cudaEventRecord(ev[4], c->stream);
       result = cache_train(c->cache, (const float4 *)c->nrc_records.p, (int)nr, n->train_steps, n->batch, n->lr, lo,
                            ext, (uint32_t)(n->seed * 2654435761ull + pass), c->stream);
+      if (result != TPT_OK) break;
       cudaEventRecord(ev[5], c->stream);
-      cudaStreamSynchronize(c->stream);
+      if ((ce = cudaStreamSynchronize(c->stream)) != cudaSuccess) {
+        result = cuda_status(ce);
+        break;
+      }
       float ms = 0.f;
       cudaEventElapsedTime(&ms, ev[4], ev[5]);
       train_ms += ms;
