@@ -90,6 +90,7 @@ struct DevScene {
   int32_t light_is_list;  // 0: single light_shape hitable; 1: hitable_list
   int32_t has_lights;
   int32_t flat_max;  // BVH items of at most this many nodes use the stackless walk
+  int32_t feat;      // FEAT_* (device.cuh): the leaf kinds present, for kernel specialisation
   Camera cam;
 };
 

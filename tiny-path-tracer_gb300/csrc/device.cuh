@@ -296,12 +296,18 @@ __device__ __forceinline__ void to_world(const f4 *data, int nops, float3 &p, fl
 
 // Candidate of a geometric primitive leaf (sphere, moving sphere, rect,
 // box).  face: box face or -1.
+// Scene feature sets the traversal can be specialised for: every leaf kind
+// (the general case), or spheres only (no rects, boxes, moving spheres,
+// instances or media), whose kernels carry none of that code.
+enum { FEAT_ALL = 0, FEAT_SPHERES = 1 };
+
+template <int FEAT = FEAT_ALL>
 __device__ __forceinline__ bool prim_t(const DevScene &S, const i4 &h, const Ray &r, float3 inv, float tmin,
                                        float tmax, float &t, int &face) {
   const f4 *d = S.leaf_data + h.y;
   int type = h.x & LEAF_TYPE_MASK;
   face = -1;
-  if (type == LT_SPHERE) {
+  if (FEAT == FEAT_SPHERES || type == LT_SPHERE) {
     f4 s = ldg4(d);
     return sphere_t(f3(s), s.w, r, tmin, tmax, t);
   }
@@ -389,6 +395,7 @@ enum { FLAT_PRUNE_MIN = 32 };
 // (t, -leaf order), and a subtree is skipped only when the lower bound
 // prune_key() on any t its primitives can report exceeds the best t.  stk: this thread's stack slots, `stride`
 // entries apart.  err receives TPT_ERR_STACK_OVERFLOW on overflow.
+template <int FEAT = FEAT_ALL>
 __device__ bool trace_closest(const DevScene &S, const Ray &wr, float tmin, int2 *stk, int stride,
                               const MediumRng &mrng, HitRef &res, int &err) {
   const RayPre W = precompute(wr);
@@ -419,7 +426,7 @@ __device__ bool trace_closest(const DevScene &S, const Ray &wr, float tmin, int2
       while (sp > 0 && !overflow) {
         --sp;
         const int2 e = stk[sp * stride];
-        if (e.x == STK_RESTORE) {
+        if (FEAT != FEAT_SPHERES && e.x == STK_RESTORE) {
           cur = wr;
           curp = W;
           cur_inst = -1;
@@ -432,7 +439,7 @@ __device__ bool trace_closest(const DevScene &S, const Ray &wr, float tmin, int2
           const int type = h.x & LEAF_TYPE_MASK;
           float t;
           int face = -1;
-          if (type == LT_INSTANCE) {
+          if (FEAT != FEAT_SPHERES && type == LT_INSTANCE) {
             const f4 *d = S.leaf_data + h.y;
             const Ray o = to_object(d, (int)ldg4(d).x, wr);
             const RayPre op = precompute(o);
@@ -457,10 +464,10 @@ __device__ bool trace_closest(const DevScene &S, const Ray &wr, float tmin, int2
           const int outer = cur_inst >= 0 ? cur_inst : leaf;
           const int inner = cur_inst >= 0 ? leaf : -1;
           bool ok;
-          if (type == LT_MEDIUM)
+          if (FEAT != FEAT_SPHERES && type == LT_MEDIUM)
             ok = medium_t(S, h, cur, tmin, tmax, medium_u(mrng, S.leaf_user[leaf]), t);
           else
-            ok = prim_t(S, h, cur, curp.inv, tmin, tmax, t, face);
+            ok = prim_t<FEAT>(S, h, cur, curp.inv, tmin, tmax, t, face);
           if (ok && beats(t, outer, inner, bt, bo, bn)) {
             bt = t; bl = leaf; bi = cur_inst; bf = face; bo = outer; bn = inner;
           }

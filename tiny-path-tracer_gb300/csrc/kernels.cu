@@ -119,6 +119,7 @@ __device__ __forceinline__ void write_path(const PathBuf &B, unsigned idx, const
 // ---------------------------------------------------------------- kernels -
 
 // Batched world->hit for the parity boundary (tpt_trace_closest).
+template <int FEAT>
 __global__ void k_trace_closest(DevScene S, const float *__restrict__ rays, long long n, uint2 key,
                                 float *__restrict__ hit_f, int *__restrict__ hit_i, int *err) {
   extern __shared__ int2 stack_smem[];
@@ -130,7 +131,7 @@ __global__ void k_trace_closest(DevScene S, const float *__restrict__ rays, long
     MediumRng m{make_uint4((uint32_t)k, (uint32_t)(k >> 32), 0u, 0x4d454449u), key, 0};
     HitRef h;
     float *o = hit_f + 9 * k;
-    if (trace_closest(S, r, 0.001f, stk, blockDim.x, m, h, e)) {
+    if (trace_closest<FEAT>(S, r, 0.001f, stk, blockDim.x, m, h, e)) {
       Surface sf;
       finalize(S, r, h, sf);
       o[0] = h.t; o[1] = sf.u; o[2] = sf.v;
@@ -161,6 +162,7 @@ __global__ void k_wf_generate(DevScene S, FrameDesc F, PathBuf out, unsigned lon
 
 // Closest hit for every live path of buffer `cur`; also clears the append
 // counter of the other buffer for the following shade pass.
+template <int FEAT = FEAT_ALL>
 __global__ void k_wf_traverse(DevScene S, PathBuf in, int cur, WfCounters *C, int4 *__restrict__ hits, uint2 key) {
   extern __shared__ int2 stack_smem[];
   int2 *stk = stack_smem + threadIdx.x;
@@ -177,7 +179,7 @@ __global__ void k_wf_traverse(DevScene S, PathBuf in, int cur, WfCounters *C, in
     MediumRng m{make_uint4((uint32_t)__float_as_int(tp.w), (uint32_t)__float_as_int(rs.w),
                            (uint32_t)__float_as_int(dd.w), 0u), key, 1};
     HitRef h;
-    if (trace_closest(S, r, 0.001f, stk, blockDim.x, m, h, e))
+    if (trace_closest<FEAT>(S, r, 0.001f, stk, blockDim.x, m, h, e))
       hits[k] = make_int4(__float_as_int(h.t), h.leaf, h.inst, h.face);
     else
       hits[k] = make_int4(0, -1, -1, -1);
@@ -449,7 +451,7 @@ __global__ void k_wf_shade_learn(DevScene S, RenderCfg cfg, FrameDesc F, PathBuf
 // path ends it accumulates and claims the next camera sample (one atomic per
 // warp for all lanes that need one), so lanes do not idle behind the longest
 // path of their warp.
-template <int MIN_BLOCKS>
+template <int MIN_BLOCKS, int FEAT = FEAT_ALL>
 __global__ void __launch_bounds__(128, MIN_BLOCKS) k_persistent(DevScene S, RenderCfg cfg, FrameDesc F, WfCounters *C) {
   extern __shared__ int2 stack_smem[];
   int2 *stk = stack_smem + threadIdx.x;
@@ -485,7 +487,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS) k_persistent(DevScene S, Rend
     if (alive) {
       MediumRng m{make_uint4(pixel, sample, (uint32_t)depth, 0u), cfg.key, 1};
       HitRef h;
-      const bool hit = trace_closest(S, r, 0.001f, stk, blockDim.x, m, h, e);
+      const bool hit = trace_closest<FEAT>(S, r, 0.001f, stk, blockDim.x, m, h, e);
       segs++;
       if (shade_vertex(S, cfg, r, hit, h, T, L, depth, pixel, sample)) {
         depth++;
@@ -509,7 +511,7 @@ struct BatchItem {
   unsigned long long first;
 };
 
-template <int MIN_BLOCKS>
+template <int MIN_BLOCKS, int FEAT = FEAT_ALL>
 __global__ void __launch_bounds__(128, MIN_BLOCKS)
     k_persistent_batch(const BatchItem *__restrict__ items, int n_items, unsigned long long total_all, RenderCfg cfg,
                        WfCounters *C) {
@@ -558,7 +560,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
       const DevScene &S = items[item].scene;
       MediumRng m{make_uint4(pixel, sample, (uint32_t)depth, 0u), cfg.key, 1};
       HitRef h;
-      const bool hit = trace_closest(S, r, 0.001f, stk, blockDim.x, m, h, e);
+      const bool hit = trace_closest<FEAT>(S, r, 0.001f, stk, blockDim.x, m, h, e);
       segs++;
       if (shade_vertex(S, cfg, r, hit, h, T, L, depth, pixel, sample)) {
         depth++;
@@ -1008,6 +1010,9 @@ static DevScene dev_scene_at(const HostScene &S, const ArenaLayout &L, uint8_t *
   d.light_f = (const f4 *)(base + L.off[15]);
   d.node_kids = (const f4 *)(base + L.off[16]);
   d.flat_max = DEFAULT_FLAT_MAX;
+  d.feat = FEAT_SPHERES;
+  for (const i4 &h : S.leaf_hdr)
+    if ((h.x & LEAF_TYPE_MASK) != LT_SPHERE) d.feat = FEAT_ALL;
   d.n_nodes = (int32_t)S.node_lo.size();
   d.n_leaves = (int32_t)S.leaf_hdr.size();
   d.n_items = (int32_t)S.items.size();
@@ -1093,12 +1098,13 @@ tpt_status tpt_trace_closest(tpt_context *c, int32_t slot, const float *rays, in
   const int block = 128, smem = stack_smem(block);
   DevScene ds = c->slots[slot].ds;
   ds.flat_max = c->flat_nodes;
-  int grid = grid_for(c, k_trace_closest, block, smem);
+  // the same specialisation the renders of this scene use
+  auto kern = ds.feat == FEAT_SPHERES ? k_trace_closest<FEAT_SPHERES> : k_trace_closest<FEAT_ALL>;
+  int grid = grid_for(c, kern, block, smem);
   const long long need = (n + block - 1) / block;
   if (grid > need) grid = (int)need;
-  k_trace_closest<<<grid, block, smem, c->stream>>>(ds, d_rays, n,
-                                                   make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)), d_f, d_i,
-                                                   c->err);
+  kern<<<grid, block, smem, c->stream>>>(ds, d_rays, n, make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)), d_f, d_i,
+                                         c->err);
   TPT_CUDA(cudaGetLastError());
   int herr = 0;
   TPT_CUDA(cudaMemcpyAsync(&herr, c->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -1153,7 +1159,8 @@ static tpt_status run_wavefront_t(tpt_context *c, const DevScene &S, const Rende
   std::memcpy(c->counters_host, &init, sizeof(init));
   TPT_CUDA(cudaMemcpyAsync(c->counters, c->counters_host, sizeof(WfCounters), cudaMemcpyHostToDevice, c->stream));
   const int smem = stack_smem(block);
-  TPT_CUDA(smem_optin(k_wf_traverse, smem));
+  auto traverse = S.feat == FEAT_SPHERES ? k_wf_traverse<FEAT_SPHERES> : k_wf_traverse<FEAT_ALL>;
+  TPT_CUDA(smem_optin(traverse, smem));
   const int g_gen = std::max(1, std::min<int>((int)((first + block - 1) / block), c->sm_count * 8));
   if constexpr (MODE == 0)
     k_wf_generate<<<g_gen, block, 0, c->stream>>>(S, F, P[0], 0ull, first, cfg.key);
@@ -1161,7 +1168,7 @@ static tpt_status run_wavefront_t(tpt_context *c, const DevScene &S, const Rende
     k_wf_generate_learn<<<g_gen, block, 0, c->stream>>>(S, F, P[0], first, cfg.key, *W);
   TPT_CUDA(cudaGetLastError());
   int launches = 1;
-  const int g_tr = grid_for(c, k_wf_traverse, block, smem);
+  const int g_tr = grid_for(c, traverse, block, smem);
   const int g_sh = MODE == 0 ? grid_for(c, k_wf_shade, block, 0) : grid_for(c, k_wf_shade_learn<MODE == 0 ? 1 : MODE>, block, 0);
   // iteration bound: every sample lives at most max_depth+1 segments
   const unsigned long long max_iters = (F.total * (unsigned long long)(cfg.max_depth + 1)) / wave + 64;
@@ -1178,7 +1185,7 @@ static tpt_status run_wavefront_t(tpt_context *c, const DevScene &S, const Rende
   for (int it = 0; it < kIters; it++) {
     const int cur = it & 1;
     if (profile) cudaEventRecordWithFlags(c->prof_ev[3 * it], c->stream, cudaEventRecordExternal);
-    k_wf_traverse<<<g_tr, block, smem, c->stream>>>(S, P[cur], cur, c->counters, (int4 *)c->hits.p, cfg.key);
+    traverse<<<g_tr, block, smem, c->stream>>>(S, P[cur], cur, c->counters, (int4 *)c->hits.p, cfg.key);
     if (profile) cudaEventRecordWithFlags(c->prof_ev[3 * it + 1], c->stream, cudaEventRecordExternal);
     if constexpr (MODE == 0)
       k_wf_shade<<<g_sh, block, 0, c->stream>>>(S, cfg, F, P[cur], P[cur ^ 1], cur, c->counters,
@@ -1235,7 +1242,14 @@ static tpt_status run_wavefront(tpt_context *c, const DevScene &S, const RenderC
 // Register-capped variants of the persistent kernel (occupancy vs spills),
 // selected by tpt_render_params.wave when the persistent engine runs.
 typedef void (*PersistentKernel)(DevScene, RenderCfg, FrameDesc, WfCounters *);
-static PersistentKernel persistent_variant(int v) {
+static PersistentKernel persistent_variant(int v, int feat = FEAT_ALL) {
+  if (feat == FEAT_SPHERES) {  // sphere-only scenes: the traversal without the other leaf kinds
+    switch (v) {
+      case 5: return k_persistent<5, FEAT_SPHERES>;
+      case 6: return k_persistent<6, FEAT_SPHERES>;
+      default: return k_persistent<4, FEAT_SPHERES>;
+    }
+  }
   switch (v) {
     case 5: return k_persistent<5>;
     case 6: return k_persistent<6>;
@@ -1254,7 +1268,7 @@ static tpt_status run_persistent(tpt_context *c, const DevScene &S, const Render
   std::memcpy(c->counters_host, &init, sizeof(init));
   TPT_CUDA(cudaMemcpyAsync(c->counters, c->counters_host, sizeof(WfCounters), cudaMemcpyHostToDevice, c->stream));
   const int smem = stack_smem(block);
-  const PersistentKernel kern = persistent_variant(variant);
+  const PersistentKernel kern = persistent_variant(variant, S.feat);
   if (block > 128) return TPT_ERR_INVALID_ARGUMENT;  // launch bounds of the variants
   TPT_CUDA(smem_optin(kern, smem));
   const int grid = grid_for(c, kern, block, smem);
@@ -1357,7 +1371,14 @@ static uint64_t fnv1a(uint64_t h, const void *data, size_t n) {
 }
 
 typedef void (*BatchKernel)(const BatchItem *, int, unsigned long long, RenderCfg, WfCounters *);
-static BatchKernel batch_variant(int v) {
+static BatchKernel batch_variant(int v, int feat = FEAT_ALL) {
+  if (feat == FEAT_SPHERES) {  // every item sphere-only
+    switch (v) {
+      case 5: return k_persistent_batch<5, FEAT_SPHERES>;
+      case 6: return k_persistent_batch<6, FEAT_SPHERES>;
+      default: return k_persistent_batch<4, FEAT_SPHERES>;
+    }
+  }
   switch (v) {
     case 5: return k_persistent_batch<5>;
     case 6: return k_persistent_batch<6>;
@@ -1471,7 +1492,10 @@ extern "C" tpt_status tpt_render_batch(tpt_context *c, const tpt_batch_item *ite
   key = fnv1a(key, &p->wave, sizeof(p->wave));
   key = fnv1a(key, &mem, sizeof(mem));
   for (int k = 0; k < n; k++) key = fnv1a(key, &items[k].out_rgb, sizeof(float *));
-  const BatchKernel kern = batch_variant(p->wave);
+  int feat = FEAT_SPHERES;
+  for (int k = 0; k < n; k++)
+    if (table[k].scene.feat != FEAT_SPHERES) feat = FEAT_ALL;
+  const BatchKernel kern = batch_variant(p->wave, feat);
   const int smem = stack_smem(block);
   if (!c->batch_graph || c->batch_key != key) {
     if (c->batch_graph) {
@@ -2096,7 +2120,7 @@ extern "C" tpt_status tpt_render_noalloc(const tpt_scene *scene, void *arena_dev
   const FrameDesc F{p->width, p->height, p->spp, npix * (unsigned long long)p->spp, accum, nullptr};
   const RenderCfg cfg{p->max_depth, p->semantics, p->background, p->sky_scale,
                       make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32)), p->refill > 0 ? p->refill : 1};
-  const PersistentKernel kern = persistent_variant(p->wave);
+  const PersistentKernel kern = persistent_variant(p->wave, d.feat);
   const int smem = stack_smem(block);
   TPT_CUDA(smem_optin(kern, smem));
   int per_sm = 0;
