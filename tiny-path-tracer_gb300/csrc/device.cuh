@@ -297,9 +297,10 @@ __device__ __forceinline__ void to_world(const f4 *data, int nops, float3 &p, fl
 // Candidate of a geometric primitive leaf (sphere, moving sphere, rect,
 // box).  face: box face or -1.
 // Scene feature sets the traversal can be specialised for: every leaf kind
-// (the general case), or spheres only (no rects, boxes, moving spheres,
-// instances or media), whose kernels carry none of that code.
-enum { FEAT_ALL = 0, FEAT_SPHERES = 1 };
+// (the general case), spheres only (no rects, boxes, moving spheres,
+// instances or media), or no media and no moving spheres; their kernels
+// carry none of the code of the kinds they exclude.
+enum { FEAT_ALL = 0, FEAT_SPHERES = 1, FEAT_NO_MEDIA = 2 };  // NO_MEDIA: no media, no moving spheres
 
 template <int FEAT = FEAT_ALL>
 __device__ __forceinline__ bool prim_t(const DevScene &S, const i4 &h, const Ray &r, float3 inv, float tmin,
@@ -319,7 +320,7 @@ __device__ __forceinline__ bool prim_t(const DevScene &S, const i4 &h, const Ray
     f4 p0 = ldg4(d), p1 = ldg4(d + 1);
     return box_t(f3(p0), f3(p1), r, inv, tmin, tmax, t, face);
   }
-  if (type == LT_MSPHERE) {
+  if (FEAT != FEAT_NO_MEDIA && type == LT_MSPHERE) {
     f4 d0 = ldg4(d), d1 = ldg4(d + 1), d2 = ldg4(d + 2);
     return sphere_t(msphere_center(d0, d1, d2, r.time), d0.w, r, tmin, tmax, t);
   }
@@ -464,7 +465,7 @@ __device__ bool trace_closest(const DevScene &S, const Ray &wr, float tmin, int2
           const int outer = cur_inst >= 0 ? cur_inst : leaf;
           const int inner = cur_inst >= 0 ? leaf : -1;
           bool ok;
-          if (FEAT != FEAT_SPHERES && type == LT_MEDIUM)
+          if (FEAT == FEAT_ALL && type == LT_MEDIUM)
             ok = medium_t(S, h, cur, tmin, tmax, medium_u(mrng, S.leaf_user[leaf]), t);
           else
             ok = prim_t<FEAT>(S, h, cur, curp.inv, tmin, tmax, t, face);

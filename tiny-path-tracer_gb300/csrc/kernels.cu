@@ -1010,9 +1010,13 @@ static DevScene dev_scene_at(const HostScene &S, const ArenaLayout &L, uint8_t *
   d.light_f = (const f4 *)(base + L.off[15]);
   d.node_kids = (const f4 *)(base + L.off[16]);
   d.flat_max = DEFAULT_FLAT_MAX;
-  d.feat = FEAT_SPHERES;
-  for (const i4 &h : S.leaf_hdr)
-    if ((h.x & LEAF_TYPE_MASK) != LT_SPHERE) d.feat = FEAT_ALL;
+  bool only_spheres = true, media = false;
+  for (const i4 &h : S.leaf_hdr) {
+    const int t = h.x & LEAF_TYPE_MASK;
+    only_spheres = only_spheres && t == LT_SPHERE;
+    media = media || t == LT_MEDIUM || t == LT_MSPHERE;
+  }
+  d.feat = only_spheres ? FEAT_SPHERES : (media ? FEAT_ALL : FEAT_NO_MEDIA);
   d.n_nodes = (int32_t)S.node_lo.size();
   d.n_leaves = (int32_t)S.leaf_hdr.size();
   d.n_items = (int32_t)S.items.size();
@@ -1099,7 +1103,9 @@ tpt_status tpt_trace_closest(tpt_context *c, int32_t slot, const float *rays, in
   DevScene ds = c->slots[slot].ds;
   ds.flat_max = c->flat_nodes;
   // the same specialisation the renders of this scene use
-  auto kern = ds.feat == FEAT_SPHERES ? k_trace_closest<FEAT_SPHERES> : k_trace_closest<FEAT_ALL>;
+  auto kern = ds.feat == FEAT_SPHERES   ? k_trace_closest<FEAT_SPHERES>
+              : ds.feat == FEAT_NO_MEDIA ? k_trace_closest<FEAT_NO_MEDIA>
+                                         : k_trace_closest<FEAT_ALL>;
   int grid = grid_for(c, kern, block, smem);
   const long long need = (n + block - 1) / block;
   if (grid > need) grid = (int)need;
@@ -1159,7 +1165,9 @@ static tpt_status run_wavefront_t(tpt_context *c, const DevScene &S, const Rende
   std::memcpy(c->counters_host, &init, sizeof(init));
   TPT_CUDA(cudaMemcpyAsync(c->counters, c->counters_host, sizeof(WfCounters), cudaMemcpyHostToDevice, c->stream));
   const int smem = stack_smem(block);
-  auto traverse = S.feat == FEAT_SPHERES ? k_wf_traverse<FEAT_SPHERES> : k_wf_traverse<FEAT_ALL>;
+  auto traverse = S.feat == FEAT_SPHERES   ? k_wf_traverse<FEAT_SPHERES>
+                  : S.feat == FEAT_NO_MEDIA ? k_wf_traverse<FEAT_NO_MEDIA>
+                                            : k_wf_traverse<FEAT_ALL>;
   TPT_CUDA(smem_optin(traverse, smem));
   const int g_gen = std::max(1, std::min<int>((int)((first + block - 1) / block), c->sm_count * 8));
   if constexpr (MODE == 0)
@@ -1250,6 +1258,9 @@ static PersistentKernel persistent_variant(int v, int feat = FEAT_ALL) {
       default: return k_persistent<4, FEAT_SPHERES>;
     }
   }
+  // scenes without media keep the general persistent kernel: its no-media
+  // specialisation measured slower on the Cornell box (950 against 1036
+  // Msamples/s: different register allocation), unlike the wavefront traversal
   switch (v) {
     case 5: return k_persistent<5>;
     case 6: return k_persistent<6>;
@@ -1492,7 +1503,7 @@ extern "C" tpt_status tpt_render_batch(tpt_context *c, const tpt_batch_item *ite
   key = fnv1a(key, &p->wave, sizeof(p->wave));
   key = fnv1a(key, &mem, sizeof(mem));
   for (int k = 0; k < n; k++) key = fnv1a(key, &items[k].out_rgb, sizeof(float *));
-  int feat = FEAT_SPHERES;
+  int feat = FEAT_SPHERES;  // the widest feature set of the items (batch kernels: spheres only or all)
   for (int k = 0; k < n; k++)
     if (table[k].scene.feat != FEAT_SPHERES) feat = FEAT_ALL;
   const BatchKernel kern = batch_variant(p->wave, feat);
