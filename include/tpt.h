@@ -130,12 +130,17 @@ tpt_status tpt_scene_from_text(const char *sd_text, tpt_scene **out, char *err, 
 /* BVH topology the compiler flattens for every bvh_node.  REFERENCE (the
  * default) is the reference's own tree (random axis, median split,
  * hitable.cc:32-56), required for closest-hit parity.  SAH rebuilds each
- * bvh_node's primitives with a binned surface-area heuristic (no
- * counterpart in the reference): the same closest hits except which of
- * several primitives at exactly equal t wins, and renders that agree
- * statistically, usually faster on large scenes.  tpt_scene_bvh_dump always
- * reports the reference tree. */
-enum { TPT_BVH_REFERENCE = 0, TPT_BVH_SAH = 1 };
+ * bvh_node's primitives with a binned surface-area heuristic on the host;
+ * LBVH leaves them to a linear BVH built on the GPU when the scene is
+ * uploaded (Morton-ordered primitives, Karras 2012 radix tree; the build
+ * runs again on every tpt_render_noalloc call).  Neither has a counterpart
+ * in the reference: they give the same closest hits except which of several
+ * primitives at exactly equal t wins, and renders that agree statistically,
+ * usually faster on large scenes.  An LBVH tree's depth is known only after
+ * the build: tpt_scene_upload fails with TPT_ERR_STACK_OVERFLOW if it
+ * exceeds the traversal stack (tpt_scene_info.max_stack counts its BVHs as
+ * one level).  tpt_scene_bvh_dump always reports the reference tree. */
+enum { TPT_BVH_REFERENCE = 0, TPT_BVH_SAH = 1, TPT_BVH_LBVH = 2 };
 tpt_status tpt_builder_set_bvh_build(tpt_builder *b, int32_t mode);
 tpt_status tpt_scene_from_text_opt(const char *sd_text, int32_t bvh_build, tpt_scene **out, char *err,
                                    size_t errlen);
@@ -164,9 +169,18 @@ void tpt_context_destroy(tpt_context *ctx);
 /* Use this cudaStream_t (passed as void*) for all later work; NULL = the
  * context's own stream. */
 tpt_status tpt_context_set_stream(tpt_context *ctx, void *stream);
-/* Copy a compiled scene into device memory; returns a slot id. */
+/* Copy a compiled scene into device memory (and build its BVHs there if it
+ * was compiled with TPT_BVH_LBVH); returns a slot id. */
 tpt_status tpt_scene_upload(tpt_context *ctx, const tpt_scene *s, int32_t *slot);
 tpt_status tpt_scene_release(tpt_context *ctx, int32_t slot);
+
+/* The GPU linear-BVH builder of TPT_BVH_LBVH over n boxes (host buffers,
+ * 6 floats each: min xyz, max xyz).  Writes m = max(n - 1, 1) nodes in
+ * pre-order: node_boxes (m x 6), node_kids (m x 2: >= 0 a node, < 0 ~box
+ * index), node_skip (m: the pre-order index just past the node's subtree),
+ * and *depth = levels of internal nodes.  Synchronous. */
+tpt_status tpt_bvh_build_boxes(tpt_context *ctx, const float *boxes, int32_t n, float *node_boxes,
+                               int32_t *node_kids, int32_t *node_skip, int32_t *depth);
 
 /* Context options (tpt_context_set_option). */
 enum {

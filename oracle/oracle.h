@@ -110,6 +110,18 @@ int32_t oracle_render(const oracle_scene *s, const oracle_render_params *p,
  * int(255.99*c), clamp to [0,255]. */
 void oracle_quantize(const float *mean_rgb, int64_t n_pixels, uint8_t *rgb8);
 
+/* Linear BVH over n boxes (6 floats each: min xyz, max xyz), the CPU
+ * restatement of the GPU builder of TPT_BVH_LBVH (lbvh.cc).  keys: the
+ * n unsorted 64-bit keys (Morton code of the centroid, then the index);
+ * returns the Morton bits per axis. */
+int32_t oracle_lbvh_keys(const float *boxes, int32_t n, uint64_t *keys);
+/* The tree: max(n - 1, 1) internal nodes in pre-order; per node its box
+ * (6 floats), children (>= 0: node, < 0: ~box index) and the pre-order index
+ * just past its subtree; *out_depth = levels of internal nodes.  Returns the
+ * node count, or -1 for n < 1. */
+int32_t oracle_lbvh_build(const float *boxes, int32_t n, float *out_boxes, int32_t *out_kids,
+                          int32_t *out_skip, int32_t *out_depth);
+
 /* Philox-4x32-10 block (Salmon et al., SC'11). */
 void oracle_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 

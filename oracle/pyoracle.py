@@ -74,6 +74,10 @@ def lib():
         L.oracle_quantize.argtypes = [C.c_void_p, C.c_int64, C.c_void_p]
         L.oracle_philox.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_procedural_image.argtypes = [C.c_int32, C.c_int32, C.c_uint32, C.c_void_p]
+        L.oracle_lbvh_keys.restype = C.c_int32
+        L.oracle_lbvh_keys.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
+        L.oracle_lbvh_build.restype = C.c_int32
+        L.oracle_lbvh_build.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib = L
     return _lib
 
@@ -190,6 +194,31 @@ def procedural_image(w: int, h: int, seed: int) -> np.ndarray:
     out = np.zeros((h, w, 3), np.uint8)
     lib().oracle_procedural_image(w, h, seed, _ptr(out))
     return out
+
+
+def lbvh_keys(boxes: np.ndarray):
+    """Unsorted keys of the linear BVH over boxes (n x 6: min xyz, max
+    xyz) and the Morton bits per axis (oracle/lbvh.cc)."""
+    boxes = np.ascontiguousarray(boxes, np.float32)
+    keys = np.zeros(len(boxes), np.uint64)
+    bits = lib().oracle_lbvh_keys(_ptr(boxes), len(boxes), _ptr(keys))
+    return keys, bits
+
+
+def lbvh_build(boxes: np.ndarray):
+    """The linear BVH over boxes, restated on the CPU (oracle/lbvh.cc):
+    pre-order node boxes (m x 6), children (m x 2; >= 0 node, < 0 ~box
+    index), skip (m) and the depth in internal-node levels."""
+    boxes = np.ascontiguousarray(boxes, np.float32)
+    m = max(len(boxes) - 1, 1)
+    nb = np.zeros((m, 6), np.float32)
+    kids = np.zeros((m, 2), np.int32)
+    skip = np.zeros(m, np.int32)
+    depth = C.c_int32(0)
+    k = lib().oracle_lbvh_build(_ptr(boxes), len(boxes), _ptr(nb), _ptr(kids), _ptr(skip), C.byref(depth))
+    if k < 0:
+        raise ValueError("lbvh_build needs at least one box")
+    return nb, kids, skip, depth.value
 
 
 def ref_frontend_bvh(n: int):

@@ -1,8 +1,9 @@
-"""The SAH topology option (TPT_BVH_SAH): the closest hit of every ray is the
-reference's (checked against the CPU oracle, which builds the reference's
-own tree) except which primitive wins where several report exactly the same
-t - the scene built from coincident primitives ("ties") is left out - and
-renders agree with the reference topology's."""
+"""The alternative topologies - SAH built on the host (TPT_BVH_SAH) and the
+linear BVH built on the GPU (TPT_BVH_LBVH): the closest hit of every ray is
+the reference's (checked against the CPU oracle, which builds the
+reference's own tree) except which primitive wins where several report
+exactly the same t - the scene built from coincident primitives ("ties") is
+left out - and renders agree with the reference topology's."""
 import numpy as np
 import pytest
 
@@ -13,13 +14,14 @@ from tpt import scenes
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("bvh", ["sah", "lbvh"])
 @pytest.mark.parametrize("flat", [0, 1 << 20], ids=["stack", "stackless"])
 @pytest.mark.parametrize("name", ["one_weekend", "next_week", "instances", "cornell_guiding"])
-def test_sah_closest_hits_match_oracle(ctx, name, flat):
+def test_closest_hits_match_oracle(ctx, name, flat, bvh):
     sd = scenes.PRESETS[name]()
     text = sd.text()
     ctx.set_flat_nodes(flat)
-    slot = ctx.upload(tpt.Scene(text, bvh="sah"))
+    slot = ctx.upload(tpt.Scene(text, bvh=bvh))
     ora = pyoracle.Scene(text)
     rays = ora.make_rays(200_000, 21, 0.5, 0.05)
     f, i = ctx.trace_closest(slot, rays, seed=5)
@@ -38,10 +40,11 @@ def test_sah_closest_hits_match_oracle(ctx, name, flat):
     assert differ.mean() < 1e-2, differ.sum()
 
 
-def test_sah_render_matches_reference_topology(ctx):
+@pytest.mark.parametrize("bvh", ["sah", "lbvh"])
+def test_render_matches_reference_topology(ctx, bvh):
     sd = scenes.one_weekend()
     a = ctx.upload(tpt.Scene(sd.text()))
-    b = ctx.upload(tpt.Scene(sd.text(), bvh="sah"))
+    b = ctx.upload(tpt.Scene(sd.text(), bvh=bvh))
     k, w, h = 6, 48, 48
     ra = np.stack([ctx.render(a, w, h, 16, background=tpt.BACKGROUND_SKY, seed=10 + j)[0] for j in range(k)])
     rb = np.stack([ctx.render(b, w, h, 16, background=tpt.BACKGROUND_SKY, seed=10 + j)[0] for j in range(k)])

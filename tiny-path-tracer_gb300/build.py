@@ -3,8 +3,9 @@ host scene compiler + C ABI), compiled in-tree into tiny-path-tracer_gb300/_buil
 
     python tiny-path-tracer_gb300/build.py
 
-The translation units compile in parallel: kernels.cu (path tracing) and
-learn.cu (tensor-core MLPs of the learned parts) with nvcc
+The translation units compile in parallel: kernels.cu (path tracing),
+learn.cu (tensor-core MLPs of the learned parts) and lbvh.cu (the GPU BVH
+builder) with nvcc
 (-gencode arch=compute_103a,code=sm_103a; hit arithmetic is written with
 unfused round-to-nearest intrinsics, so FMA contraction stays on for the
 rest), scene.cc (scene compiler) and config.cc (config.ini, PPM strips) with
@@ -53,7 +54,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     nvcc = _nvcc()
     cuda = _cuda_home(nvcc)
     objs, cmds = [], []
-    for cu in ("kernels.cu", "learn.cu"):
+    for cu in ("kernels.cu", "learn.cu", "lbvh.cu"):
         obj = os.path.join(OUT, cu.replace(".cu", ".o"))
         objs.append(obj)
         cmds.append([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",

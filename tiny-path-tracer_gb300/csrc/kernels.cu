@@ -1029,6 +1029,56 @@ static DevScene dev_scene_at(const HostScene &S, const ArenaLayout &L, uint8_t *
   return d;
 }
 
+// The LBVH build jobs of a scene whose arena starts at `base` (device).
+static LbvhArgs lbvh_args(const HostScene &S, const ArenaLayout &L, uint8_t *base) {
+  LbvhArgs a;
+  a.jobs = (const i4 *)(base + L.off[ARENA_LBVH_JOBS]);
+  a.n_jobs = (int32_t)S.lbvh_jobs.size();
+  a.prims = (const f4 *)(base + L.off[ARENA_LBVH_PRIMS]);
+  a.n_prims = (int32_t)(S.lbvh_prims.size() / 2);
+  a.n_keys = S.lbvh_keys;
+  a.max_pad = S.lbvh_max_pad;
+  a.node_lo = (f4 *)(base + L.off[0]);
+  a.node_hi = (f4 *)(base + L.off[1]);
+  a.node_skip = (int32_t *)(base + L.off[2]);
+  a.node_kids = (f4 *)(base + L.off[16]);
+  a.n_leaves = (int32_t)S.leaf_hdr.size();
+  a.work = base + L.off[ARENA_LBVH_WORK];
+  return a;
+}
+
+// Builds a TPT_BVH_LBVH scene's trees in its device arena, waits for the
+// build and checks it: every reference inside its tree, and the traversal
+// stack bound against the trees' depths (the compile-time check counted each
+// tree as one level).
+static tpt_status lbvh_scene_build(const HostScene &S, const ArenaLayout &L, uint8_t *base, cudaStream_t stream) {
+  if (S.lbvh_jobs.empty()) return TPT_OK;
+  const LbvhArgs a = lbvh_args(S, L, base);
+  TPT_CUDA(lbvh_build(a, stream));
+  std::vector<int32_t> depth(a.n_jobs + 1);
+  TPT_CUDA(cudaMemcpyAsync(depth.data(), lbvh_depths(a.work, a.n_prims, a.n_jobs, a.n_keys),
+                           sizeof(int32_t) * (a.n_jobs + 1), cudaMemcpyDeviceToHost, stream));
+  TPT_CUDA(cudaStreamSynchronize(stream));
+  if (depth[a.n_jobs]) {
+    std::snprintf(g_last_error, sizeof(g_last_error), "LBVH build produced %d nodes with out-of-range references",
+                  depth[a.n_jobs]);
+    return TPT_ERR_CUDA;
+  }
+  int top = 0, blas = 0;
+  for (int j = 0; j < a.n_jobs; j++) {
+    int &d = S.lbvh_blas[j] ? blas : top;
+    d = std::max(d, depth[j]);
+  }
+  const int need = top + 2 + (S.n_blas ? blas + 2 : 0);  // as the host compiler counts it
+  if (need > TRAVERSAL_STACK) {
+    std::snprintf(g_last_error, sizeof(g_last_error),
+                  "LBVH of depth %d (instanced %d) needs %d traversal stack entries, the device has %d", top, blas,
+                  need, (int)TRAVERSAL_STACK);
+    return TPT_ERR_STACK_OVERFLOW;
+  }
+  return TPT_OK;
+}
+
 tpt_status tpt_scene_upload(tpt_context *c, const tpt_scene *sc, int32_t *slot) {
   if (!c || !sc || !slot) return TPT_ERR_INVALID_ARGUMENT;
   const HostScene &S = *host_scene(sc);
@@ -1038,7 +1088,7 @@ tpt_status tpt_scene_upload(tpt_context *c, const tpt_scene *sc, int32_t *slot) 
   ArenaSection sec[ARENA_SECTIONS];
   arena_sections(S, sec);
   for (int i = 0; i < ARENA_SECTIONS; i++)
-    if (sec[i].bytes) std::memcpy(host.data() + L.off[i], sec[i].data, sec[i].bytes);
+    if (sec[i].bytes && sec[i].data) std::memcpy(host.data() + L.off[i], sec[i].data, sec[i].bytes);
   Slot s;
   TPT_CUDA(cudaMalloc(&s.arena, L.total));
   cudaError_t e = cudaMemcpyAsync(s.arena, host.data(), L.total, cudaMemcpyHostToDevice, c->stream);
@@ -1049,6 +1099,12 @@ tpt_status tpt_scene_upload(tpt_context *c, const tpt_scene *sc, int32_t *slot) 
   }
   s.bytes = L.total;
   uint8_t *base = (uint8_t *)s.arena;
+  const tpt_status bst = lbvh_scene_build(S, L, base, c->stream);
+  if (bst != TPT_OK) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(s.arena);
+    return bst;
+  }
   s.ds = dev_scene_at(S, L, base);
   for (int i = 0; i < 3; i++) {
     s.world_lo[i] = S.world_lo[i];
@@ -1063,6 +1119,76 @@ tpt_status tpt_scene_upload(tpt_context *c, const tpt_scene *sc, int32_t *slot) 
     }
   c->slots.push_back(s);
   *slot = (int32_t)c->slots.size() - 1;
+  return TPT_OK;
+}
+
+tpt_status tpt_bvh_build_boxes(tpt_context *c, const float *boxes, int32_t n, float *node_boxes,
+                               int32_t *node_kids, int32_t *node_skip, int32_t *depth) {
+  if (!c || !boxes || n < 1 || !node_boxes || !node_kids || !node_skip || !depth) return TPT_ERR_INVALID_ARGUMENT;
+  TPT_CUDA(cudaSetDevice(c->device));
+  const int m = n > 1 ? n - 1 : 1;
+  const int64_t pad = lbvh_pad(n);
+  // one job: inputs, the node arrays of m nodes and the build scratch
+  const size_t sz[7] = {sizeof(i4), 2 * (size_t)n * sizeof(f4), (size_t)m * sizeof(f4), (size_t)m * sizeof(f4),
+                        4 * (size_t)m * sizeof(f4), (size_t)m * sizeof(int32_t), lbvh_work_bytes(n, 1, pad)};
+  size_t off[7], total = 0;
+  for (int i = 0; i < 7; i++) {
+    off[i] = total;
+    total += lbvh_align(sz[i]);
+  }
+  std::vector<uint8_t> host(off[2], 0);
+  const i4 job{0, n, 0, 0};
+  std::memcpy(host.data(), &job, sizeof job);
+  f4 *prims = (f4 *)(host.data() + off[1]);
+  for (int i = 0; i < n; i++) {
+    const int32_t ref = ~i, zero = 0;
+    prims[2 * i] = f4{boxes[6 * i], boxes[6 * i + 1], boxes[6 * i + 2], 0};
+    prims[2 * i + 1] = f4{boxes[6 * i + 3], boxes[6 * i + 4], boxes[6 * i + 5], 0};
+    std::memcpy(&prims[2 * i].w, &ref, 4);
+    std::memcpy(&prims[2 * i + 1].w, &zero, 4);
+  }
+  uint8_t *d = nullptr;
+  TPT_CUDA(cudaMalloc(&d, total));
+  LbvhArgs a;
+  a.jobs = (const i4 *)d;
+  a.n_jobs = 1;
+  a.prims = (const f4 *)(d + off[1]);
+  a.n_prims = n;
+  a.n_keys = pad;
+  a.max_pad = (int32_t)pad;
+  a.node_lo = (f4 *)(d + off[2]);
+  a.node_hi = (f4 *)(d + off[3]);
+  a.node_kids = (f4 *)(d + off[4]);
+  a.node_skip = (int32_t *)(d + off[5]);
+  a.n_leaves = n;
+  a.work = d + off[6];
+  std::vector<f4> lo(m), hi(m);
+  cudaError_t e = cudaMemcpyAsync(d, host.data(), off[2], cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = lbvh_build(a, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(lo.data(), a.node_lo, m * sizeof(f4), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(hi.data(), a.node_hi, m * sizeof(f4), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(node_skip, a.node_skip, m * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+  int32_t dep[2] = {0, 0};
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dep, lbvh_depths(a.work, n, 1, pad), sizeof dep, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (dep[1]) {
+    std::snprintf(g_last_error, sizeof(g_last_error), "LBVH build produced %d nodes with out-of-range references",
+                  dep[1]);
+    return TPT_ERR_CUDA;
+  }
+  *depth = dep[0];
+  for (int p = 0; p < m; p++) {
+    const float b[6] = {lo[p].x, lo[p].y, lo[p].z, hi[p].x, hi[p].y, hi[p].z};
+    std::memcpy(node_boxes + 6 * (size_t)p, b, sizeof b);
+    std::memcpy(node_kids + 2 * (size_t)p, &lo[p].w, 4);
+    std::memcpy(node_kids + 2 * (size_t)p + 1, &hi[p].w, 4);
+  }
   return TPT_OK;
 }
 
@@ -2119,7 +2245,12 @@ extern "C" tpt_status tpt_render_noalloc(const tpt_scene *scene, void *arena_dev
   arena_sections(H, sec);
   uint8_t *base = (uint8_t *)arena_dev;
   for (int i = 0; i < ARENA_SECTIONS; i++)
-    if (sec[i].bytes) TPT_CUDA(cudaMemcpyAsync(base + L.off[i], sec[i].data, sec[i].bytes, cudaMemcpyHostToDevice, stream));
+    if (sec[i].bytes && sec[i].data)
+      TPT_CUDA(cudaMemcpyAsync(base + L.off[i], sec[i].data, sec[i].bytes, cudaMemcpyHostToDevice, stream));
+  {  // TPT_BVH_LBVH: the trees are built in the caller's buffer on every call
+    const tpt_status bst = lbvh_scene_build(H, L, base, stream);
+    if (bst != TPT_OK) return bst;
+  }
   DevScene d = dev_scene_at(H, L, base);
   d.flat_max = p->flat_nodes > 0 ? p->flat_nodes : DEFAULT_FLAT_MAX;
 

@@ -523,16 +523,19 @@ int32_t tpt_bvh_node(tpt_builder *b, const int32_t *items, int32_t n, float t0, 
   int root = build_bvh(*b, l.data(), n, t0, t1);
   if (root < 0) return root;
   // the root becomes a user-visible hitable; it keeps the shutter interval
-  // for rebuilds of its topology (TPT_BVH_SAH)
+  // and its items, in the caller's order, for rebuilds of its topology
+  // (TPT_BVH_SAH, TPT_BVH_LBVH)
   b->nodes[root].internal = false;
   b->nodes[root].t0 = t0;
   b->nodes[root].t1 = t1;
+  b->nodes[root].items = l;
   if (b->auto_user) b->set_user(root, root);
   return root;
 }
 
 tpt_status tpt_builder_set_bvh_build(tpt_builder *b, int32_t mode) {
-  if (!b || (mode != TPT_BVH_REFERENCE && mode != TPT_BVH_SAH)) return TPT_ERR_INVALID_ARGUMENT;
+  if (!b || (mode != TPT_BVH_REFERENCE && mode != TPT_BVH_SAH && mode != TPT_BVH_LBVH))
+    return TPT_ERR_INVALID_ARGUMENT;
   b->bvh_build = mode;
   return TPT_OK;
 }
@@ -686,6 +689,7 @@ struct Compiler {
 
   int flatten_bvh(int h, bool in_blas, int depth, int &max_depth) {
     if (B.bvh_build == TPT_BVH_SAH) return flatten_sah(h, in_blas, depth, max_depth);
+    if (B.bvh_build == TPT_BVH_LBVH) return flatten_lbvh(h, in_blas, depth, max_depth);
     if (depth > max_depth) max_depth = depth;
     const HNode &n = B.nodes[h];
     int me = (int)S.node_lo.size();
@@ -849,6 +853,50 @@ struct Compiler {
     std::memcpy(&S.node_lo[me].w, &refs[0], 4);
     std::memcpy(&S.node_hi[me].w, &refs[1], 4);
     S.node_skip[me] = (int32_t)S.node_lo.size();
+    return me;
+  }
+
+  // ---- alternative topology built on the GPU (lbvh.cu): the primitives'
+  // leaves in the caller's order, their boxes and max(n - 1, 1) reserved
+  // node slots become one build job.
+  void lbvh_collect(int h, float t0, float t1, std::vector<SahLeaf> &out, int guard = 0) {
+    const HNode &n = B.nodes[h];
+    if (n.kind == H_BVH && !n.items.empty() && guard < 64) {
+      for (int c : n.items) lbvh_collect(c, t0, t1, out, guard + 1);
+      return;
+    }
+    sah_collect(h, t0, t1, out);
+  }
+
+  int flatten_lbvh(int h, bool in_blas, int depth, int &max_depth) {
+    if (depth > max_depth) max_depth = depth;  // the device build reports the rest
+    std::vector<SahLeaf> leaves;
+    lbvh_collect(h, B.nodes[h].t0, B.nodes[h].t1, leaves);
+    if (st != TPT_OK || leaves.empty()) return -1;
+    const int n = (int)leaves.size();
+    std::vector<int32_t> refs(n);
+    for (int i = 0; i < n; i++) {  // leaves before nodes: the job's slots stay contiguous
+      refs[i] = sah_leaf_ref(leaves[i], in_blas);
+      if (st != TPT_OK) return -1;
+    }
+    const int me = (int)S.node_lo.size(), slots = n > 1 ? n - 1 : 1;
+    S.node_lo.resize(me + slots, f4{0, 0, 0, 0});
+    S.node_hi.resize(me + slots, f4{0, 0, 0, 0});
+    S.node_skip.resize(me + slots, 0);
+    const int32_t job = (int32_t)S.lbvh_jobs.size();
+    const int64_t pad = lbvh_pad(n);
+    S.lbvh_jobs.push_back(i4{me, n, (int32_t)(S.lbvh_prims.size() / 2), (int32_t)S.lbvh_keys});
+    S.lbvh_keys += pad;
+    S.lbvh_max_pad = std::max(S.lbvh_max_pad, (int32_t)pad);
+    S.lbvh_blas.push_back(in_blas ? 1 : 0);
+    for (int i = 0; i < n; i++) {
+      f4 lo{leaves[i].box.mn.e[0], leaves[i].box.mn.e[1], leaves[i].box.mn.e[2], 0};
+      f4 hi{leaves[i].box.mx.e[0], leaves[i].box.mx.e[1], leaves[i].box.mx.e[2], 0};
+      std::memcpy(&lo.w, &refs[i], 4);
+      std::memcpy(&hi.w, &job, 4);
+      S.lbvh_prims.push_back(lo);
+      S.lbvh_prims.push_back(hi);
+    }
     return me;
   }
 

@@ -8,6 +8,7 @@
 
 #include "../../include/tpt.h"
 #include "arena.h"
+#include "lbvh.h"
 
 namespace tpt {
 
@@ -33,10 +34,19 @@ struct HostScene {
   float world_lo[3] = {0, 0, 0}, world_hi[3] = {0, 0, 0};  // world bounding box (0 if none)
   Camera cam{};
   float cam_in[15] = {};  // the camera's inputs: lookfrom, lookat, vup, vfov, aspect, aperture, focus, t0, t1
+  // TPT_BVH_LBVH: one device build job per bvh_node (lbvh.h); its node slots
+  // stay zero on the host and are filled after upload
+  std::vector<i4> lbvh_jobs;
+  std::vector<f4> lbvh_prims;
+  std::vector<uint8_t> lbvh_blas;  // per job: 1 if the BVH is instanced
+  int64_t lbvh_keys = 0;
+  int32_t lbvh_max_pad = 0;
 };
 
-// Sections of the device arena, each 256-byte aligned, in DevScene order.
-enum { ARENA_SECTIONS = 17 };
+// Sections of the device arena, each 256-byte aligned, in DevScene order,
+// then the LBVH build inputs and scratch (a section with null data is
+// reserved, not copied).
+enum { ARENA_SECTIONS = 20, ARENA_LBVH_JOBS = 17, ARENA_LBVH_PRIMS = 18, ARENA_LBVH_WORK = 19 };
 struct ArenaSection {
   const void *data;
   size_t bytes;
@@ -59,7 +69,12 @@ inline void arena_sections(const HostScene &S, ArenaSection out[ARENA_SECTIONS])
       {S.perlin_perm.data(), S.perlin_perm.size() * sizeof(int32_t)},
       {S.light_i.data(), S.light_i.size() * sizeof(i4)},
       {S.light_f.data(), S.light_f.size() * sizeof(f4)},
-      {S.node_kids.data(), S.node_kids.size() * sizeof(f4)}};
+      {S.node_kids.data(), S.node_kids.size() * sizeof(f4)},
+      {S.lbvh_jobs.data(), S.lbvh_jobs.size() * sizeof(i4)},
+      {S.lbvh_prims.data(), S.lbvh_prims.size() * sizeof(f4)},
+      {nullptr, S.lbvh_jobs.empty() ? 0
+                                    : lbvh_work_bytes((int64_t)S.lbvh_prims.size() / 2, (int32_t)S.lbvh_jobs.size(),
+                                                      S.lbvh_keys)}};
   for (int i = 0; i < ARENA_SECTIONS; i++) out[i] = t[i];
 }
 

@@ -27,7 +27,7 @@ BACKGROUND_SKY = 1
 ENGINE_AUTO = 0
 ENGINE_WAVEFRONT = 1
 ENGINE_PERSISTENT = 2
-BVH_REFERENCE, BVH_SAH = 0, 1
+BVH_REFERENCE, BVH_SAH, BVH_LBVH = 0, 1, 2
 
 STATUS = {0: "TPT_OK", 1: "TPT_ERR_INVALID_ARGUMENT", 2: "TPT_ERR_PARSE", 3: "TPT_ERR_UNSUPPORTED",
           4: "TPT_ERR_NO_BOUNDING_BOX", 5: "TPT_ERR_CUDA", 6: "TPT_ERR_OUT_OF_MEMORY",
@@ -151,6 +151,8 @@ _SIGS = {
     "tpt_context_set_option": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int64]),
     "tpt_scene_upload": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int32)]),
     "tpt_scene_release": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "tpt_bvh_build_boxes": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p]),
     "tpt_trace_closest": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_uint64, C.c_void_p,
                                       C.c_void_p, C.c_int32]),
     "tpt_render_params_default": (None, [C.POINTER(RenderParams)]),
@@ -235,11 +237,12 @@ class Scene:
     """A compiled scene (host arena) built from scene-description text."""
 
     def __init__(self, sd_text: str, bvh: str = "reference"):
-        """bvh: "reference" (the reference's tree, closest-hit parity) or
-        "sah" (binned SAH rebuild of every bvh_node, TPT_BVH_SAH)."""
+        """bvh: "reference" (the reference's tree, closest-hit parity),
+        "sah" (binned SAH rebuild of every bvh_node on the host, TPT_BVH_SAH)
+        or "lbvh" (linear BVH built on the GPU at upload, TPT_BVH_LBVH)."""
         h = C.c_void_p()
         err = C.create_string_buffer(512)
-        mode = {"reference": BVH_REFERENCE, "sah": BVH_SAH}[bvh]
+        mode = {"reference": BVH_REFERENCE, "sah": BVH_SAH, "lbvh": BVH_LBVH}[bvh]
         st = lib().tpt_scene_from_text_opt(sd_text.encode(), mode, C.byref(h), err, 512)
         if st != 0:
             raise TptError(st, err.value.decode())
@@ -321,6 +324,21 @@ class Context:
 
     def release(self, slot: int) -> None:
         check(lib().tpt_scene_release(self._h, slot))
+
+    def bvh_build_boxes(self, boxes: np.ndarray):
+        """The GPU linear-BVH builder over boxes (n x 6: min xyz, max xyz):
+        pre-order node boxes (m x 6), children (m x 2; >= 0 node, < 0 ~box
+        index), skip (m) and the depth in internal-node levels."""
+        boxes = np.ascontiguousarray(boxes, np.float32).reshape(-1, 6)
+        n = boxes.shape[0]
+        m = max(n - 1, 1)
+        nb = np.zeros((m, 6), np.float32)
+        kids = np.zeros((m, 2), np.int32)
+        skip = np.zeros(m, np.int32)
+        depth = C.c_int32(0)
+        check(lib().tpt_bvh_build_boxes(self._h, _ptr(boxes), n, _ptr(nb), _ptr(kids), _ptr(skip), C.byref(depth)),
+              "bvh_build_boxes")
+        return nb, kids, skip, depth.value
 
     def trace_closest(self, slot: int, rays: np.ndarray, seed: int = 0):
         rays = np.ascontiguousarray(rays, np.float32)
