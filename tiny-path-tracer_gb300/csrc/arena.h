@@ -85,7 +85,8 @@ struct DevScene {
   const int32_t *perlin_perm;
   const i4 *light_i;
   const f4 *light_f;
-  const f4 *node_kids;  // 4 per node: both children's boxes, refs in lo.w
+  const f4 *node_kids;  // 4 per node: both children's boxes, refs in lo.w; a sphere leaf child
+                        // carries {center, ref}, {radius, 1, 0, 0}
   int32_t n_nodes, n_leaves, n_items, n_mats, n_texs, n_lights;
   int32_t light_is_list;  // 0: single light_shape hitable; 1: hitable_list
   int32_t has_lights;

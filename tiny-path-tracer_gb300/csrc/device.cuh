@@ -396,7 +396,7 @@ enum { FLAT_PRUNE_MIN = 32 };
 // (t, -leaf order), and a subtree is skipped only when the lower bound
 // prune_key() on any t its primitives can report exceeds the best t.  stk: this thread's stack slots, `stride`
 // entries apart.  err receives TPT_ERR_STACK_OVERFLOW on overflow.
-template <int FEAT = FEAT_ALL>
+template <int FEAT = FEAT_ALL, bool INL = true>
 __device__ bool trace_closest(const DevScene &S, const Ray &wr, float tmin, int2 *stk, int stride,
                               const MediumRng &mrng, HitRef &res, int &err) {
   const RayPre W = precompute(wr);
@@ -491,6 +491,19 @@ __device__ bool trace_closest(const DevScene &S, const Ray &wr, float tmin, int2
             if (slab(curp, clo, chi, tmin, tmax, en)) {
               ent[nq] = en;
               q[nq++] = make_int2(ref, __float_as_int(prune_key_ext(curp, chi.w, en)));  // chi.w: box size term
+            }
+          } else if (INL && (FEAT == FEAT_SPHERES || (c == 0 ? k1 : k3).y != 0.f)) {
+            // a sphere leaf: its center and radius ride in the child's box
+            // slot, so it is tested here, with no stack entry and no header
+            // or data load (INL: compiled in; the general persistent kernel
+            // leaves it out, which keeps tiny mixed scenes' code smaller)
+            const f4 sc = c == 0 ? k0 : k2;
+            const int leaf = ~ref;
+            const int outer = cur_inst >= 0 ? cur_inst : leaf, inner = cur_inst >= 0 ? leaf : -1;
+            float t;
+            if (sphere_t(v3(sc.x, sc.y, sc.z), (c == 0 ? k1 : k3).x, cur, tmin, tmax, t) &&
+                beats(t, outer, inner, bt, bo, bn)) {
+              bt = t; bl = leaf; bi = cur_inst; bf = -1; bo = outer; bn = inner;
             }
           } else {
             push(-2 - ~ref, never_pruned);

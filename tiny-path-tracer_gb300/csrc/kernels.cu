@@ -487,7 +487,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS) k_persistent(DevScene S, Rend
     if (alive) {
       MediumRng m{make_uint4(pixel, sample, (uint32_t)depth, 0u), cfg.key, 1};
       HitRef h;
-      const bool hit = trace_closest<FEAT>(S, r, 0.001f, stk, blockDim.x, m, h, e);
+      const bool hit = trace_closest<FEAT, FEAT != FEAT_ALL>(S, r, 0.001f, stk, blockDim.x, m, h, e);
       segs++;
       if (shade_vertex(S, cfg, r, hit, h, T, L, depth, pixel, sample)) {
         depth++;
@@ -1043,6 +1043,8 @@ static LbvhArgs lbvh_args(const HostScene &S, const ArenaLayout &L, uint8_t *bas
   a.node_skip = (int32_t *)(base + L.off[2]);
   a.node_kids = (f4 *)(base + L.off[16]);
   a.n_leaves = (int32_t)S.leaf_hdr.size();
+  a.leaf_hdr = (const i4 *)(base + L.off[3]);
+  a.leaf_data = (const f4 *)(base + L.off[5]);
   a.work = base + L.off[ARENA_LBVH_WORK];
   return a;
 }
@@ -1161,6 +1163,8 @@ tpt_status tpt_bvh_build_boxes(tpt_context *c, const float *boxes, int32_t n, fl
   a.node_kids = (f4 *)(d + off[4]);
   a.node_skip = (int32_t *)(d + off[5]);
   a.n_leaves = n;
+  a.leaf_hdr = nullptr;  // boxes only
+  a.leaf_data = nullptr;
   a.work = d + off[6];
   std::vector<f4> lo(m), hi(m);
   cudaError_t e = cudaMemcpyAsync(d, host.data(), off[2], cudaMemcpyHostToDevice, c->stream);

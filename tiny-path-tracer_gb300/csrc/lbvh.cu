@@ -295,8 +295,23 @@ __global__ void k_lbvh_boxes(const i4 *jobs, const f4 *prims, int n_prims, f4 *n
   }
 }
 
+// node_kids entry of a leaf child: a sphere leaf carries {center, radius}
+// and the flag hi.y = 1 (the scene compiler's encoding); other leaves zeros.
+__device__ __forceinline__ void leaf_kid(const i4 *leaf_hdr, const f4 *leaf_data, int ref, float4 &lo, float4 &hi) {
+  lo = make_float4(0.f, 0.f, 0.f, __int_as_float(ref));
+  hi = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (!leaf_hdr) return;
+  const i4 h = leaf_hdr[~ref];
+  if ((h.x & LEAF_TYPE_MASK) == LT_SPHERE) {
+    const float4 sp = ld4(leaf_data + h.y);
+    lo = make_float4(sp.x, sp.y, sp.z, __int_as_float(ref));
+    hi = make_float4(sp.w, 1.f, 0.f, 0.f);
+  }
+}
+
 __global__ void k_lbvh_finish(const i4 *jobs, const f4 *prims, int n_prims, const f4 *node_lo, const f4 *node_hi,
-                              f4 *node_kids, int32_t *node_skip, int n_leaves, int n_jobs, Work w) {
+                              f4 *node_kids, int32_t *node_skip, int n_leaves, const i4 *leaf_hdr,
+                              const f4 *leaf_data, int n_jobs, Work w) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n_prims) return;
   const int j = __float_as_int(prims[2 * g + 1].w);
@@ -305,12 +320,16 @@ __global__ void k_lbvh_finish(const i4 *jobs, const f4 *prims, int n_prims, cons
   if (n == 1) {
     if (i == 0) {
       const int ref = __float_as_int(prims[2 * p0].w);
-      if (ref >= 0 || ~ref >= n_leaves) atomicAdd(w.depth + n_jobs, 1);
-      const float4 z = make_float4(0.f, 0.f, 0.f, prims[2 * p0].w);
-      float4 *kd = reinterpret_cast<float4 *>(node_kids + 4 * (size_t)base);
-      kd[0] = kd[2] = z;
-      kd[1] = kd[3] = make_float4(0.f, 0.f, 0.f, 0.f);
       node_skip[base] = base + 1;
+      if (ref >= 0 || ~ref >= n_leaves) {
+        atomicAdd(w.depth + n_jobs, 1);
+        return;
+      }
+      float4 lo, hi;
+      leaf_kid(leaf_hdr, leaf_data, ref, lo, hi);
+      float4 *kd = reinterpret_cast<float4 *>(node_kids + 4 * (size_t)base);
+      kd[0] = kd[2] = lo;
+      kd[1] = kd[3] = hi;
     }
     return;
   }
@@ -345,6 +364,8 @@ __global__ void k_lbvh_finish(const i4 *jobs, const f4 *prims, int n_prims, cons
     } else if (refs[c] >= 0 || ~refs[c] >= n_leaves) {
       bad = true;
       continue;
+    } else {
+      leaf_kid(leaf_hdr, leaf_data, refs[c], lo, hi);
     }
     out[2 * c] = lo;
     out[2 * c + 1] = hi;
@@ -375,7 +396,7 @@ cudaError_t lbvh_build(const LbvhArgs &a, cudaStream_t s) {
   k_lbvh_place<<<grid, 256, 0, s>>>(a.jobs, a.prims, a.n_prims, w);
   k_lbvh_boxes<<<grid, 256, 0, s>>>(a.jobs, a.prims, a.n_prims, a.node_lo, a.node_hi, w);
   k_lbvh_finish<<<grid, 256, 0, s>>>(a.jobs, a.prims, a.n_prims, a.node_lo, a.node_hi, a.node_kids, a.node_skip,
-                                     a.n_leaves, a.n_jobs, w);
+                                     a.n_leaves, a.leaf_hdr, a.leaf_data, a.n_jobs, w);
   return cudaGetLastError();
 }
 

@@ -29,6 +29,8 @@ struct LbvhArgs {
   f4 *node_lo, *node_hi, *node_kids;
   int32_t *node_skip;
   int32_t n_leaves;  // leaf records of the scene (bound of the leaf references)
+  const i4 *leaf_hdr;   // the scene's leaves (null: no scene), for sphere
+  const f4 *leaf_data;  // leaves' data carried in node_kids
   void *work;        // lbvh_work_bytes(n_prims, n_jobs, n_keys)
 };
 

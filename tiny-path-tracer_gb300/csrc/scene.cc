@@ -1157,6 +1157,12 @@ struct Compiler {
           // the box's size term of the pruning bound, in the device's order
           // of float operations (prune_key)
           hi.w = ((hi.x - lo.x) + (hi.y - lo.y)) + (hi.z - lo.z);
+        } else if ((S.leaf_hdr[~ref[c]].x & LEAF_TYPE_MASK) == LT_SPHERE) {
+          // a sphere leaf carries its {center, radius} (flag hi.y = 1): the
+          // stack walk tests it without loading the leaf
+          const f4 sp = S.leaf_data[S.leaf_hdr[~ref[c]].y];
+          lo = f4{sp.x, sp.y, sp.z, 0};
+          hi = f4{sp.w, 1.f, 0, 0};
         }
         std::memcpy(&lo.w, &ref[c], 4);
         S.node_kids[4 * i + 2 * c] = lo;

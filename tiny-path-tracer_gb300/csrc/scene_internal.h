@@ -15,7 +15,8 @@ namespace tpt {
 struct HostScene {
   std::vector<f4> node_lo, node_hi;
   std::vector<int32_t> node_skip;  // pre-order index just past each node's subtree
-  std::vector<f4> node_kids;       // per node: {left lo, ref}, {left hi, ext}, {right lo, ref}, {right hi, ext}
+  std::vector<f4> node_kids;       // per node: {left lo, ref}, {left hi, ext}, {right lo, ref}, {right hi, ext};
+                                   // a sphere leaf child: {center, ref}, {radius, 1, 0, 0}
   std::vector<i4> leaf_hdr;
   std::vector<int32_t> leaf_user;
   std::vector<f4> leaf_data;
