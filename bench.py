@@ -52,11 +52,11 @@ WORKLOAD = "cornell_box_600x600_1024spp_depth50"
 BYTES_PER_SEGMENT = 192
 TRAVERSE_BYTES_PER_SEGMENT = 64 + 16  # traverse reads the path record, writes the hit
 # k_persistent DRAM read+write bytes and warp instructions per ray segment,
-# from the ncu capture of the 16 spp case
-# (profiles/k_persistent_cornell_600x600_16spp.md): 5.865 MB and 3.167 G warp
-# instructions over 30.42 M segments
-NCU_DRAM_BYTES_PER_SEGMENT = 5.864704e6 / 30416883
-NCU_WARP_INST_PER_SEGMENT = 3167059649 / 30416883
+# from the ncu capture of the 16 spp case in the tuned launch (block 64,
+# 5-block register variant; profiles/k_persistent_cornell_600x600_16spp.md):
+# 9.174 MB and 3.412 G warp instructions over 30.42 M segments
+NCU_DRAM_BYTES_PER_SEGMENT = (8.19712e6 + 0.976896e6) / 30416883
+NCU_WARP_INST_PER_SEGMENT = 3411932611 / 30416883
 # instruction issue peak: 152 SMs x 4 schedulers x 1 warp instruction per
 # cycle at the maximum SM clock (MEASURED_PEAKS.json sm_max_mhz)
 SMS, SCHEDULERS_PER_SM = 152, 4
@@ -290,7 +290,9 @@ def learned_equal_time(ctx, which: str) -> dict:
     guided: Cornell box with the 40x40 light and the second box, 600x600,
             plain at 1024 spp against guided at the spp that takes the same
             time (alpha 0.5, the 50/50 MIS of the configuration); FP64
-            reference 16384 spp.
+            reference 16384 spp.  Also reported: the same comparison with
+            the guide's share lowered to alpha 0.25 (the rest is the plain
+            light/cosine mixture), which measured best on this scene.
     nrc:    the seeded next-week scene, 800x800, plain at 256 spp against the
             cached renderer (paths terminated into the cache after 2 bounces)
             at the spp that takes the same time; FP64 reference 4096 spp.
@@ -323,23 +325,31 @@ def learned_equal_time(ctx, which: str) -> dict:
     plain(spp)  # warm-up
     t_plain, _ = timed(lambda: plain(spp))
     e_plain = _relmse(dev.cpu().numpy(), ref)
-    run(spp, dev.data_ptr())  # warm-up
-    t_eq, r = timed(lambda: run(spp, dev.data_ptr()))
-    e_eq = _relmse(dev.cpu().numpy(), ref)
     passes = 8
-    spp_et = max(passes, int(round(spp * t_plain / t_eq / passes)) * passes)
-    t_et, r2 = timed(lambda: run(spp_et, dev.data_ptr()))
-    e_et = _relmse(dev.cpu().numpy(), ref)
+
+    def compare(run):
+        run(spp, dev.data_ptr())  # warm-up
+        t_eq, r = timed(lambda: run(spp, dev.data_ptr()))
+        e_eq = _relmse(dev.cpu().numpy(), ref)
+        spp_et = max(passes, int(round(spp * t_plain / t_eq / passes)) * passes)
+        t_et, _ = timed(lambda: run(spp_et, dev.data_ptr()))
+        e_et = _relmse(dev.cpu().numpy(), ref)
+        return ({"spp": spp, "ms": t_eq, "relmse": e_eq, "stats": r[2]}, {"spp": spp_et, "ms": t_et, "relmse": e_et},
+                {"equal_spp_relmse_ratio": e_eq / e_plain, "equal_time_relmse_ratio": e_et / e_plain,
+                 "time_ratio_at_equal_spp": t_eq / t_plain})
+
+    eq, et, ratios = compare(run)
+    extra = {}
+    if which == "guided":
+        _, et2, ratios2 = compare(lambda n, out: tpt.render_guided(ctx, slot, w, h, n, seed=5, out=out, alpha=0.25))
+        extra = {"guided_alpha_0.25": dict(alpha=0.25, equal_time_spp=et2["spp"], equal_time_ms=et2["ms"],
+                                           equal_time_relmse=et2["relmse"], **ratios2)}
     ctx.release(slot)
     name = "cornell_40x40_light_two_boxes" if which == "guided" else "next_week_final_seeded"
     return {"scene": name, "width": w, "height": h, "ref_spp_fp64": ref_spp,
             "engine": ["auto", "wavefront", "persistent"][tuned[0]],
             "plain": {"spp": spp, "ms": t_plain, "relmse": e_plain},
-            which: {"spp": spp, "ms": t_eq, "relmse": e_eq, "stats": r[2]},
-            which + "_equal_time": {"spp": spp_et, "ms": t_et, "relmse": e_et},
-            "equal_spp_relmse_ratio": e_eq / e_plain,
-            "equal_time_relmse_ratio": e_et / e_plain,
-            "time_ratio_at_equal_spp": t_eq / t_plain}
+            which: eq, which + "_equal_time": et, **ratios, **extra}
 
 
 def main() -> None:

@@ -361,6 +361,9 @@ typedef struct {
   float alpha;          /* guide probability at a diffuse vertex (0.5) */
   int32_t record_cap;   /* training records kept per pass */
   uint64_t seed;        /* network initialisation and record sampling */
+  float light_share;    /* probability of light sampling within the non-guide part
+                           (0.5: the plain tracer's light/cosine mixture; 0: cosine
+                           only, the guide then carries all light sampling) */
 } tpt_guide_params;
 typedef struct {
   double render_ms, train_ms;  /* device time spent rendering / training + table refresh */

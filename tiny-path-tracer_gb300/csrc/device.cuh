@@ -880,7 +880,8 @@ struct GuideView {
   const float4 *lobes;  // nullptr: not guided
   float3 lo, inv_ext;
   int res;
-  float alpha;  // probability of sampling the guide at a diffuse vertex
+  float alpha;        // probability of sampling the guide at a diffuse vertex
+  float light_share;  // light sampling's share of the other techniques (0.5: the plain mixture)
 };
 // The first diffuse vertex of a path, kept to form a training record.
 struct GuideRec {
@@ -1056,18 +1057,19 @@ __device__ bool shade_vertex_t(const DevScene &S, const RenderCfg &cfg, Ray &ray
       const float4 *lob = nullptr;
       float u = r.x;  // technique choice; rescaled to [0,1) for the technique chosen
       if (GUIDED && gv.lobes) lob = guide_entry(gv, sf.p, sf.n);
+      // light sampling's share of the non-guide techniques: the plain
+      // mixture's 0.5, or the guided render's light_share
+      const float ls = !S.has_lights ? 0.f : (GUIDED && lob) ? gv.light_share : 0.5f;
       if (GUIDED && lob && u < gv.alpha) {
         dir = guide_sample(lob, u / gv.alpha, r.z, r.w);
-      } else if (S.has_lights) {
-        if (GUIDED && lob) u = (u - gv.alpha) / (1.f - gv.alpha);
-        dir = u < 0.5f ? light_random(S, sf.p, r.y, r.z, r.w) : uvw.local(cos_hemisphere(r.z, r.w));
       } else {
-        dir = uvw.local(cos_hemisphere(r.z, r.w));
+        if (GUIDED && lob) u = (u - gv.alpha) / (1.f - gv.alpha);
+        dir = u < ls ? light_random(S, sf.p, r.y, r.z, r.w) : uvw.local(cos_hemisphere(r.z, r.w));
       }
       {
         const float c = dot3(unit3(dir), uvw.w);
         const float pc = c > 0.f ? c * cos_scale : 0.f;
-        pdf = S.has_lights ? 0.5f * light_pdf(S, sf.p, dir) + 0.5f * pc : pc;
+        pdf = ls > 0.f ? ls * light_pdf(S, sf.p, dir) + (1.f - ls) * pc : pc;
         if (GUIDED && lob) pdf = gv.alpha * guide_pdf(lob, unit3(dir)) + (1.f - gv.alpha) * pdf;
       }
       if (GUIDED && !rec.valid) rec = GuideRec{sf.p, sf.n, unit3(dir), T, L, true};

@@ -1809,6 +1809,7 @@ extern "C" void tpt_guide_params_default(tpt_guide_params *g) {
   g->alpha = 0.5f;
   g->record_cap = 1 << 20;
   g->seed = 1;
+  g->light_share = 0.5f;
 }
 
 // Engine of a learned render: as asked, else the slot's tuned one, else the
@@ -1832,7 +1833,7 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
   if (slot < 0 || slot >= (int32_t)c->slots.size() || !c->slots[slot].live) return TPT_ERR_BAD_HANDLE;
   if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->max_depth < 0 || g->passes < 1 ||
       p->semantics != TPT_SEMANTICS_PHYSICAL || g->grid_res < 1 || g->grid_res > 64 || g->record_cap < 1 ||
-      !(g->alpha >= 0.f && g->alpha <= 1.f) || g->batch < 16)
+      !(g->alpha >= 0.f && g->alpha <= 1.f) || !(g->light_share >= 0.f && g->light_share <= 1.f) || g->batch < 16)
     return TPT_ERR_INVALID_ARGUMENT;
   TPT_CUDA(cudaSetDevice(c->device));
   const Slot &sl = c->slots[slot];
@@ -1890,7 +1891,7 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
   tpt_status result = TPT_OK;
   for (int pass = 0; pass < g->passes && result == TPT_OK; pass++) {
     GuideView gv{have_table ? (const float4 *)c->guide_table.p : nullptr, lo,
-                 make_float3(1.f / ext.x, 1.f / ext.y, 1.f / ext.z), g->grid_res, g->alpha};
+                 make_float3(1.f / ext.x, 1.f / ext.y, 1.f / ext.z), g->grid_res, g->alpha, g->light_share};
     cudaEventRecord(e[0], c->stream);
     if (wf) {
       WfLearn W{};

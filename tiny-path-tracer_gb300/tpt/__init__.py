@@ -75,7 +75,8 @@ class BatchItem(C.Structure):
 
 class GuideParams(C.Structure):
     _fields_ = [("passes", C.c_int32), ("train_steps", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float),
-                ("grid_res", C.c_int32), ("alpha", C.c_float), ("record_cap", C.c_int32), ("seed", C.c_uint64)]
+                ("grid_res", C.c_int32), ("alpha", C.c_float), ("record_cap", C.c_int32), ("seed", C.c_uint64),
+                ("light_share", C.c_float)]
 
 
 class GuideStats(C.Structure):
