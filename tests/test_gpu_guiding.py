@@ -86,7 +86,8 @@ def test_guided_argument_errors(built):
                                      tpt.TPT_MEM_HOST, None, None)
     assert st == 1
     p = tpt.make_params(8, 8, 4, 50, tpt.SEMANTICS_PHYSICAL)
-    for field, bad in (("passes", 0), ("grid_res", 65), ("alpha", 1.5), ("batch", 8)):
+    for field, bad in (("passes", 0), ("grid_res", 65), ("alpha", 1.5), ("batch", 8), ("light_share", -0.1),
+                       ("light_share", float("nan"))):
         g2 = tpt.GuideParams()
         tpt.lib().tpt_guide_params_default(C.byref(g2))
         setattr(g2, field, bad)
