@@ -364,6 +364,9 @@ typedef struct {
   float light_share;    /* probability of light sampling within the non-guide part
                            (0.5: the plain tracer's light/cosine mixture; 0: cosine
                            only, the guide then carries all light sampling) */
+  int32_t warm_start;   /* 0: a fresh network (seed); 1: continue from the context's
+                           network (the last guided render's, or tpt_learned_load's),
+                           guiding from the first pass */
 } tpt_guide_params;
 typedef struct {
   double render_ms, train_ms;  /* device time spent rendering / training + table refresh */
@@ -404,6 +407,9 @@ typedef struct {
   int32_t record_cap;       /* training records per pass */
   int32_t query_cap;        /* cache queries per launch (paths are launched in chunks) */
   uint64_t seed;
+  int32_t warm_start;       /* 0: a fresh cache (seed); 1: continue from the context's
+                               cache (the last cached render's, or tpt_learned_load's),
+                               querying it from the first pass */
 } tpt_nrc_params;
 typedef struct {
   double render_ms, infer_ms, train_ms;
@@ -413,6 +419,20 @@ typedef struct {
 void tpt_nrc_params_default(tpt_nrc_params *n);
 tpt_status tpt_render_nrc(tpt_context *ctx, int32_t slot, const tpt_render_params *p, const tpt_nrc_params *n,
                           float *out_rgb, int32_t mem, tpt_render_stats *stats, tpt_nrc_stats *nstats);
+
+/* Checkpoint and resume of the learned parts (no counterpart in the
+ * reference, which has no learned state): the context's guiding network
+ * (TPT_NET_GUIDE) or radiance cache (TPT_NET_CACHE) as 3 P + 1 floats -
+ * weights, Adam first and second moments (P each), and the Adam step count.
+ * tpt_learned_save with out = NULL (or cap too small) only reports *count;
+ * it fails with TPT_ERR_BAD_HANDLE before the context has rendered with that
+ * network.  tpt_learned_load restores a checkpoint into a context (creating
+ * the network), so that the next render with warm_start = 1 continues from
+ * it; a network's inputs are positions normalised to the scene's world box,
+ * so a checkpoint carries over between scenes with the same box. */
+enum { TPT_NET_GUIDE = 0, TPT_NET_CACHE = 1 };
+tpt_status tpt_learned_save(tpt_context *ctx, int32_t which, float *out, int64_t cap, int64_t *count);
+tpt_status tpt_learned_load(tpt_context *ctx, int32_t which, const float *in, int64_t count);
 
 /* ------------------------------------------------------------------------
  * The formats on either side of the render loop of main.cpp.

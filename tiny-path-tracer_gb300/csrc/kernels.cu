@@ -1810,6 +1810,7 @@ extern "C" void tpt_guide_params_default(tpt_guide_params *g) {
   g->record_cap = 1 << 20;
   g->seed = 1;
   g->light_share = 0.5f;
+  g->warm_start = 0;
 }
 
 // Engine of a learned render: as asked, else the slot's tuned one, else the
@@ -1841,8 +1842,10 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
   const int spp_pass = (p->spp + g->passes - 1) / g->passes;
   const int spp_total = spp_pass * g->passes;
   tpt_status st;
-  if (!c->guide && (st = guide_create(c->device, g->seed, &c->guide)) != TPT_OK) return st;
-  {  // fresh network for every render: reproducible online training
+  // a fresh network for every render (reproducible online training), unless
+  // warm_start continues from the context's network
+  const bool warm = g->warm_start != 0 && c->guide != nullptr;
+  if (!warm) {
     guide_destroy(c->guide);
     c->guide = nullptr;
     if ((st = guide_create(c->device, g->seed, &c->guide)) != TPT_OK) return st;
@@ -1888,6 +1891,10 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
   TPT_CUDA(cudaMemsetAsync(c->guide_count.p, 0, sizeof(unsigned), c->stream));
   unsigned emitted_before = 0;
   bool have_table = false;
+  if (warm) {  // the continued network guides from the first pass
+    if ((st = guide_refresh(c->guide, g->grid_res, (float4 *)c->guide_table.p, c->stream)) != TPT_OK) return st;
+    have_table = true;
+  }
   tpt_status result = TPT_OK;
   for (int pass = 0; pass < g->passes && result == TPT_OK; pass++) {
     GuideView gv{have_table ? (const float4 *)c->guide_table.p : nullptr, lo,
@@ -2012,6 +2019,31 @@ extern "C" void tpt_nrc_params_default(tpt_nrc_params *n) {
   n->record_cap = 1 << 20;
   n->query_cap = 1 << 22;
   n->seed = 1;
+  n->warm_start = 0;
+}
+
+extern "C" tpt_status tpt_learned_save(tpt_context *c, int32_t which, float *out, int64_t cap, int64_t *count) {
+  if (!c || !count || (which != TPT_NET_GUIDE && which != TPT_NET_CACHE)) return TPT_ERR_INVALID_ARGUMENT;
+  tpt_mlp *m = which == TPT_NET_GUIDE ? (c->guide ? guide_mlp(c->guide) : nullptr)
+                                      : (c->cache ? cache_mlp(c->cache) : nullptr);
+  if (!m) return TPT_ERR_BAD_HANDLE;
+  *count = mlp_state_count(m);
+  if (!out || cap < *count) return TPT_OK;
+  TPT_CUDA(cudaSetDevice(c->device));
+  TPT_CUDA(cudaStreamSynchronize(c->stream));
+  return mlp_save_state(m, out);
+}
+
+extern "C" tpt_status tpt_learned_load(tpt_context *c, int32_t which, const float *in, int64_t count) {
+  if (!c || !in || (which != TPT_NET_GUIDE && which != TPT_NET_CACHE)) return TPT_ERR_INVALID_ARGUMENT;
+  TPT_CUDA(cudaSetDevice(c->device));
+  TPT_CUDA(cudaStreamSynchronize(c->stream));
+  tpt_status st;
+  if (which == TPT_NET_GUIDE && !c->guide && (st = guide_create(c->device, 1, &c->guide)) != TPT_OK) return st;
+  if (which == TPT_NET_CACHE && !c->cache && (st = cache_create(c->device, 1, &c->cache)) != TPT_OK) return st;
+  tpt_mlp *m = which == TPT_NET_GUIDE ? guide_mlp(c->guide) : cache_mlp(c->cache);
+  if (count != mlp_state_count(m)) return TPT_ERR_INVALID_ARGUMENT;
+  return mlp_load_state(m, in);
 }
 
 extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_render_params *p,
@@ -2028,9 +2060,14 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
   const int spp_pass = (p->spp + n->passes - 1) / n->passes;
   const int spp_total = spp_pass * n->passes;
   tpt_status st;
-  cache_destroy(c->cache);  // fresh cache for every render: reproducible online training
-  c->cache = nullptr;
-  if ((st = cache_create(c->device, n->seed, &c->cache)) != TPT_OK) return st;
+  // a fresh cache for every render (reproducible online training), unless
+  // warm_start continues from the context's cache
+  const bool warm = n->warm_start != 0 && c->cache != nullptr;
+  if (!warm) {
+    cache_destroy(c->cache);
+    c->cache = nullptr;
+    if ((st = cache_create(c->device, n->seed, &c->cache)) != TPT_OK) return st;
+  }
   if ((st = ensure(c->nrc_records, (size_t)n->record_cap * 5 * sizeof(float4))) != TPT_OK) return st;
   if ((st = ensure(c->nrc_queries, (size_t)n->query_cap * 6 * sizeof(float4))) != TPT_OK) return st;
   if ((st = ensure(c->nrc_counts, 2 * sizeof(unsigned))) != TPT_OK) return st;
@@ -2063,7 +2100,7 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
   const unsigned long long chunk = (unsigned long long)n->query_cap;  // samples per launch
   tpt_status result = TPT_OK;
   for (int pass = 0; pass < n->passes && result == TPT_OK; pass++) {
-    const bool cached = pass > 0;
+    const bool cached = pass > 0 || warm;  // a continued cache is queried from the first pass
     const int term = cached ? n->terminate_depth : (1 << 30);
     cudaMemsetAsync(counts, 0, sizeof(unsigned), c->stream);  // records of this pass
     const unsigned long long pass_begin = (unsigned long long)pass * spp_pass * npix;

@@ -790,6 +790,7 @@ tpt_status guide_refresh(GuideNet *G, int res, float4 *table, cudaStream_t s) {
 }
 
 float guide_last_loss(const GuideNet *G) { return G->last_loss; }
+tpt_mlp *guide_mlp(GuideNet *G) { return G->net; }
 
 // Radiance-cache network state used by the renderer.
 struct CacheNet {
@@ -876,6 +877,32 @@ tpt_status cache_infer(CacheNet *G, const float4 *queries, int count, float3 lo,
 }
 
 float cache_last_loss(const CacheNet *G) { return G->last_loss; }
+tpt_mlp *cache_mlp(CacheNet *G) { return G->net; }
+
+int64_t mlp_state_count(const tpt_mlp *M) { return 3 * (int64_t)M->params + 1; }
+
+tpt_status mlp_save_state(const tpt_mlp *M, float *out) {
+  const size_t P = (size_t)M->params;
+  MLP_CUDA(cudaSetDevice(M->device));
+  MLP_CUDA(cudaDeviceSynchronize());  // training runs on the caller's stream
+  MLP_CUDA(cudaMemcpy(out, M->w32, P * 4, cudaMemcpyDeviceToHost));
+  MLP_CUDA(cudaMemcpy(out + P, M->m, P * 4, cudaMemcpyDeviceToHost));
+  MLP_CUDA(cudaMemcpy(out + 2 * P, M->v, P * 4, cudaMemcpyDeviceToHost));
+  out[3 * P] = (float)M->steps;
+  return TPT_OK;
+}
+
+tpt_status mlp_load_state(tpt_mlp *M, const float *in) {
+  const size_t P = (size_t)M->params;
+  const float steps = in[3 * P];
+  if (!(steps >= 0.f && steps < 16777216.f) || steps != (float)(int)steps) return TPT_ERR_INVALID_ARGUMENT;
+  tpt_status st = tpt_mlp_set_params(M, in);  // weights (FP32 and FP16), gradient cleared
+  if (st != TPT_OK) return st;
+  MLP_CUDA(cudaMemcpy(M->m, in + P, P * 4, cudaMemcpyHostToDevice));
+  MLP_CUDA(cudaMemcpy(M->v, in + 2 * P, P * 4, cudaMemcpyHostToDevice));
+  M->steps = (int)steps;
+  return TPT_OK;
+}
 
 }  // namespace tpt
 

@@ -23,5 +23,13 @@ tpt_status cache_train(CacheNet *g, const float4 *records, int count, int steps,
 tpt_status cache_infer(CacheNet *g, const float4 *queries, int count, float3 lo, float3 ext, const float **y_out,
                        cudaStream_t s);
 float cache_last_loss(const CacheNet *g);
+
+// Checkpoint of a network's training state: weights, Adam moments, step
+// count (3 P + 1 floats); loading also refreshes the FP16 weights.
+tpt_mlp *guide_mlp(GuideNet *g);
+tpt_mlp *cache_mlp(CacheNet *g);
+int64_t mlp_state_count(const tpt_mlp *m);
+tpt_status mlp_save_state(const tpt_mlp *m, float *out);
+tpt_status mlp_load_state(tpt_mlp *m, const float *in);
 }  // namespace tpt
 #endif

@@ -76,7 +76,7 @@ class BatchItem(C.Structure):
 class GuideParams(C.Structure):
     _fields_ = [("passes", C.c_int32), ("train_steps", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float),
                 ("grid_res", C.c_int32), ("alpha", C.c_float), ("record_cap", C.c_int32), ("seed", C.c_uint64),
-                ("light_share", C.c_float)]
+                ("light_share", C.c_float), ("warm_start", C.c_int32)]
 
 
 class GuideStats(C.Structure):
@@ -90,7 +90,7 @@ class GuideStats(C.Structure):
 class NrcParams(C.Structure):
     _fields_ = [("passes", C.c_int32), ("train_steps", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float),
                 ("terminate_depth", C.c_int32), ("train_stride", C.c_int32), ("record_cap", C.c_int32),
-                ("query_cap", C.c_int32), ("seed", C.c_uint64)]
+                ("query_cap", C.c_int32), ("seed", C.c_uint64), ("warm_start", C.c_int32)]
 
 
 class NrcStats(C.Structure):
@@ -200,6 +200,8 @@ _SIGS = {
     "tpt_read_ppm": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "tpt_render_nrc": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.POINTER(NrcParams),
                                    C.c_void_p, C.c_int32, C.POINTER(RenderStats), C.POINTER(NrcStats)]),
+    "tpt_learned_save": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "tpt_learned_load": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),
     "tpt_quantize": (None, [C.c_void_p, C.c_int64, C.c_void_p]),
     "tpt_write_ppm": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int32, C.c_int32]),
 }
@@ -389,6 +391,27 @@ def render_guided(ctx: "Context", slot: int, width: int, height: int, spp: int, 
     check(lib().tpt_render_guided(ctx._h, slot, C.byref(p), C.byref(g), dst, mem, C.byref(st), C.byref(gs)),
           "render_guided")
     return img, st.as_dict(), gs.as_dict()
+
+
+NET_GUIDE, NET_CACHE = 0, 1
+
+
+def learned_save(ctx: "Context", which: int) -> np.ndarray:
+    """Checkpoint of the context's guiding network (NET_GUIDE) or radiance
+    cache (NET_CACHE): weights, Adam moments and step count
+    (tpt_learned_save)."""
+    n = C.c_int64()
+    check(lib().tpt_learned_save(ctx._h, which, None, 0, C.byref(n)), "learned_save")
+    out = np.zeros(n.value, np.float32)
+    check(lib().tpt_learned_save(ctx._h, which, _ptr(out), n.value, C.byref(n)), "learned_save")
+    return out
+
+
+def learned_load(ctx: "Context", which: int, state: np.ndarray) -> None:
+    """Restores a checkpoint; the next render with warm_start=1 continues
+    from it (tpt_learned_load)."""
+    state = np.ascontiguousarray(state, np.float32)
+    check(lib().tpt_learned_load(ctx._h, which, _ptr(state), state.size), "learned_load")
 
 
 def config(text: str | None = None, path: str | None = None) -> dict:
