@@ -1707,9 +1707,13 @@ extern "C" tpt_status tpt_autotune_batch(tpt_context *c, const tpt_batch_item *i
   for (int block : {64, 128})
     for (int var : {4, 5, 6})
       for (int flat : {16, 48}) cands.push_back({block, var, flat});
-  cudaEvent_t e0, e1;
-  TPT_CUDA(cudaEventCreate(&e0));
-  TPT_CUDA(cudaEventCreate(&e1));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t ce = cudaEventCreate(&e0);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+  if (ce != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    return cuda_status(ce);
+  }
   double best = -1.0;
   Cand win = cands[0];
   tpt_status st = TPT_OK;
@@ -1882,20 +1886,27 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
   if ((st = ensure(c->learn_pend, (size_t)g->record_cap * 5 * sizeof(float4))) != TPT_OK) return st;
   const unsigned long long per_pass = F.total;
   const uint32_t stride = (uint32_t)std::max<unsigned long long>(1ull, per_pass / (unsigned long long)g->record_cap);
-  cudaEvent_t e[4];
-  for (auto &ev : e) TPT_CUDA(cudaEventCreate(&ev));
-  double render_ms = 0.0, train_ms = 0.0;
-  long long records = 0, segments = 0;
   TPT_CUDA(cudaMemsetAsync(c->accum.p, 0, npix * sizeof(float4), c->stream));
   // records accumulate over the passes in a ring of record_cap entries
   TPT_CUDA(cudaMemsetAsync(c->guide_count.p, 0, sizeof(unsigned), c->stream));
+  cudaEvent_t e[4] = {};
+  for (auto &ev : e) {
+    const cudaError_t ce = cudaEventCreate(&ev);
+    if (ce != cudaSuccess) {
+      for (auto &x : e)
+        if (x) cudaEventDestroy(x);
+      return cuda_status(ce);
+    }
+  }
+  double render_ms = 0.0, train_ms = 0.0;
+  long long records = 0, segments = 0;
   unsigned emitted_before = 0;
   bool have_table = false;
-  if (warm) {  // the continued network guides from the first pass
-    if ((st = guide_refresh(c->guide, g->grid_res, (float4 *)c->guide_table.p, c->stream)) != TPT_OK) return st;
-    have_table = true;
-  }
   tpt_status result = TPT_OK;
+  if (warm) {  // the continued network guides from the first pass
+    result = guide_refresh(c->guide, g->grid_res, (float4 *)c->guide_table.p, c->stream);
+    have_table = result == TPT_OK;
+  }
   for (int pass = 0; pass < g->passes && result == TPT_OK; pass++) {
     GuideView gv{have_table ? (const float4 *)c->guide_table.p : nullptr, lo,
                  make_float3(1.f / ext.x, 1.f / ext.y, 1.f / ext.z), g->grid_res, g->alpha, g->light_share};
@@ -2091,11 +2102,18 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
   const int grid = grid_for(c, kern, block, smem);
   if ((st = ensure(c->learn_pend, (size_t)n->record_cap * 2 * sizeof(float4))) != TPT_OK) return st;
   unsigned *counts = (unsigned *)c->nrc_counts.p;  // [0] records, [1] queries
-  cudaEvent_t ev[6];
-  for (auto &x : ev) TPT_CUDA(cudaEventCreate(&x));
+  TPT_CUDA(cudaMemsetAsync(c->accum.p, 0, npix * sizeof(float4), c->stream));
+  cudaEvent_t ev[6] = {};
+  for (auto &x : ev) {
+    const cudaError_t ce = cudaEventCreate(&x);
+    if (ce != cudaSuccess) {
+      for (auto &y : ev)
+        if (y) cudaEventDestroy(y);
+      return cuda_status(ce);
+    }
+  }
   double render_ms = 0, infer_ms = 0, train_ms = 0;
   long long n_rec = 0, n_q = 0, segments = 0;
-  TPT_CUDA(cudaMemsetAsync(c->accum.p, 0, npix * sizeof(float4), c->stream));
   FrameDesc F{p->width, p->height, spp_pass, 0, (float4 *)c->accum.p, nullptr};
   const unsigned long long chunk = (unsigned long long)n->query_cap;  // samples per launch
   tpt_status result = TPT_OK;
