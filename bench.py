@@ -296,17 +296,19 @@ def learned_equal_time(ctx, which: str) -> dict:
     nrc:    the seeded next-week scene, 800x800, plain at 256 spp against the
             cached renderer (paths terminated into the cache after 2 bounces)
             at the spp that takes the same time; FP64 reference 4096 spp.
-    The reference's own noise adds ~spp/ref_spp of the plain relMSE to both."""
+    The equal-time side is the mean over three seeds (each run trains its own
+    network online; the per-seed ratios are reported too).  The reference's
+    own noise adds ~spp/ref_spp of the plain relMSE to both."""
     import torch
     import tpt
     from tpt import scenes
 
     if which == "guided":
         sd, w, h, spp, ref_spp = scenes.cornell_guiding(), 600, 600, 1024, 16384
-        run = lambda n, out: tpt.render_guided(ctx, slot, w, h, n, seed=5, out=out)
+        run = lambda n, out, sd_: tpt.render_guided(ctx, slot, w, h, n, seed=sd_, out=out)
     else:
         sd, w, h, spp, ref_spp = scenes.next_week(), 800, 800, 256, 4096
-        run = lambda n, out: tpt.render_nrc(ctx, slot, w, h, n, seed=5, out=out)
+        run = lambda n, out, sd_: tpt.render_nrc(ctx, slot, w, h, n, seed=sd_, out=out)
     slot = ctx.upload(tpt.Scene(sd.text()))
     # both sides use the engine the autotuner picks for this scene (physical
     # semantics): the plain baseline is the tracer's best configuration
@@ -326,22 +328,29 @@ def learned_equal_time(ctx, which: str) -> dict:
     t_plain, _ = timed(lambda: plain(spp))
     e_plain = _relmse(dev.cpu().numpy(), ref)
     passes = 8
+    seeds = (5, 6, 7)  # equal-time runs: the mean over three seeds (each run trains its own network)
 
     def compare(run):
-        run(spp, dev.data_ptr())  # warm-up
-        t_eq, r = timed(lambda: run(spp, dev.data_ptr()))
+        run(spp, dev.data_ptr(), seeds[0])  # warm-up
+        t_eq, r = timed(lambda: run(spp, dev.data_ptr(), seeds[0]))
         e_eq = _relmse(dev.cpu().numpy(), ref)
         spp_et = max(passes, int(round(spp * t_plain / t_eq / passes)) * passes)
-        t_et, _ = timed(lambda: run(spp_et, dev.data_ptr()))
-        e_et = _relmse(dev.cpu().numpy(), ref)
-        return ({"spp": spp, "ms": t_eq, "relmse": e_eq, "stats": r[2]}, {"spp": spp_et, "ms": t_et, "relmse": e_et},
-                {"equal_spp_relmse_ratio": e_eq / e_plain, "equal_time_relmse_ratio": e_et / e_plain,
+        t_et, e_et = [], []
+        for sd_ in seeds:
+            t, _ = timed(lambda: run(spp_et, dev.data_ptr(), sd_))
+            t_et.append(t)
+            e_et.append(_relmse(dev.cpu().numpy(), ref))
+        return ({"spp": spp, "ms": t_eq, "relmse": e_eq, "stats": r[2]},
+                {"spp": spp_et, "ms": float(np.mean(t_et)), "relmse": float(np.mean(e_et)), "seeds": list(seeds)},
+                {"equal_spp_relmse_ratio": e_eq / e_plain, "equal_time_relmse_ratio": float(np.mean(e_et)) / e_plain,
+                 "equal_time_relmse_ratio_per_seed": [e / e_plain for e in e_et],
                  "time_ratio_at_equal_spp": t_eq / t_plain})
 
     eq, et, ratios = compare(run)
     extra = {}
     if which == "guided":
-        _, et2, ratios2 = compare(lambda n, out: tpt.render_guided(ctx, slot, w, h, n, seed=5, out=out, alpha=0.25))
+        _, et2, ratios2 = compare(lambda n, out, sd_: tpt.render_guided(ctx, slot, w, h, n, seed=sd_, out=out,
+                                                                        alpha=0.25))
         extra = {"guided_alpha_0.25": dict(alpha=0.25, equal_time_spp=et2["spp"], equal_time_ms=et2["ms"],
                                            equal_time_relmse=et2["relmse"], **ratios2)}
     ctx.release(slot)
