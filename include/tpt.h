@@ -294,17 +294,22 @@ tpt_status tpt_render_batch(tpt_context *ctx, const tpt_batch_item *items, int32
 /* Autotuner: renders `probe_spp` samples per pixel (raised so that a probe
  * has at least 16 M samples: smaller probes measure launch tails) with each candidate
  * configuration - engine, threads per block, register variant, wavefront
- * queue size, stackless-walk threshold - times them with CUDA events, writes
- * the fastest into *p (engine, block, wave, flat_nodes; the other fields are
- * kept) and remembers it for the slot, so later renders of that slot with
- * engine = TPT_ENGINE_AUTO use it.  best_msps (may be NULL) receives the
- * winner's Msamples/s. */
+ * queue size, stackless-walk threshold - times them with CUDA events, times
+ * the three fastest again on a probe of ~0.1 s (at least 4x longer;
+ * fastest of three runs: the leaders are often within a percent or two, and
+ * a short probe's launch tail hides differences a full frame shows), writes
+ * the winner into *p
+ * (engine, block, wave, flat_nodes; the other fields are kept) and remembers
+ * it for the slot, so later renders of that slot with engine =
+ * TPT_ENGINE_AUTO use it.  best_msps (may be NULL) receives the winner's
+ * Msamples/s. */
 tpt_status tpt_autotune(tpt_context *ctx, int32_t slot, tpt_render_params *p, int32_t probe_spp, double *best_msps);
 /* Autotuner of a batch: renders the batch with every item's spp divided by
  * spp_divisor (at least 1) for each candidate block size, register variant
  * and stackless-walk threshold of the batched persistent launch, times them
- * with CUDA events and writes the fastest into p (block, wave, flat_nodes)
- * for tpt_render_batch.  best_msps (may be NULL) receives its Msamples/s. */
+ * with CUDA events, times the three fastest again (fastest of three runs)
+ * and writes the winner into p (block, wave, flat_nodes) for
+ * tpt_render_batch.  best_msps (may be NULL) receives its Msamples/s. */
 tpt_status tpt_autotune_batch(tpt_context *ctx, const tpt_batch_item *items, int32_t n, tpt_render_params *p,
                               int32_t spp_divisor, double *best_msps);
 

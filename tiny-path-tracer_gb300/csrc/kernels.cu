@@ -1714,29 +1714,51 @@ extern "C" tpt_status tpt_autotune_batch(tpt_context *c, const tpt_batch_item *i
     if (e0) cudaEventDestroy(e0);
     return cuda_status(ce);
   }
-  double best = -1.0;
-  Cand win = cands[0];
   tpt_status st = TPT_OK;
-  for (const Cand &cd : cands) {
+  // Msamples/s of a candidate: the fastest of `reps` timed runs after the
+  // run that captures its graph
+  auto measure = [&](const Cand &cd, int reps, double &msps) -> tpt_status {
     tpt_render_params q = *p;
     q.block = cd.block;
     q.wave = cd.variant;
     q.flat_nodes = cd.flat;
     q.profile = 0;
     tpt_render_stats rs{};
-    float ms = 0.f;
-    for (int rep = 0; rep < 2 && st == TPT_OK; rep++) {  // the first run captures the graph
+    float best_ms = 1e30f;
+    for (int rep = 0; rep <= reps; rep++) {
+      float ms = 0.f;
       cudaEventRecord(e0, c->stream);
-      st = tpt_render_batch(c, probe.data(), n, &q, TPT_MEM_DEVICE, &rs);
+      const tpt_status s2 = tpt_render_batch(c, probe.data(), n, &q, TPT_MEM_DEVICE, &rs);
+      if (s2 != TPT_OK) return s2;
       cudaEventRecord(e1, c->stream);
       cudaEventSynchronize(e1);
       cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) best_ms = std::min(best_ms, ms);
     }
-    if (st != TPT_OK) break;
-    const double msps = (double)rs.samples / (ms * 1e3);
-    if (msps > best) {
-      best = msps;
-      win = cd;
+    msps = (double)rs.samples / (best_ms * 1e3);
+    return TPT_OK;
+  };
+  std::vector<std::pair<double, int>> ranked;
+  for (int i = 0; i < (int)cands.size() && st == TPT_OK; i++) {
+    double msps = 0.0;
+    st = measure(cands[i], 1, msps);
+    ranked.push_back({msps, i});
+  }
+  // the best three again, fastest of three runs
+  double best = -1.0;
+  Cand win = cands[0];
+  if (st == TPT_OK) {
+    std::sort(ranked.begin(), ranked.end(), [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
+      return a.first > b.first;
+    });
+    win = cands[ranked[0].second];
+    for (int k = 0; k < 3 && k < (int)ranked.size() && st == TPT_OK; k++) {
+      double msps = 0.0;
+      st = measure(cands[ranked[k].second], 3, msps);
+      if (st == TPT_OK && msps > best) {
+        best = msps;
+        win = cands[ranked[k].second];
+      }
     }
   }
   cudaEventDestroy(e0);
@@ -1768,28 +1790,50 @@ extern "C" tpt_status tpt_autotune(tpt_context *c, int32_t slot, tpt_render_para
   probe_spp = std::max<int32_t>(probe_spp, (int32_t)((16ull << 20) / npix) + 1);
   tpt_status st;
   if ((st = ensure(c->staging, npix * 3 * sizeof(float))) != TPT_OK) return st;
-  double best = -1.0;
-  Cand win = cands[0];
-  for (const Cand &cd : cands) {
+  // Msamples/s of a candidate: the fastest of `reps` timed runs after one
+  // untimed run (caches, allocations)
+  auto measure = [&](const Cand &cd, int spp, int reps, double &msps) -> tpt_status {
     tpt_render_params q = *p;
     q.engine = cd.engine;
     q.block = cd.block;
     q.wave = cd.wave;
     q.flat_nodes = cd.flat;
-    q.spp = probe_spp;
+    q.spp = spp;
     q.profile = 0;
     q.accumulate_fp64 = 0;
     tpt_render_stats rs;
-    double t = 0.0;
-    for (int rep = 0; rep < 2; rep++) {  // first run warms caches and allocations
-      st = tpt_render(c, slot, &q, (float *)c->staging.p, TPT_MEM_DEVICE, &rs);
-      if (st != TPT_OK) return st;
-      t = rs.device_ms;
+    double t = 1e30;
+    for (int rep = 0; rep <= reps; rep++) {
+      const tpt_status s2 = tpt_render(c, slot, &q, (float *)c->staging.p, TPT_MEM_DEVICE, &rs);
+      if (s2 != TPT_OK) return s2;
+      if (rep > 0) t = std::min(t, rs.device_ms);
     }
-    const double msps = (double)npix * probe_spp / (t * 1e3);
+    msps = (double)npix * spp / (t * 1e3);
+    return TPT_OK;
+  };
+  std::vector<std::pair<double, int>> ranked;
+  for (int i = 0; i < (int)cands.size(); i++) {
+    double msps = 0.0;
+    if ((st = measure(cands[i], probe_spp, 1, msps)) != TPT_OK) return st;
+    ranked.push_back({msps, i});
+  }
+  // the leaders are often within a percent or two, and the launch tail of a
+  // short probe hides differences that show on a full frame: time the best
+  // three again on a probe of ~0.1 s (at least 4x the first), fastest of
+  // three runs
+  std::sort(ranked.begin(), ranked.end(), [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
+    return a.first > b.first;
+  });
+  const double long_spp = std::ceil(0.1 * ranked[0].first * 1e6 / (double)npix);
+  const int refine_spp = (int)std::min<double>(std::max<double>(4.0 * probe_spp, long_spp), 65536.0);
+  double best = -1.0;
+  Cand win = cands[ranked[0].second];
+  for (int k = 0; k < 3 && k < (int)ranked.size(); k++) {
+    double msps = 0.0;
+    if ((st = measure(cands[ranked[k].second], refine_spp, 3, msps)) != TPT_OK) return st;
     if (msps > best) {
       best = msps;
-      win = cd;
+      win = cands[ranked[k].second];
     }
   }
   p->engine = win.engine;
