@@ -26,6 +26,9 @@ def test_save_needs_a_trained_network(built):
     assert e.value.status == 10  # TPT_ERR_BAD_HANDLE
     with pytest.raises(tpt.TptError):
         tpt.learned_load(ctx, tpt.NET_CACHE, np.zeros(7, np.float32))  # wrong size
+    with pytest.raises(tpt.TptError) as e:  # and the failed load left no network behind
+        tpt.learned_save(ctx, tpt.NET_CACHE)
+    assert e.value.status == 10
     ctx.close()
 
 

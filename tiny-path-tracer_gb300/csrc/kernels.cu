@@ -2093,12 +2093,22 @@ extern "C" tpt_status tpt_learned_load(tpt_context *c, int32_t which, const floa
   if (!c || !in || (which != TPT_NET_GUIDE && which != TPT_NET_CACHE)) return TPT_ERR_INVALID_ARGUMENT;
   TPT_CUDA(cudaSetDevice(c->device));
   TPT_CUDA(cudaStreamSynchronize(c->stream));
+  // a context without the network gets one only if the checkpoint fits it
   tpt_status st;
-  if (which == TPT_NET_GUIDE && !c->guide && (st = guide_create(c->device, 1, &c->guide)) != TPT_OK) return st;
-  if (which == TPT_NET_CACHE && !c->cache && (st = cache_create(c->device, 1, &c->cache)) != TPT_OK) return st;
-  tpt_mlp *m = which == TPT_NET_GUIDE ? guide_mlp(c->guide) : cache_mlp(c->cache);
-  if (count != mlp_state_count(m)) return TPT_ERR_INVALID_ARGUMENT;
-  return mlp_load_state(m, in);
+  GuideNet *g = nullptr;
+  CacheNet *k = nullptr;
+  if (which == TPT_NET_GUIDE && !c->guide && (st = guide_create(c->device, 1, &g)) != TPT_OK) return st;
+  if (which == TPT_NET_CACHE && !c->cache && (st = cache_create(c->device, 1, &k)) != TPT_OK) return st;
+  tpt_mlp *m = which == TPT_NET_GUIDE ? guide_mlp(g ? g : c->guide) : cache_mlp(k ? k : c->cache);
+  st = count == mlp_state_count(m) ? mlp_load_state(m, in) : TPT_ERR_INVALID_ARGUMENT;
+  if (st != TPT_OK) {
+    guide_destroy(g);
+    cache_destroy(k);
+    return st;
+  }
+  if (g) c->guide = g;
+  if (k) c->cache = k;
+  return TPT_OK;
 }
 
 extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_render_params *p,
