@@ -63,12 +63,14 @@ def test_guided_gains_at_equal_spp(ctx):
     w = h = 64
     ref, _ = ctx.render(slot, w, h, 16384, semantics=tpt.SEMANTICS_PHYSICAL, seed=999, fp64=True)
     plain = [relmse(ctx.render(slot, w, h, 256, semantics=tpt.SEMANTICS_PHYSICAL, seed=20 + i)[0], ref)
-             for i in range(3)]
+             for i in range(5)]
     guided = [relmse(tpt.render_guided(ctx, slot, w, h, 256, seed=40 + i, passes=8, train_steps=32)[0], ref)
-              for i in range(3)]
-    print("relMSE plain", np.mean(plain), "guided", np.mean(guided))
-    # what the trained guide gains over the plain mixture: lower error per sample
-    assert np.mean(guided) < 0.95 * np.mean(plain)
+              for i in range(5)]
+    print("relMSE plain", plain, "guided", guided)
+    # what the trained guide gains over the plain mixture: lower error per
+    # sample.  Medians: at 64x64 one rare light path can dominate an image's
+    # relMSE (one guided seed in twenty measured 1.5x its median)
+    assert np.median(guided) < 0.9 * np.median(plain)
     ctx.release(slot)
 
 

@@ -267,6 +267,13 @@ __device__ __forceinline__ bool wf_training(const FrameDesc &F, const WfLearn &W
   const unsigned long long npix = (unsigned long long)F.nx * F.ny;
   return ((unsigned long long)(sample - W.sample_add) * npix + pixel) % W.stride == 0;
 }
+// A path's aux.w: the training flag (decided once, when the path is
+// generated: the 64-bit modulo above is too costly per vertex) and, for the
+// cache, the count of its records in the low bits.
+enum { AUX_TRAIN = 1 << 8, AUX_COUNT = 0xff };
+__device__ __forceinline__ int4 fresh_aux(const FrameDesc &F, const WfLearn &W, uint32_t pixel, uint32_t sample) {
+  return make_int4(-1, -1, -1, wf_training(F, W, pixel, sample) ? AUX_TRAIN : 0);
+}
 
 // Fills slots [0, count) with camera samples first..first+count of a learned pass.
 __global__ void k_wf_generate_learn(DevScene S, FrameDesc F, PathBuf out, unsigned count, uint2 key, WfLearn W) {
@@ -277,7 +284,7 @@ __global__ void k_wf_generate_learn(DevScene S, FrameDesc F, PathBuf out, unsign
     sample += W.sample_add;
     const Ray r = camera_ray(S.cam, i, j, F.nx, F.ny, pixel, sample, key);
     write_path(out, k, r, 0, v3(1.f, 1.f, 1.f), v3(0.f, 0.f, 0.f), pixel, sample);
-    out.aux[k] = make_int4(-1, -1, -1, 0);
+    out.aux[k] = fresh_aux(F, W, pixel, sample);
   }
 }
 
@@ -320,7 +327,7 @@ __global__ void k_wf_shade_learn(DevScene S, RenderCfg cfg, FrameDesc F, PathBuf
       Lb = L;
       const int4 hv = hits[k];
       const HitRef h{__int_as_float(hv.x), hv.y, hv.z, hv.w};
-      const bool training = wf_training(F, W, pixel, sample);
+      const bool training = (aux.w & AUX_TRAIN) != 0;
       if (MODE == 1) {
         grec.valid = aux.x >= 0 || !training;  // only recording paths without a record yet take one
         const bool had = grec.valid;
@@ -328,7 +335,7 @@ __global__ void k_wf_shade_learn(DevScene S, RenderCfg cfg, FrameDesc F, PathBuf
         new_rec = !had && grec.valid && finite3(grec.x) && finite3(grec.n) && finite3(grec.d);
       } else {
         const bool may_query = !training && depth >= W.term_depth;
-        const bool rec_here = training && hv.y >= 0 && aux.w < 3;
+        const bool rec_here = training && hv.y >= 0 && (aux.w & AUX_COUNT) < 3;
         bool queried = false;
         cont = shade_vertex_t<false>(S, cfg, r, hv.y >= 0, h, T, L, depth, pixel, sample, W.gv, grec,
                                      (rec_here || may_query) ? &vi : nullptr, may_query ? W.term_depth : (1 << 30),
@@ -373,8 +380,8 @@ __global__ void k_wf_shade_learn(DevScene S, RenderCfg cfg, FrameDesc F, PathBuf
           W.pend[2 * (size_t)rs + 1] = make_float4(Lb.x, Lb.y, Lb.z, 0.f);
         }
         const int slot = rs < W.rec_cap ? (int)rs : -1;
-        if (aux.w == 0) aux.x = slot;
-        else if (aux.w == 1) aux.y = slot;
+        if ((aux.w & AUX_COUNT) == 0) aux.x = slot;
+        else if ((aux.w & AUX_COUNT) == 1) aux.y = slot;
         else aux.z = slot;
         aux.w++;
       }
@@ -400,7 +407,7 @@ __global__ void k_wf_shade_learn(DevScene S, RenderCfg cfg, FrameDesc F, PathBuf
       }
       if (MODE == 2) {
         const int slots[3] = {aux.x, aux.y, aux.z};
-        for (int j = 0; j < aux.w && j < 3; j++) {
+        for (int j = 0; j < (aux.w & AUX_COUNT) && j < 3; j++) {
           const int sl = slots[j];
           if (sl < 0) continue;
           const float4 pT = W.pend[2 * (size_t)sl], pL = W.pend[2 * (size_t)sl + 1];
@@ -434,7 +441,7 @@ __global__ void k_wf_shade_learn(DevScene S, RenderCfg cfg, FrameDesc F, PathBuf
         depth = 0;
         T = v3(1.f, 1.f, 1.f);
         L = v3(0.f, 0.f, 0.f);
-        aux = make_int4(-1, -1, -1, 0);
+        aux = fresh_aux(F, W, pixel, sample);
         fresh = true;
       }
     }
