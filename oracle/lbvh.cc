@@ -1,8 +1,8 @@
 /*
  * lbvh.cc - CPU restatement of the GPU linear-BVH build (TPT_BVH_LBVH).
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the product's GPU builder
- * (tiny-path-tracer_gb300/csrc/lbvh.cu).  The reference has no such builder
+ * TEST INFRASTRUCTURE ONLY: the tests compare the product's GPU builder
+ * (tiny-path-tracer_gb300/csrc/lbvh.cu) against it.  The reference has no such builder
  * (its bvh_node, hitable.cc:32-56, splits at the median of a random axis on
  * the host); this is the opt-in alternative topology, restated from the
  * published algorithm:

@@ -1,7 +1,7 @@
 """CPU reference of the learned parts' networks and losses (numpy, float64).
 
-TEST INFRASTRUCTURE ONLY: the checker for the GPU kernels of
-tiny-path-tracer_gb300/csrc/learn.cu.  The MLP is in -> [64 ReLU] x
+TEST INFRASTRUCTURE ONLY: the tests compare the GPU kernels of
+tiny-path-tracer_gb300/csrc/learn.cu against it.  The MLP is in -> [64 ReLU] x
 n_hidden -> out, no biases, weights row-major [out][in] per layer,
 concatenated.  The GPU stores weights and activations in f16 and
 accumulates in f32; callers pass f16-rounded weights and inputs, and compare

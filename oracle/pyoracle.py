@@ -1,9 +1,10 @@
 """ctypes bindings of the CPU oracle (liboracle.so) and of the reference
 harness (_ref/libtptref.so).
 
-TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
-by bench.py's CPU-baseline / reference legs, always as the checker or the
-timed CPU baseline - never as the product path.
+TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke() entry point and
+by bench.py's CPU-baseline / reference legs, always as the reference that
+results are compared against or as the timed CPU baseline - never as the
+product path.
 """
 from __future__ import annotations
 

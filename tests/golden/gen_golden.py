@@ -1,6 +1,6 @@
 """Generates the golden fixtures in this directory from the REFERENCE itself.
 
-Run here, where the reference checkout exists (the GPU machine has none):
+Run where the reference checkout exists (the GPU test machines have none):
 
     make -C oracle REF=/root/reference && python tests/golden/gen_golden.py
 
