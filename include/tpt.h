@@ -364,7 +364,7 @@ typedef struct {
   float lr;             /* Adam learning rate (1e-3) */
   int32_t grid_res;     /* table cells per axis (16) */
   float alpha;          /* guide probability at a diffuse vertex (0.5) */
-  int32_t record_cap;   /* training records kept per pass */
+  int32_t record_cap;   /* training records kept per pass (1 to 2^28) */
   uint64_t seed;        /* network initialisation and record sampling */
   float light_share;    /* probability of light sampling within the non-guide part
                            (0.5: the plain tracer's light/cosine mixture; 0: cosine

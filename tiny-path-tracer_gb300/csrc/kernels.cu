@@ -274,8 +274,28 @@ enum { AUX_TRAIN = 1 << 8, AUX_COUNT = 0xff };
 __device__ __forceinline__ int4 fresh_aux(const FrameDesc &F, const WfLearn &W, uint32_t pixel, uint32_t sample) {
   return make_int4(-1, -1, -1, wf_training(F, W, pixel, sample) ? AUX_TRAIN : 0);
 }
+// Path guiding needs only the pending-record slot and the training flag: one
+// int per path instead of the int4 (bits 0-29: slot + 1, bit 30: training),
+// which spares the shade kernel 24 B of the path state's traffic each way.
+__device__ __forceinline__ int pack_aux1(const int4 &a) { return (a.x + 1) | ((a.w & AUX_TRAIN) ? (1 << 30) : 0); }
+__device__ __forceinline__ int4 unpack_aux1(int v) {
+  return make_int4((v & 0x3fffffff) - 1, -1, -1, (v >> 30) & 1 ? AUX_TRAIN : 0);
+}
+template <int MODE>
+__device__ __forceinline__ int4 load_aux(const PathBuf &b, unsigned k) {
+  if (MODE == 1) return unpack_aux1(reinterpret_cast<const int *>(b.aux)[k]);
+  return b.aux[k];
+}
+template <int MODE>
+__device__ __forceinline__ void store_aux(const PathBuf &b, unsigned k, const int4 &a) {
+  if (MODE == 1)
+    reinterpret_cast<int *>(b.aux)[k] = pack_aux1(a);
+  else
+    b.aux[k] = a;
+}
 
 // Fills slots [0, count) with camera samples first..first+count of a learned pass.
+template <int MODE>
 __global__ void k_wf_generate_learn(DevScene S, FrameDesc F, PathBuf out, unsigned count, uint2 key, WfLearn W) {
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
     uint32_t pixel, sample;
@@ -284,7 +304,7 @@ __global__ void k_wf_generate_learn(DevScene S, FrameDesc F, PathBuf out, unsign
     sample += W.sample_add;
     const Ray r = camera_ray(S.cam, i, j, F.nx, F.ny, pixel, sample, key);
     write_path(out, k, r, 0, v3(1.f, 1.f, 1.f), v3(0.f, 0.f, 0.f), pixel, sample);
-    out.aux[k] = fresh_aux(F, W, pixel, sample);
+    store_aux<MODE>(out, k, fresh_aux(F, W, pixel, sample));
   }
 }
 
@@ -322,7 +342,7 @@ __global__ void k_wf_shade_learn(DevScene S, RenderCfg cfg, FrameDesc F, PathBuf
       L = v3(rs.x, rs.y, rs.z);
       pixel = (uint32_t)__float_as_int(tp.w);
       sample = (uint32_t)__float_as_int(rs.w);
-      aux = in.aux[k];
+      aux = load_aux<MODE>(in, k);
       Tb = T;
       Lb = L;
       const int4 hv = hits[k];
@@ -449,7 +469,7 @@ __global__ void k_wf_shade_learn(DevScene S, RenderCfg cfg, FrameDesc F, PathBuf
     const unsigned slot = warp_append(emit, &C->count[cur ^ 1]);
     if (emit) {
       write_path(out, slot, r, depth, T, L, pixel, sample);
-      out.aux[slot] = aux;
+      store_aux<MODE>(out, slot, aux);
     }
   }
 }
@@ -1310,7 +1330,7 @@ static tpt_status run_wavefront_t(tpt_context *c, const DevScene &S, const Rende
   if constexpr (MODE == 0)
     k_wf_generate<<<g_gen, block, 0, c->stream>>>(S, F, P[0], 0ull, first, cfg.key);
   else
-    k_wf_generate_learn<<<g_gen, block, 0, c->stream>>>(S, F, P[0], first, cfg.key, *W);
+    k_wf_generate_learn<MODE == 0 ? 1 : MODE><<<g_gen, block, 0, c->stream>>>(S, F, P[0], first, cfg.key, *W);
   TPT_CUDA(cudaGetLastError());
   int launches = 1;
   const int g_tr = grid_for(c, traverse, block, smem);
@@ -1889,6 +1909,7 @@ extern "C" tpt_status tpt_render_guided(tpt_context *c, int32_t slot, const tpt_
   if (slot < 0 || slot >= (int32_t)c->slots.size() || !c->slots[slot].live) return TPT_ERR_BAD_HANDLE;
   if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->max_depth < 0 || g->passes < 1 ||
       p->semantics != TPT_SEMANTICS_PHYSICAL || g->grid_res < 1 || g->grid_res > 64 || g->record_cap < 1 ||
+      g->record_cap > (1 << 28) ||
       !(g->alpha >= 0.f && g->alpha <= 1.f) || !(g->light_share >= 0.f && g->light_share <= 1.f) || g->batch < 16)
     return TPT_ERR_INVALID_ARGUMENT;
   TPT_CUDA(cudaSetDevice(c->device));
