@@ -26,7 +26,7 @@ constexpr int HID = 64;
 constexpr int MAX_IN = 128;
 constexpr int MAX_OUT = 64;
 constexpr int MAX_HIDDEN = 6;
-constexpr int WARPS = 4;  // warps per CTA (64 rows per CTA step)
+constexpr int WARPS = 8;  // warps per CTA (128 rows per CTA step)
 
 struct Net {
   int in_dim, n_hidden, out_dim;
