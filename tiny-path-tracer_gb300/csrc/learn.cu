@@ -237,15 +237,20 @@ __global__ void __launch_bounds__(128) k_mlp_wgrad(Net n, const __half *__restri
   }
   const int r0 = ck * WG_ROWS, nr = min(WG_ROWS, rows - r0);  // nr: a multiple of 16
   __half *sH = wsm, *sZ = wsm + (size_t)K * WG_LD;
-  // stage: row q of (Ht | dZt) holds chunk rows r0 .. r0+nr of input (output) q
+  // stage: row q of (Ht | dZt) holds chunk rows r0 .. r0+nr of input (output)
+  // q, as asynchronous 16-byte global-to-shared copies (every row start is
+  // 16-byte aligned: rows, r0 and the row stride are multiples of 8 halves),
+  // so a thread keeps all its copies in flight instead of a load-store chain
   const int vec = nr / 8;  // 16-byte pieces per row
   for (int idx = threadIdx.x; idx < (K + N) * vec; idx += blockDim.x) {
     const int q = idx / vec, v = idx - q * vec;
     const __half *src = q < K ? Ht + ht_off + (size_t)q * rows + r0 + v * 8
                               : dZt + dz_off + (size_t)(q - K) * rows + r0 + v * 8;
     __half *dst = (q < K ? sH + (size_t)q * WG_LD : sZ + (size_t)(q - K) * WG_LD) + v * 8;
-    *reinterpret_cast<uint4 *>(dst) = __ldg(reinterpret_cast<const uint4 *>(src));
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
   }
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   if (warp * 16 >= N) return;
