@@ -89,3 +89,30 @@ def test_lbvh_batch_matches_reference_topology(ctx):
         np.testing.assert_allclose(b, a, rtol=1e-4, atol=1e-5)
     for s in ref + lb:
         ctx.release(s)
+
+
+def test_nested_bvh_nodes_trace_as_the_reference(ctx):
+    """bvh_nodes nested in a bvh_node: the rebuilt topologies flatten them
+    into one tree and still report the reference's closest hits."""
+    rng = np.random.default_rng(5)
+    sd = scenes.SD()
+    m = sd.lambertian(sd.const(0.5, 0.5, 0.5))
+    inner = []
+    for g in range(2):
+        sph = [sd.sphere(rng.uniform(-5, 5, 3) + [10 * g, 0, 0], float(rng.uniform(0.2, 1.0)), m) for _ in range(40)]
+        inner.append(sd.bvh(sph))
+    sd.world(sd.bvh(inner + [sd.box((-1, -1, -1), (1, 1, 1), m)]))
+    sd.camera((0, 0, 30), (5, 0, 0), (0, 1, 0), 40.0, 1.0, 0.0, 10.0)
+    text = sd.text()
+    ora = pyoracle.Scene(text)
+    rays = ora.make_rays(20_000, 31, 0.5, 0.05)
+    of, oi = ora.trace(rays, seed=5, media_mode=0)
+    for bvh in ("sah", "lbvh"):
+        slot = ctx.upload(tpt.Scene(text, bvh=bvh))
+        f, i = ctx.trace_closest(slot, rays, seed=5)
+        ctx.release(slot)
+        assert np.array_equal(i[:, 0], oi[:, 0]), bvh
+        hit = oi[:, 0] == 1
+        np.testing.assert_allclose(f[hit, 0], of[hit, 0], rtol=1e-5, atol=1e-6)
+        differ = hit & (i[:, 1] != oi[:, 1])
+        assert (f[differ, 0] == of[differ, 0]).all(), bvh  # only exact ties may pick another primitive

@@ -144,3 +144,43 @@ def test_host_compiler_reserves_lbvh_slots(built):
         assert lb["n_nodes"] == sah["n_nodes"]
         assert lb["n_leaves"] == sah["n_leaves"]
         assert lb["arena_bytes"] > sah["arena_bytes"]  # build inputs and scratch
+
+
+def nested_bvh_scene():
+    """Spheres in two bvh_nodes nested inside a third, plus a box: the LBVH
+    and SAH rebuilds flatten the nesting into one tree over the primitives."""
+    from tpt import scenes
+
+    rng = np.random.default_rng(5)
+    sd = scenes.SD()
+    m = sd.lambertian(sd.const(0.5, 0.5, 0.5))
+    inner = []
+    for g in range(2):
+        sph = [sd.sphere(rng.uniform(-5, 5, 3) + [10 * g, 0, 0], float(rng.uniform(0.2, 1.0)), m) for _ in range(40)]
+        inner.append(sd.bvh(sph))
+    outer = sd.bvh(inner + [sd.box((-1, -1, -1), (1, 1, 1), m)])
+    sd.world(outer)
+    sd.camera((0, 0, 30), (5, 0, 0), (0, 1, 0), 40.0, 1.0, 0.0, 10.0)
+    return sd.text()
+
+
+def test_nested_bvh_nodes_become_one_tree(built):
+    import tpt
+
+    text = nested_bvh_scene()
+    for bvh in ("sah", "lbvh"):
+        info = tpt.Scene(text, bvh=bvh).info()
+        assert info["n_leaves"] == 81 and info["n_nodes"] == 80, (bvh, info)  # n - 1 nodes over 81 primitives
+    ref = tpt.Scene(text).info()
+    assert ref["n_leaves"] == 81 and ref["n_nodes"] > 80  # the reference keeps the nesting (n == 1 nodes too)
+
+
+def test_unknown_topology_is_rejected(built):
+    import ctypes as C
+
+    import tpt
+
+    h = C.c_void_p()
+    err = C.create_string_buffer(256)
+    st = tpt.lib().tpt_scene_from_text_opt(nested_bvh_scene().encode(), 3, C.byref(h), err, 256)
+    assert st == 1 and not h.value  # TPT_ERR_INVALID_ARGUMENT, no scene
