@@ -116,3 +116,32 @@ def test_nested_bvh_nodes_trace_as_the_reference(ctx):
         np.testing.assert_allclose(f[hit, 0], of[hit, 0], rtol=1e-5, atol=1e-6)
         differ = hit & (i[:, 1] != oi[:, 1])
         assert (f[differ, 0] == of[differ, 0]).all(), bvh  # only exact ties may pick another primitive
+
+
+def test_moving_spheres_under_rebuilt_topologies(ctx):
+    """Moving spheres (boxes over the bvh_node's shutter interval) under the
+    rebuilt topologies: the reference's closest hits at each ray's time."""
+    rng = np.random.default_rng(9)
+    sd = scenes.SD()
+    m = sd.lambertian(sd.const(0.4, 0.6, 0.5))
+    items = []
+    for _ in range(60):
+        c0 = rng.uniform(-6, 6, 3)
+        items.append(sd.moving_sphere(c0, c0 + rng.uniform(-1, 1, 3), 0.0, 1.0, float(rng.uniform(0.2, 0.8)), m))
+    items += [sd.sphere(rng.uniform(-6, 6, 3), float(rng.uniform(0.2, 0.8)), m) for _ in range(20)]
+    sd.world(sd.bvh(items, 0.0, 1.0))
+    sd.camera((0, 2, 25), (0, 0, 0), (0, 1, 0), 40.0, 1.0, 0.0, 10.0, 0.0, 1.0)
+    text = sd.text()
+    ora = pyoracle.Scene(text)
+    rays = ora.make_rays(20_000, 17, 0.5, 0.05)
+    of, oi = ora.trace(rays, seed=5, media_mode=0)
+    assert (oi[:, 0] == 1).mean() > 0.05  # the batch does hit the spheres
+    for bvh in ("sah", "lbvh"):
+        slot = ctx.upload(tpt.Scene(text, bvh=bvh))
+        f, i = ctx.trace_closest(slot, rays, seed=5)
+        ctx.release(slot)
+        assert np.array_equal(i[:, 0], oi[:, 0]), bvh
+        hit = oi[:, 0] == 1
+        np.testing.assert_allclose(f[hit, 0], of[hit, 0], rtol=1e-5, atol=1e-6)
+        differ = hit & (i[:, 1] != oi[:, 1])
+        assert (f[differ, 0] == of[differ, 0]).all(), bvh
