@@ -52,9 +52,9 @@ WORKLOAD = "cornell_box_600x600_1024spp_depth50"
 BYTES_PER_SEGMENT = 192
 TRAVERSE_BYTES_PER_SEGMENT = 64 + 16  # traverse reads the path record, writes the hit
 # k_persistent DRAM read+write bytes and warp instructions per ray segment,
-# from the ncu capture of the 16 spp case in the tuned launch (block 64,
-# 5-block register variant; profiles/k_persistent_cornell_600x600_16spp.md):
-# 9.174 MB and 3.412 G warp instructions over 30.42 M segments
+# from the ncu capture (--set full) of this script's 16 spp case in the tuned
+# launch (--spp 16 --engine 2 --block 64 --wave 5): 9.174 MB and 3.412 G warp
+# instructions over 30.42 M segments
 NCU_DRAM_BYTES_PER_SEGMENT = (8.19712e6 + 0.976896e6) / 30416883
 NCU_WARP_INST_PER_SEGMENT = 3411932611 / 30416883
 # instruction issue peak: 152 SMs x 4 schedulers x 1 warp instruction per
