@@ -483,7 +483,7 @@ def main() -> None:
         algo_bytes = seg_per_launch * per_seg
         achieved = algo_bytes / (tr_ms / tr_n / 1e3) / 1e9
         # DRAM bytes per segment from the ncu capture of the same kernel on the
-        # 16 spp case (profiles/), scaled to this launch's segments
+        # 16 spp case (NCU_DRAM_BYTES_PER_SEGMENT), scaled to this launch's segments
         traffic = None if wavefront else seg_per_launch * NCU_DRAM_BYTES_PER_SEGMENT
         roof = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
