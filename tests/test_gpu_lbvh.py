@@ -145,3 +145,36 @@ def test_moving_spheres_under_rebuilt_topologies(ctx):
         np.testing.assert_allclose(f[hit, 0], of[hit, 0], rtol=1e-5, atol=1e-6)
         differ = hit & (i[:, 1] != oi[:, 1])
         assert (f[differ, 0] == of[differ, 0]).all(), bvh
+
+
+def _chain_points():
+    """Centroids whose Morton codes have one bit each, at 57 positions: the
+    radix tree over them is a chain of depth 57."""
+    pts = [[0.0, 0.0, 0.0]]
+    for a in range(3):
+        for k in range(2, 21):
+            p = [0.0, 0.0, 0.0]
+            p[a] = float(2 ** k)
+            pts.append(p)
+    pts.append([2.0 ** 21] * 3)
+    return np.array(pts, np.float32)
+
+
+def test_too_deep_lbvh_fails_at_upload(ctx):
+    pts = _chain_points()
+    boxes = np.hstack([pts - 0.25, pts + 0.25]).astype(np.float32)
+    _, _, _, depth = ctx.bvh_build_boxes(boxes)
+    assert depth == pyoracle.lbvh_build(boxes)[3] == 57
+    sd = scenes.SD()
+    m = sd.lambertian(sd.const(0.5, 0.5, 0.5))
+    sd.world(sd.bvh([sd.sphere(p, 0.25, m) for p in pts]))
+    sd.camera((0, 0, -10), (0, 0, 0), (0, 1, 0), 40.0, 1.0, 0.0, 10.0)
+    text = sd.text()
+    # the traversal stack holds 32 entries: the upload refuses the tree
+    with pytest.raises(tpt.TptError) as e:
+        ctx.upload(tpt.Scene(text, bvh="lbvh"))
+    assert e.value.status == 8  # TPT_ERR_STACK_OVERFLOW
+    assert b"LBVH of depth 57" in tpt.lib().tpt_last_error()
+    # the reference's median-split tree over the same spheres is shallow
+    slot = ctx.upload(tpt.Scene(text))
+    ctx.release(slot)
