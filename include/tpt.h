@@ -250,10 +250,10 @@ tpt_status tpt_render(tpt_context *ctx, int32_t slot, const tpt_render_params *p
 
 /* Render without allocating any memory (no counterpart in the reference).
  * For callers that cannot call cudaMalloc: a plugin inside a host program
- * that owns all device memory through its own pool, code running while a
- * CUDA graph is being captured, or a real-time loop that must not take the
- * implicit device synchronisation of an allocation.  The caller passes, in
- * memory it owns:
+ * that owns all device memory through its own pool (an allocation behind the
+ * pool's back breaks its accounting or fails under its memory cap), or a
+ * real-time loop that must not take the implicit device synchronisation of
+ * an allocation.  The caller passes, in memory it owns:
  *   arena_dev    device buffer of at least tpt_scene_info.arena_bytes bytes;
  *                each call copies the compiled scene into it (host-to-device
  *                copies only),
@@ -264,11 +264,16 @@ tpt_status tpt_render(tpt_context *ctx, int32_t slot, const tpt_render_params *p
  * array of TPT_NOALLOC_MAX_PIXELS*16 + 256 bytes (16 MiB), which every GPU
  * that loads the library holds until the process exits; images of more than
  * TPT_NOALLOC_MAX_PIXELS pixels are rejected with TPT_ERR_INVALID_ARGUMENT.
- * The persistent engine renders; the call returns after the stream has
- * finished.  The first call on a device looks up the array's device address
+ * The persistent engine renders.  The call is synchronous: it waits for
+ * `stream` before it returns (it reads the kernels' error flag back).  The
+ * first call on a device looks up the array's device address
  * (cudaGetSymbolAddress), so make that first call before any stream capture.
- * All calls share the array: calls that overlap on the GPU (other threads,
- * other streams) race and corrupt each other's images. */
+ * All calls share the array, which keeps the last call's contents (each call
+ * clears what it uses): calls that overlap on the GPU (other threads, other
+ * streams) race and corrupt each other's images.  Fields of
+ * tpt_render_params this call ignores: engine (always persistent), profile;
+ * accumulate_fp64 = 1 is rejected with TPT_ERR_INVALID_ARGUMENT.  Every
+ * TPT_ERR_INVALID_ARGUMENT return leaves its reason in tpt_last_error(). */
 #define TPT_NOALLOC_MAX_PIXELS (1 << 20)
 tpt_status tpt_render_noalloc(const tpt_scene *scene, void *arena_dev, int64_t arena_bytes,
                               const tpt_render_params *p, float *out_rgb_dev, void *stream);
@@ -341,6 +346,28 @@ tpt_status tpt_mlp_backward_given(tpt_mlp *m, const void *x_f16, const float *dy
  * receives the unscaled loss sum. */
 tpt_status tpt_mlp_backward_vmf(tpt_mlp *m, const void *x_f16, const float *target, int64_t rows, float scale,
                                 float *loss_out, void *stream);
+/* Radiance-cache network only: accumulates the weight gradient of the
+ * relative L2 loss of Mueller et al. 2021, sum_rows sum_rgb
+ * (y - t)^2 / (sg(y)^2 + 0.01) with the denominator held constant, times
+ * `scale`; target: f32 [rows][4] = (rgb, unused).  loss_out (host, may be
+ * NULL) receives the unscaled loss sum. */
+tpt_status tpt_mlp_backward_rel_l2(tpt_mlp *m, const void *x_f16, const float *target, int64_t rows, float scale,
+                                   float *loss_out, void *stream);
+/* The learned parts' input encodings, one row per record (device buffers).
+ * tpt_guide_encode: records of 3 float4 (position, weight), (normal, -),
+ * (sampled direction, -) -> f16 rows of 112: the position normalised to the
+ * box [lo, lo + extent] as a one-blob of 32 bins per axis, then the normal;
+ * target (may be NULL) receives (direction, weight) per row, an unusable
+ * record (non-finite or negative weight) a zero weight.
+ * tpt_nrc_encode: records of `stride` float4 (>= 4; the first four are
+ * (position, roughness), (outgoing direction, -), (normal, -), (albedo, -))
+ * -> f16 rows of 64: a 12-octave triangle wave per position axis, spherical
+ * one-blobs (4 + 4 bins) of the direction and the normal, a 4-bin roughness
+ * one-blob, the albedo. */
+tpt_status tpt_guide_encode(const float *records, int64_t count, const float *lo, const float *extent, void *x_f16,
+                            float *target, void *stream);
+tpt_status tpt_nrc_encode(const float *records, int64_t count, int32_t stride, const float *lo, const float *extent,
+                          void *x_f16, void *stream);
 /* Adam step (lr, beta 0.9/0.999, eps 1e-8) on the accumulated gradient
  * multiplied by inv_loss_scale; clears the gradient. */
 tpt_status tpt_mlp_adam(tpt_mlp *m, float lr, float inv_loss_scale, void *stream);

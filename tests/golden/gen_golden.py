@@ -2,7 +2,7 @@
 
 Run where the reference checkout exists (the GPU test machines have none):
 
-    make -C oracle REF=/root/reference && python tests/golden/gen_golden.py
+    make -C oracle REF=<reference checkout> && python tests/golden/gen_golden.py [scene ...]
 
 It loads each preset scene into the reference harness (oracle/_ref, the
 reference's unmodified src/*.cc compiled by oracle/Makefile) and records:
@@ -35,15 +35,20 @@ sys.path.insert(0, os.path.join(ROOT, "tiny-path-tracer_gb300"))
 import pyoracle  # noqa: E402
 from tpt import scenes  # noqa: E402
 
-TRACE_SCENES = ["cornell", "one_weekend", "cornell_guiding", "ties", "instances", "next_week"]
+TRACE_SCENES = ["cornell", "one_weekend", "cornell_guiding", "ties", "instances", "next_week",
+                "metals", "textures", "motion", "media"]
 RENDERS = {  # scene: (width, height, spp, max_depth, runs)
     "cornell": (48, 48, 64, 50, 8),
     "cornell_guiding": (48, 48, 64, 50, 8),
+    "metals": (48, 48, 64, 50, 8),
+    "textures": (48, 48, 64, 50, 8),
+    "motion": (48, 48, 64, 50, 8),
+    "media": (48, 48, 64, 50, 8),
 }
 N_RAYS = 2048
 
 
-EDGE_SCENES = ["cornell", "one_weekend", "instances", "next_week"]
+EDGE_SCENES = ["cornell", "one_weekend", "instances", "next_week", "metals", "textures"]
 
 
 def edge_rays(sd, seed: int) -> np.ndarray:
@@ -108,10 +113,12 @@ def bvh_ids(sd) -> list[int]:
     return [int(l.split()[1]) for l in sd.lines if l.startswith("node ") and l.split()[2] == "bvh_node"]
 
 
-def main() -> None:
+def main(only: list[str]) -> None:
+    """Regenerates the fixtures of the scenes named in `only` (all when empty)."""
     if not pyoracle.ref_available():
         raise SystemExit("reference harness not built: make -C oracle REF=/path/to/reference")
-    for name in TRACE_SCENES:
+    pick = (lambda names: [n for n in names if n in only]) if only else (lambda names: list(names))
+    for name in pick(TRACE_SCENES):
         sd = scenes.PRESETS[name]()
         text = sd.text()
         with open(os.path.join(HERE, f"{name}.sd"), "w") as f:
@@ -128,13 +135,14 @@ def main() -> None:
             dumps[f"kids_{b}"] = kids
         np.savez_compressed(os.path.join(HERE, f"{name}_bvh.npz"), **dumps)
         print(name, "trace + bvh", hi[:, 0].sum(), "hits")
-    for name in EDGE_SCENES:
+    for name in pick(EDGE_SCENES):
         text = scenes.PRESETS[name]().text()
         rays = edge_rays(scenes.PRESETS[name](), 77)
         hf, hi = pyoracle.RefScene(text).trace(rays)
         np.savez_compressed(os.path.join(HERE, f"{name}_edge.npz"), rays=rays, hit_f=hf, hit_i=hi)
         print(name, "edge rays", len(rays), hi[:, 0].sum(), "hits")
-    for name, (w, h, spp, depth, runs) in RENDERS.items():
+    for name in pick(RENDERS):
+        w, h, spp, depth, runs = RENDERS[name]
         text = scenes.PRESETS[name]().text()
         ref = pyoracle.RefScene(text)
         imgs = []
@@ -147,4 +155,4 @@ def main() -> None:
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -1,7 +1,9 @@
 """Batched rendering (one persistent launch over many scenes, replayed from a
-CUDA graph) and the autotuner.  An item of a batch must equal tpt_render of
-the same scene with the same parameters: both draw each sample from the same
-counter-based stream, so images differ only by float accumulation order."""
+CUDA graph) and the autotuner.  The items of a batch agree statistically
+with the CPU oracle's renders of their scenes, and an item must equal
+tpt_render of the same scene with the same parameters: both draw each
+sample from the same counter-based stream, so images differ only by float
+accumulation order."""
 import numpy as np
 import pytest
 
@@ -79,4 +81,33 @@ def test_batch_autotuner_and_variant_5(ctx):
     for a, b in zip(ref, got):
         np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-6)
     for s in set(slots):
+        ctx.release(s)
+
+
+def test_batch_items_match_oracle_renders(ctx):
+    """Parity of the batched launch itself against the CPU oracle: three of
+    the 64-scene batch's random-sphere scenes (the smallest, a middle and the
+    largest sphere count) rendered together in one persistent launch, K runs
+    with distinct seeds, each item compared with K oracle renders of its
+    scene (per-pixel z statistics and image means, tests/conftest.py
+    zcheck)."""
+    import pyoracle
+    from conftest import zcheck
+
+    sds = scenes.batch_scenes()
+    order = sorted(range(len(sds)), key=lambda k: sds[k].meta["n_spheres"])
+    pick = [sds[order[0]], sds[order[len(order) // 2]], sds[order[-1]]]
+    assert pick[0].meta["n_spheres"] < 200 and pick[-1].meta["n_spheres"] > 4500
+    slots = [ctx.upload(tpt.Scene(sd.text())) for sd in pick]
+    w = h = 24
+    spp, k = 32, 6
+    jobs = [(s, w, h, spp) for s in slots]
+    runs = [tpt.render_batch(ctx, jobs, max_depth=50, background=tpt.BACKGROUND_SKY, seed=300 + r)[0]
+            for r in range(k)]
+    for j, sd in enumerate(pick):
+        ora = pyoracle.Scene(sd.text())
+        ref = np.stack([ora.render(w, h, spp, 50, background=1, seed=600 + r)[0] for r in range(k)])
+        mine = np.stack([runs[r][j] for r in range(k)])
+        zcheck(mine.astype(np.float64), ref.astype(np.float64))
+    for s in slots:
         ctx.release(s)

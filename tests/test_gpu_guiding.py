@@ -41,7 +41,11 @@ def test_guided_is_unbiased(ctx, engine):
     d = gb.mean(0) - pb.mean(0)
     s = np.sqrt(gb.var(0, ddof=1) / k + pb.var(0, ddof=1) / k)
     z = d[s > 0] / s[s > 0]
-    assert abs(z.mean()) < 0.5 and z.std() < 1.8, (z.mean(), z.std())
+    # K = 8 a side: Student's t with 14 degrees of freedom has spread 1.08;
+    # 192 block values put the sampling error of that spread near 0.06 and
+    # of the mean near 0.08 (measured on a GB300: mean -0.04 / 0.03, spread
+    # 1.05 / 1.08 for the two engines)
+    assert abs(z.mean()) < 0.25 and 0.75 < z.std() < 1.35, (z.mean(), z.std())
     ctx.release(slot)
 
 

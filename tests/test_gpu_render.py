@@ -20,7 +20,7 @@ import pyoracle
 import tpt
 from tpt import scenes
 
-from conftest import GOLDEN
+from conftest import GOLDEN, zcheck as _zcheck
 
 pytestmark = pytest.mark.gpu
 
@@ -36,21 +36,12 @@ def _sd(name):
         return f.read()
 
 
-def _zcheck(a, b):
-    """a, b: (K, H, W, 3) independent render sets of the same estimator."""
-    k = a.shape[0]
-    ma, mb = a.mean(axis=(1, 2, 3)), b.mean(axis=(1, 2, 3))
-    se = np.sqrt(ma.var(ddof=1) / k + mb.var(ddof=1) / len(mb))
-    assert abs(ma.mean() - mb.mean()) < 4 * se + 1e-7, (ma.mean(), mb.mean(), se)
-    d = a.mean(0) - b.mean(0)
-    s = np.sqrt(a.var(0, ddof=1) / k + b.var(0, ddof=1) / b.shape[0])
-    ok = s > 0
-    z = d[ok] / s[ok]
-    assert abs(z.mean()) < 0.1 and 0.5 < z.std() < 1.6, (z.mean(), z.std())
-
-
-@pytest.mark.parametrize("name", ["cornell", "cornell_guiding"])
+@pytest.mark.parametrize("name", ["cornell", "cornell_guiding", "metals", "textures", "motion", "media"])
 def test_render_matches_reference_renders(ctx, name):
+    """Against the reference's own renders: the Cornell boxes, and the
+    Cornell room holding metals (fuzz 0, 0.35, a clamped 1.6, a metal box),
+    checker / perlin / image textures, moving spheres under a shutter, and
+    media (which absorb in the reference's semantics)."""
     g = np.load(os.path.join(GOLDEN, f"{name}_render.npz"))
     ref = g["images"].astype(np.float64)
     w, h, spp, depth, runs = [int(v) for v in g["meta"]]

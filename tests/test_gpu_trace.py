@@ -1,8 +1,14 @@
 """Closest-hit parity on the GPU: tpt_trace_closest (CUDA traversal) against
 the CPU oracle, which is itself pinned bit-exact to the reference
-(test_oracle_ref.py / golden fixtures).  Bar: primitive ids bit-exact; t,
-uv, point and normal within 1e-5 relative (absolute floor 1e-5 for
-components near zero and 2e-4 for points far from the origin)."""
+(test_oracle_golden.py / golden fixtures), and against the reference's own
+hit records.  Bar: primitive ids bit-exact; t, point, normal and uv within
+1e-5 relative.  Floors for components near zero: a point component is
+measured against max(|p|, 1), a normal component against the normal's
+length, and u, v (in [0, 1]) get an absolute floor of 1e-6 (eight ulps at
+1.0; the device's atan2f / asinf differ from the host's by an ulp or two).
+Measured on a GB300 over 200k rays per scene: ids, points and normals are
+bit-identical, t differs in the last bit on a few instanced or medium hits,
+u and v differ by at most 1.2e-7."""
 import numpy as np
 import pytest
 
@@ -13,26 +19,29 @@ from tpt import scenes
 pytestmark = pytest.mark.gpu
 
 RTOL = 1e-5
+SCENES = ["cornell", "one_weekend", "cornell_guiding", "ties", "instances", "next_week",
+          "metals", "textures", "motion", "media"]
 
 
 def _compare(f, i, of, oi, medium_ids=()):
     assert np.array_equal(i, oi), f"id mismatch on {(i != oi).any(axis=1).sum()} rays"
     hit = oi[:, 0] == 1
-    # t exact-ish: the float-float sphere root reproduces the double root
-    np.testing.assert_allclose(f[hit, 0], of[hit, 0], rtol=RTOL, atol=1e-6)
+    # t: the float-float sphere root reproduces the double root
+    np.testing.assert_allclose(f[hit, 0], of[hit, 0], rtol=RTOL, atol=0)
     geo = hit & ~np.isin(oi[:, 1], list(medium_ids))
-    scale = np.maximum(1.0, np.abs(of[geo, 3:6]))
-    assert (np.abs(f[geo, 3:6] - of[geo, 3:6]) <= 2e-5 * scale + 1e-5).all(), "hit point"
+    p_gpu, p_ora = f[geo, 3:6], of[geo, 3:6]
+    assert (np.abs(p_gpu - p_ora) <= RTOL * np.maximum(1.0, np.abs(p_ora))).all(), "hit point"
     fin = np.isfinite(of[geo, 6:9]).all(axis=1)
     n_gpu, n_ora = f[geo][fin, 6:9], of[geo][fin, 6:9]
-    assert (np.abs(n_gpu - n_ora) <= 1e-4).all(), "normal"
+    n_len = np.linalg.norm(n_ora, axis=1, keepdims=True)
+    assert (np.abs(n_gpu - n_ora) <= RTOL * n_len).all(), "normal"
     uv_ok = np.isfinite(of[geo, 1:3])
     d_uv = np.abs(f[geo, 1:3] - of[geo, 1:3])
-    assert (d_uv[uv_ok] <= 1e-4).all(), "uv"
+    assert (d_uv[uv_ok] <= RTOL * np.abs(of[geo, 1:3])[uv_ok] + 1e-6).all(), "uv"
 
 
 @pytest.mark.parametrize("flat", [0, 48, 1 << 20], ids=["stack", "auto", "stackless"])
-@pytest.mark.parametrize("name", ["cornell", "one_weekend", "cornell_guiding", "ties", "instances", "next_week"])
+@pytest.mark.parametrize("name", SCENES)
 def test_trace_matches_oracle(ctx, name, flat):
     sd = scenes.PRESETS[name]()
     text = sd.text()
@@ -63,7 +72,7 @@ def test_trace_one_million_rays_one_weekend(ctx):
     ctx.release(slot)
 
 
-@pytest.mark.parametrize("name", ["cornell", "one_weekend", "cornell_guiding", "ties", "instances", "next_week"])
+@pytest.mark.parametrize("name", SCENES)
 def test_trace_matches_reference_golden(ctx, name):
     """GPU closest hits against the reference's own outputs (golden fixtures).
     A constant_medium draws its free-flight distance from drand_r inside
@@ -84,7 +93,7 @@ def test_trace_matches_reference_golden(ctx, name):
         f0, i0 = ora.trace(g["rays"], media_mode=0)
         f1, i1 = ora.trace(g["rays"], media_mode=1)
         keep = (i0 == i1).all(axis=1) & (f0[:, 0].view(np.uint32) == f1[:, 0].view(np.uint32))
-        assert keep.mean() > 0.9
+        assert keep.mean() > 0.8
     _compare(f[keep], i[keep], g["hit_f"][keep], g["hit_i"][keep])
     ctx.release(slot)
 
@@ -131,7 +140,7 @@ def _in_rect_plane(sd, rays):
 
 
 @pytest.mark.parametrize("flat", [0, 1 << 20], ids=["stack", "stackless"])
-@pytest.mark.parametrize("name", ["cornell", "one_weekend", "instances", "next_week"])
+@pytest.mark.parametrize("name", ["cornell", "one_weekend", "instances", "next_week", "metals", "textures"])
 def test_trace_edge_rays(ctx, name, flat):
     """The known-answer edge rays (tests/golden/<scene>_edge.npz, frozen from
     the reference; the oracle reproduces them bit for bit on the CPU):

@@ -60,3 +60,42 @@ def test_mlp_reference_backward_matches_finite_differences():
         ym, _ = mlp_ref.forward(pm, x, in_dim, nh, out_dim, f16_acts=False)
         num = ((yp - ym) * dy).sum() / (2 * eps)
         assert abs(num - g[k]) < 1e-5 * max(1.0, abs(g[k]))
+
+
+def test_rel_l2_gradient_matches_finite_differences():
+    """The cache loss's gradient holds the denominator constant: finite
+    differences of (y - t)^2 / (d^2 + 0.01) with d frozen at y."""
+    rng = np.random.default_rng(3)
+    y = rng.uniform(-0.5, 3.0, size=(6, 16))
+    t = np.concatenate([rng.uniform(0, 3, size=(6, 3)), np.ones((6, 1))], axis=1)
+    g = mlp_ref.rel_l2_grad(y, t, 16)
+    eps = 1e-6
+    den = y[:, :3] ** 2 + mlp_ref.REL_L2_EPS
+    for i in range(6):
+        for c in range(3):
+            yp, ym = y[i, c] + eps, y[i, c] - eps
+            num = ((yp - t[i, c]) ** 2 - (ym - t[i, c]) ** 2) / den[i, c] / (2 * eps)
+            assert abs(num - g[i, c]) < 1e-6 * max(1.0, abs(g[i, c]))
+    assert np.all(g[:, 3:] == 0)
+    assert np.allclose(mlp_ref.rel_l2(y, t), ((y[:, :3] - t[:, :3]) ** 2 / den).sum(1))
+
+
+def test_encoders_known_answers():
+    """One-blob and triangle-wave values at hand-checked points."""
+    ob = mlp_ref.one_blob(np.array([0.0, 0.5, 1.0, np.nan]), 4)
+    assert np.allclose(ob[0], [0.5, 0, 0, 0]) and np.allclose(ob[1], [0, 0.5, 0.5, 0])
+    assert np.allclose(ob[2], [0, 0, 0, 0.5]) and np.allclose(ob[3], ob[0])
+    rec = np.zeros((1, 5, 4), np.float32)
+    rec[0, 0] = [0.25, 0.5, 0.75, 0.5]   # position (box [0,1]^3), roughness
+    rec[0, 1, :3] = [0, 0, 1]            # outgoing direction +z: theta 0
+    rec[0, 2, :3] = [1, 0, 0]            # normal +x: theta 1/2, phi 0
+    rec[0, 3, :3] = [0.1, 0.2, np.inf]   # albedo, a non-finite channel -> 0
+    x = mlp_ref.nrc_encode(rec, [0, 0, 0], [1, 1, 1]).astype(np.float32)[0]
+    # |2 frac(2^k 0.25) - 1|: 0.5, 0, 1, 1, ...
+    assert np.allclose(x[0:4], [0.5, 0.0, 1.0, 1.0])
+    assert np.allclose(x[36:40], [0.5, 0, 0, 0]) and np.allclose(x[44:48], [0, 0.5, 0.5, 0])
+    assert np.allclose(x[56:59], [0.1, 0.2, 0.0], atol=1e-3) and np.all(x[59:] == 0)
+    g, t = mlp_ref.guide_encode(np.array([[[0.5, 0.5, 0.5, 2.0], [0, 1, 0, 0], [0, 0, -1, 0]],
+                                          [[np.nan, 0, 0, 1.0], [0, 1, 0, 0], [0, 0, 1, 0]]]), [0, 0, 0], [1, 1, 1])
+    assert g[0, 15] == 0.5 and g[0, 16] == 0.5 and g[0, 97] == 1 and np.allclose(t[0], [0, 0, -1, 2])
+    assert t[1, 3] == 0 and g[1, 0] == 0.5 and g[1, 98] == 1  # unusable record: corner, +z, zero weight

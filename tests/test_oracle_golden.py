@@ -9,9 +9,11 @@ import pytest
 import pyoracle
 from tpt import scenes
 
-from conftest import GOLDEN
+from conftest import GOLDEN, zcheck
 
-SCENES = ["cornell", "one_weekend", "cornell_guiding", "ties", "instances", "next_week"]
+SCENES = ["cornell", "one_weekend", "cornell_guiding", "ties", "instances", "next_week",
+          "metals", "textures", "motion", "media"]
+RENDERS = ["cornell", "cornell_guiding", "metals", "textures", "motion", "media"]
 
 
 def _sd(name):
@@ -73,7 +75,7 @@ def test_ties_known_answers(built):
         assert np.array_equal(ri, i)
 
 
-@pytest.mark.parametrize("name", ["cornell", "cornell_guiding"])
+@pytest.mark.parametrize("name", RENDERS)
 def test_oracle_render_matches_reference_statistics(built, name):
     """Oracle renders against the reference's renders at the same resolution
     and spp: the image means agree within 4 sigma of the reference's run to
@@ -88,14 +90,10 @@ def test_oracle_render_matches_reference_statistics(built, name):
     se = np.sqrt(m_ref.var(ddof=1) / runs + m_ora.var(ddof=1) / runs)
     assert abs(m_ref.mean() - m_ora.mean()) < 4 * se + 1e-6, (m_ref.mean(), m_ora.mean(), se)
     # per pixel: difference of run means over its standard error
-    d = mine.mean(0) - ref.mean(0)
-    s = np.sqrt(mine.var(0, ddof=1) / runs + ref.var(0, ddof=1) / runs)
-    ok = s > 0
-    z = d[ok] / s[ok]
-    assert abs(z.mean()) < 0.1 and 0.5 < z.std() < 1.6, (z.mean(), z.std())
+    zcheck(mine, ref)
 
 
-@pytest.mark.parametrize("name", ["cornell", "one_weekend", "instances", "next_week"])
+@pytest.mark.parametrize("name", ["cornell", "one_weekend", "instances", "next_week", "metals", "textures"])
 def test_oracle_edge_rays_match_reference(built, name):
     """Known-answer rays at the edges of the primitives' arithmetic
     (tangent and near-tangent to spheres, from sphere surfaces, at rect and

@@ -1,9 +1,8 @@
 """tpt_render_noalloc: the render entry point for callers that cannot allocate
 device memory (a plugin whose host owns all GPU memory through its own
-pool, work issued during CUDA graph capture, real-time loops that must not
-hit an allocation's implicit synchronisation).  The caller supplies the scene
-buffer and the image buffer; the accumulators live in a fixed device array
-inside the library.
+pool, real-time loops that must not hit an allocation's implicit
+synchronisation).  The caller supplies the scene buffer and the image
+buffer; the accumulators live in a fixed device array inside the library.
 
 Checked through the C ABI against tpt_render (persistent engine, same seed,
 same parameters) on two calls in a row with different sizes and seeds, so a
@@ -56,3 +55,33 @@ def test_noalloc_rejects_oversized_images(built):
     assert b"TPT_NOALLOC_MAX_PIXELS" in tpt.lib().tpt_last_error()
     small = torch.zeros(16, dtype=torch.uint8, device="cuda")
     assert _noalloc(scene, small, tpt.make_params(8, 8, 1, 50), out) == 1
+    assert b"arena" in tpt.lib().tpt_last_error()
+    p = tpt.make_params(2, 2, 1, 50)
+    p.accumulate_fp64 = 1
+    assert _noalloc(scene, arena, p, out) == 1
+    assert b"accumulate_fp64" in tpt.lib().tpt_last_error()
+    p = tpt.make_params(2, 2, 1, 50, block=96 + 1)
+    assert _noalloc(scene, arena, p, out) == 1
+    assert b"block" in tpt.lib().tpt_last_error()
+
+
+def test_noalloc_builds_gpu_bvh_in_the_callers_buffer(ctx):
+    """A TPT_BVH_LBVH scene: every call rebuilds the trees on the GPU inside
+    the caller's arena buffer; two calls in a row give tpt_render's image of
+    the same scene uploaded through the library's own allocations."""
+    import torch
+
+    scene = tpt.Scene(scenes.one_weekend().text(), bvh="lbvh")
+    slot = ctx.upload(scene)
+    arena = torch.zeros(scene.info()["arena_bytes"], dtype=torch.uint8, device="cuda")
+    for (w, h, spp, seed) in [(48, 32, 8, 21), (32, 32, 4, 22)]:
+        out = torch.full((h, w, 3), -1.0, dtype=torch.float32, device="cuda")
+        p = tpt.make_params(w, h, spp, 50, seed=seed, engine=tpt.ENGINE_PERSISTENT, background=tpt.BACKGROUND_SKY)
+        torch.cuda.synchronize()
+        assert _noalloc(scene, arena, p, out) == 0, tpt.lib().tpt_last_error()
+        got = out.cpu().numpy()
+        ref, _ = ctx.render(slot, w, h, spp, 50, seed=seed, engine=tpt.ENGINE_PERSISTENT,
+                            background=tpt.BACKGROUND_SKY)
+        np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-6)
+        assert got.max() > 0
+    ctx.release(slot)

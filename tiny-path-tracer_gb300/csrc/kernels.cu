@@ -2355,8 +2355,15 @@ static tpt_status noalloc_scratch(int device, void **out) {
 
 extern "C" tpt_status tpt_render_noalloc(const tpt_scene *scene, void *arena_dev, int64_t arena_bytes,
                                          const tpt_render_params *p, float *out_rgb_dev, void *stream_ptr) {
-  if (!scene || !arena_dev || !p || !out_rgb_dev) return TPT_ERR_INVALID_ARGUMENT;
-  if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->max_depth < 0) return TPT_ERR_INVALID_ARGUMENT;
+  auto invalid = [](const char *why) {
+    std::snprintf(g_last_error, sizeof(g_last_error), "tpt_render_noalloc: %s", why);
+    return TPT_ERR_INVALID_ARGUMENT;
+  };
+  if (!scene || !arena_dev || !p || !out_rgb_dev) return invalid("scene, arena, params and output must be non-NULL");
+  if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->max_depth < 0)
+    return invalid("width, height and spp must be positive and max_depth non-negative");
+  if (p->accumulate_fp64)
+    return invalid("accumulate_fp64 is not supported (the scratch holds FP32 accumulators only)");
   const unsigned long long npix = (unsigned long long)p->width * (unsigned long long)p->height;
   if (npix > (unsigned long long)TPT_NOALLOC_MAX_PIXELS) {
     std::snprintf(g_last_error, sizeof(g_last_error),
@@ -2372,12 +2379,13 @@ extern "C" tpt_status tpt_render_noalloc(const tpt_scene *scene, void *arena_dev
     return TPT_ERR_INVALID_ARGUMENT;
   }
   const int block = p->block > 0 ? p->block : 128;
-  if (block % 32 || block > 128) return TPT_ERR_INVALID_ARGUMENT;
+  if (block % 32 || block > 128) return invalid("block must be a multiple of 32 and at most 128");
   cudaStream_t stream = (cudaStream_t)stream_ptr;
   int device = 0;
   TPT_CUDA(cudaGetDevice(&device));
   void *scratch = nullptr;
   tpt_status st = noalloc_scratch(device, &scratch);
+  if (st == TPT_ERR_INVALID_ARGUMENT) return invalid("device ordinal out of range (0..63)");
   if (st != TPT_OK) return st;
   int sm_count = 0;
   TPT_CUDA(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device));

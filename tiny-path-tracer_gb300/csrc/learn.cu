@@ -14,6 +14,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -402,6 +403,23 @@ __device__ __forceinline__ bool finite4(float4 v) {
   return isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(v.w);
 }
 
+// One guide record (3 float4: position and weight, normal, sampled
+// direction) -> its encoded row and its loss target (direction, weight).
+// An unusable record (non-finite, or a negative weight) becomes a zero-weight
+// row at the box corner.
+__device__ __forceinline__ float4 guide_record_row(const float4 *rec, float3 lo, float3 inv_ext, __half *dst) {
+  float4 xw = rec[0], nn = rec[1], dd = rec[2];
+  if (!(finite4(xw) && finite4(nn) && finite4(dd) && xw.w >= 0.f)) {
+    xw = make_float4(lo.x, lo.y, lo.z, 0.f);
+    nn = dd = make_float4(0.f, 0.f, 1.f, 0.f);
+  }
+  const float3 xn = make_float3((xw.x - lo.x) * inv_ext.x, (xw.y - lo.y) * inv_ext.y, (xw.z - lo.z) * inv_ext.z);
+  __align__(16) __half row[GUIDE_IN];
+  guide_encode(xn, make_float3(nn.x, nn.y, nn.z), row);
+  store_row(row, dst);
+  return make_float4(dd.x, dd.y, dd.z, xw.w);
+}
+
 // Training rows: a random record per row (with replacement), encoded.
 __global__ void k_guide_encode_records(const float4 *__restrict__ rec, int count, int rows, uint2 key, uint32_t step,
                                        float3 lo, float3 inv_ext, __half *__restrict__ X, float4 *__restrict__ target,
@@ -411,17 +429,9 @@ __global__ void k_guide_encode_records(const float4 *__restrict__ rec, int count
     uint32_t h = (uint32_t)r * 0x9E3779B1u ^ (step * 0x85EBCA77u) ^ key.x;
     h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12; h *= 0x297A2D39u; h ^= h >> 15;
     const int idx = (int)(h % (uint32_t)count);
-    float4 xw = rec[3 * idx], nn = rec[3 * idx + 1], dd = rec[3 * idx + 2];
-    if (!(finite4(xw) && finite4(nn) && finite4(dd) && xw.w >= 0.f)) {  // an unusable record: zero weight
-      xw = make_float4(lo.x, lo.y, lo.z, 0.f);
-      nn = dd = make_float4(0.f, 0.f, 1.f, 0.f);
-    }
-    const float3 xn = make_float3((xw.x - lo.x) * inv_ext.x, (xw.y - lo.y) * inv_ext.y, (xw.z - lo.z) * inv_ext.z);
-    __align__(16) __half row[GUIDE_IN];
-    guide_encode(xn, make_float3(nn.x, nn.y, nn.z), row);
-    store_row(row, X + (size_t)r * GUIDE_IN);
-    target[r] = make_float4(dd.x, dd.y, dd.z, xw.w);
-    part += xw.w;
+    const float4 t = guide_record_row(rec + 3 * (size_t)idx, lo, inv_ext, X + (size_t)r * GUIDE_IN);
+    target[r] = t;
+    part += t.w;
   }
   for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
   if ((threadIdx.x & 31) == 0 && part != 0.f) atomicAdd(wsum, part);
@@ -592,6 +602,25 @@ __global__ void k_nrc_encode_records(const float4 *__restrict__ rec, int count, 
     store_row(row, X + (size_t)r * NRC_IN);
     const float4 t = rec[5 * (size_t)idx + 4];
     target[r] = finite4(t) ? t : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+// Record r -> row r, without sampling (the encoders as the C ABI exposes
+// them).  stride: float4 per record (guide 3; cache records 5, queries 6).
+__global__ void k_guide_encode_rows(const float4 *__restrict__ rec, int count, float3 lo, float3 inv_ext,
+                                    __half *__restrict__ X, float4 *__restrict__ target) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < count; r += gridDim.x * blockDim.x) {
+    const float4 t = guide_record_row(rec + 3 * (size_t)r, lo, inv_ext, X + (size_t)r * GUIDE_IN);
+    if (target) target[r] = t;
+  }
+}
+
+__global__ void k_nrc_encode_rows(const float4 *__restrict__ rec, int count, int stride, float3 lo, float3 inv_ext,
+                                  __half *__restrict__ X) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < count; r += gridDim.x * blockDim.x) {
+    __align__(16) __half row[NRC_IN];
+    nrc_encode(rec + (size_t)stride * r, lo, inv_ext, row);
+    store_row(row, X + (size_t)r * NRC_IN);
   }
 }
 
@@ -1040,6 +1069,53 @@ tpt_status tpt_mlp_backward_vmf(tpt_mlp *M, const void *x_f16, const float *targ
     MLP_CUDA(cudaStreamSynchronize(s));
   }
   return TPT_OK;
+}
+
+tpt_status tpt_mlp_backward_rel_l2(tpt_mlp *M, const void *x_f16, const float *target, int64_t rows, float scale,
+                                   float *loss_out, void *stream) {
+  if (!M || !x_f16 || !target || rows <= 0 || rows % 16 || rows > (1 << 26)) return TPT_ERR_INVALID_ARGUMENT;
+  if (M->in_dim != NRC_IN || M->n_hidden != NRC_NH || M->out_dim != NRC_OUT) return TPT_ERR_INVALID_ARGUMENT;
+  MLP_CUDA(cudaSetDevice(M->device));
+  tpt_status st = ensure_ws(M, (int)rows);
+  if (st != TPT_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  LossRelL2 L{(const float4 *)target, scale};
+  st = launch_train<NRC_IN, NRC_NH, NRC_OUT>(M, (const __half *)x_f16, (int)rows, L, s);
+  if (st != TPT_OK) return st;
+  if (loss_out) {
+    MLP_CUDA(cudaMemcpyAsync(loss_out, M->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+    MLP_CUDA(cudaStreamSynchronize(s));
+  }
+  return TPT_OK;
+}
+
+static bool encode_args(const float *rec, int64_t count, const float *lo, const float *ext, const void *x) {
+  if (!rec || !lo || !ext || !x || count <= 0 || count > (1 << 28)) return false;
+  for (int a = 0; a < 3; a++)
+    if (!(ext[a] > 0.f) || !std::isfinite(lo[a]) || !std::isfinite(ext[a])) return false;
+  return true;
+}
+
+tpt_status tpt_guide_encode(const float *records, int64_t count, const float *lo, const float *extent, void *x_f16,
+                            float *target, void *stream) {
+  if (!encode_args(records, count, lo, extent, x_f16)) return TPT_ERR_INVALID_ARGUMENT;
+  const float3 l = make_float3(lo[0], lo[1], lo[2]);
+  const float3 inv = make_float3(1.f / extent[0], 1.f / extent[1], 1.f / extent[2]);
+  const int grid = (int)std::min<int64_t>((count + 255) / 256, 4096);
+  k_guide_encode_rows<<<grid, 256, 0, (cudaStream_t)stream>>>((const float4 *)records, (int)count, l, inv,
+                                                              (__half *)x_f16, (float4 *)target);
+  return mlp_cuda(cudaGetLastError());
+}
+
+tpt_status tpt_nrc_encode(const float *records, int64_t count, int32_t stride, const float *lo, const float *extent,
+                          void *x_f16, void *stream) {
+  if (!encode_args(records, count, lo, extent, x_f16) || stride < 4) return TPT_ERR_INVALID_ARGUMENT;
+  const float3 l = make_float3(lo[0], lo[1], lo[2]);
+  const float3 inv = make_float3(1.f / extent[0], 1.f / extent[1], 1.f / extent[2]);
+  const int grid = (int)std::min<int64_t>((count + 255) / 256, 4096);
+  k_nrc_encode_rows<<<grid, 256, 0, (cudaStream_t)stream>>>((const float4 *)records, (int)count, stride, l, inv,
+                                                            (__half *)x_f16);
+  return mlp_cuda(cudaGetLastError());
 }
 
 tpt_status tpt_mlp_adam(tpt_mlp *M, float lr, float inv_loss_scale, void *stream) {

@@ -176,6 +176,12 @@ _SIGS = {
                                            C.c_void_p]),
     "tpt_mlp_backward_vmf": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float, C.c_void_p,
                                          C.c_void_p]),
+    "tpt_mlp_backward_rel_l2": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float,
+                                            C.c_void_p, C.c_void_p]),
+    "tpt_guide_encode": (C.c_int32, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p]),
+    "tpt_nrc_encode": (C.c_int32, [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p]),
     "tpt_mlp_adam": (C.c_int32, [C.c_void_p, C.c_float, C.c_float, C.c_void_p]),
     "tpt_mlp_last_error": (C.c_char_p, []),
     "tpt_guide_params_default": (None, [C.POINTER(GuideParams)]),
@@ -601,8 +607,48 @@ class Mlp:
                                          C.byref(loss), None), "mlp_backward_vmf")
         return loss.value
 
+    def backward_rel_l2(self, x_f16_ptr: int, target_ptr: int, rows: int, scale: float = 1.0) -> float:
+        loss = C.c_float()
+        check(lib().tpt_mlp_backward_rel_l2(self._h, C.c_void_p(x_f16_ptr), C.c_void_p(target_ptr), rows, scale,
+                                            C.byref(loss), None), "mlp_backward_rel_l2")
+        return loss.value
+
     def adam(self, lr: float, inv_loss_scale: float = 1.0) -> None:
         check(lib().tpt_mlp_adam(self._h, lr, inv_loss_scale, None), "mlp_adam")
+
+
+def _encode(fn: str, records: np.ndarray, stride: int, width: int, lo, extent, with_target: bool):
+    import torch
+
+    rec = np.ascontiguousarray(records, np.float32).reshape(-1, stride * 4)
+    n = len(rec)
+    dr = torch.from_numpy(rec).cuda()
+    x = torch.empty((n, width), dtype=torch.float16, device="cuda")
+    t = torch.empty((n, 4), dtype=torch.float32, device="cuda") if with_target else None
+    lo_a = np.ascontiguousarray(lo, np.float32)
+    ext_a = np.ascontiguousarray(extent, np.float32)
+    torch.cuda.synchronize()
+    if fn == "guide":
+        st = lib().tpt_guide_encode(C.c_void_p(dr.data_ptr()), n, _ptr(lo_a), _ptr(ext_a), C.c_void_p(x.data_ptr()),
+                                    C.c_void_p(t.data_ptr()) if t is not None else None, None)
+    else:
+        st = lib().tpt_nrc_encode(C.c_void_p(dr.data_ptr()), n, stride, _ptr(lo_a), _ptr(ext_a),
+                                  C.c_void_p(x.data_ptr()), None)
+    check(st, fn + "_encode")
+    torch.cuda.synchronize()
+    return x.cpu().numpy(), (t.cpu().numpy() if t is not None else None)
+
+
+def guide_encode(records: np.ndarray, lo, extent):
+    """Path-guiding input rows (f16, n x 112) and loss targets (n x 4) of
+    guide records (n x 3 float4) through the C ABI (a CUDA kernel)."""
+    return _encode("guide", records, 3, 112, lo, extent, True)
+
+
+def nrc_encode(records: np.ndarray, lo, extent, stride: int = 5) -> np.ndarray:
+    """Radiance-cache input rows (f16, n x 64) of cache records (n x stride
+    float4) through the C ABI (a CUDA kernel)."""
+    return _encode("nrc", records, stride, 64, lo, extent, False)[0]
 
 
 def exported_symbols() -> list[str]:

@@ -349,6 +349,110 @@ def instance_scene() -> SD:
     return sd
 
 
+def _room(sd: SD, floor_mat: int | None = None) -> tuple[list[int], int]:
+    """The Cornell room of cornell() without its box and sphere: five walls
+    and the flipped light rect (emission 15).  Returns the items and the
+    light list (the light rect alone)."""
+    red = sd.lambertian(sd.const(0.65, 0.05, 0.05))
+    white = sd.lambertian(sd.const(0.73, 0.73, 0.73))
+    green = sd.lambertian(sd.const(0.12, 0.45, 0.15))
+    lightm = sd.diffuse_light(sd.const(15, 15, 15))
+    items = [
+        sd.flip(sd.rect("yz_rect", 0, 555, 0, 555, 555, green)),
+        sd.rect("yz_rect", 0, 555, 0, 555, 0, red),
+        sd.flip(sd.rect("xz_rect", 213, 343, 227, 332, 554, lightm)),
+        sd.flip(sd.rect("xz_rect", 0, 555, 0, 555, 555, white)),
+        sd.rect("xz_rect", 0, 555, 0, 555, 0, white if floor_mat is None else floor_mat),
+        sd.flip(sd.rect("xy_rect", 0, 555, 0, 555, 555, white)),
+    ]
+    dummy = sd.lambertian(sd.const(0, 0, 0))
+    lights = sd.hlist([sd.rect("xz_rect", 213, 343, 227, 332, 554, dummy)])
+    return items, lights
+
+
+def _room_camera(sd: SD, t0=0.0, t1=0.0) -> None:
+    sd.camera((278, 278, -800), (278, 278, 0), (0, 1, 0), 40.0, 1.0, 0.0, 10.0, t0, t1)
+    sd.meta = dict(width=48, height=48, spp=64, max_depth=50, background=0, sky_scale=1.0)
+
+
+def metals() -> SD:
+    """Metal scatter (material.cc:88-98) in the Cornell room: mirror (fuzz
+    0), fuzzy (0.35) and over-range fuzz 1.6, which the metal constructor
+    clamps to 1 (material.h:41-46), on spheres, plus a fuzzy metal box."""
+    sd = SD()
+    items, lights = _room(sd)
+    items.append(sd.sphere((130, 90, 170), 90, sd.metal(0.85, 0.85, 0.9, 0.0)))
+    items.append(sd.sphere((300, 90, 360), 90, sd.metal(0.9, 0.6, 0.3, 0.35)))
+    items.append(sd.sphere((440, 90, 170), 90, sd.metal(0.7, 0.8, 0.7, 1.6)))
+    mbox = sd.box((0, 0, 0), (120, 200, 120), sd.metal(0.8, 0.8, 0.8, 0.2))
+    items.append(sd.translate(sd.rotate_y(mbox, -25.0), (330, 0, 80)))
+    sd.world(sd.bvh(items, 0.0, 0.0))
+    sd.lights(lights)
+    _room_camera(sd)
+    return sd
+
+
+def textures() -> SD:
+    """Textures (texture.h:15-24, texture.cc:4-42) in the Cornell room: a
+    checker floor and a checker sphere (the sign of sin(10x)sin(10y)sin(10z)),
+    two perlin-turbulence spheres (seeded tables; scale 0.1 and 2), and a
+    sphere with a procedural 64x32 RGB image texture (nearest texel)."""
+    rng = np.random.Generator(np.random.PCG64(11))
+    sd = SD()
+    odd, even = sd.const(0.2, 0.3, 0.1), sd.const(0.9, 0.9, 0.9)
+    floor = sd.lambertian(sd.checker(odd, even))
+    items, lights = _room(sd, floor_mat=floor)
+    items.append(sd.sphere((130, 90, 170), 90, sd.lambertian(sd.checker(sd.const(0.8, 0.1, 0.1), even))))
+    sd.perlin_tables(rng)
+    items.append(sd.sphere((300, 90, 360), 90, sd.lambertian(sd.perlin(0.1))))
+    items.append(sd.sphere((440, 70, 170), 70, sd.lambertian(sd.perlin(2.0))))
+    items.append(sd.sphere((250, 300, 250), 70, sd.lambertian(sd.image(64, 32, 4242))))
+    sd.world(sd.bvh(items, 0.0, 0.0))
+    sd.lights(lights)
+    _room_camera(sd)
+    return sd
+
+
+def motion() -> SD:
+    """Moving spheres (sphere.cc:45-85) under the reference's own BVH in the
+    Cornell room: the camera's shutter is [0, 1] (camera.cc:26), the BVH
+    boxes span the motion (bvh_node t0 = 0, t1 = 1), and one sphere's
+    motion spans only [0.25, 0.75] of the shutter, so its centre is
+    extrapolated outside that range as the reference does."""
+    sd = SD()
+    items, lights = _room(sd)
+    w = sd.lambertian(sd.const(0.73, 0.73, 0.73))
+    items.append(sd.moving_sphere((130, 90, 170), (130, 190, 170), 0.0, 1.0, 80, w))
+    items.append(sd.moving_sphere((300, 90, 360), (420, 90, 360), 0.0, 1.0, 70, sd.metal(0.9, 0.8, 0.6, 0.1)))
+    items.append(sd.moving_sphere((440, 120, 150), (440, 160, 120), 0.25, 0.75, 60,
+                                  sd.lambertian(sd.const(0.2, 0.4, 0.8))))
+    items.append(sd.sphere((200, 60, 100), 60, sd.dielectric(1.5)))
+    sd.world(sd.bvh(items, 0.0, 1.0))
+    sd.lights(lights)
+    _room_camera(sd, 0.0, 1.0)
+    return sd
+
+
+def media() -> SD:
+    """Constant-density media (hitable.cc:98-128) in the Cornell room: smoke
+    in a rotated box (density 0.01, as in the reference's
+    cornell_box_smoke) and a denser medium (0.05) inside a glass sphere, as
+    the 'next week' scene nests them.  In reference semantics the isotropic
+    phase function never scatters (material.h:74-80): media absorb."""
+    sd = SD()
+    items, lights = _room(sd)
+    b = sd.translate(sd.rotate_y(sd.box((0, 0, 0), (165, 330, 165), sd.lambertian(sd.const(1, 1, 1))), 15.0),
+                     (265, 0, 295))
+    items.append(sd.medium(b, 0.01, sd.const(0.0, 0.0, 0.0)))
+    glass = sd.sphere((150, 100, 150), 100, sd.dielectric(1.5))
+    items.append(glass)
+    items.append(sd.medium(glass, 0.05, sd.const(0.2, 0.4, 0.9)))
+    sd.world(sd.hlist([sd.bvh(items[:6], 0.0, 0.0)] + items[6:]))
+    sd.lights(lights)
+    _room_camera(sd)
+    return sd
+
+
 PRESETS = {
     "one_weekend": one_weekend,
     "cornell": cornell,
@@ -356,4 +460,8 @@ PRESETS = {
     "next_week": next_week,
     "ties": tie_scene,
     "instances": instance_scene,
+    "metals": metals,
+    "textures": textures,
+    "motion": motion,
+    "media": media,
 }
