@@ -19,7 +19,9 @@
 #ifndef TPT_SCENE_HPP
 #define TPT_SCENE_HPP
 
+#include <algorithm>
 #include <cmath>
+#include <iostream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -41,16 +43,70 @@ inline int32_t checked(int32_t h, const char *what) {
   return h;
 }
 
-// vec3 (headers/vec3.h): the components the constructors take.
+// vec3 (headers/vec3.h:6-157): three floats with the reference's
+// interface, so scene code that computes positions, offsets and colours
+// (utils.cc:96-414) compiles and gets the same floats.  Every operation is
+// evaluated in float, component by component, in the reference's order
+// (length: sqrt((x*x + y*y) + z*z); make_unit_vector scales by 1.0 / length
+// rounded from double to float); the scene layout, and with it the BVH that
+// bvh_node builds, depends on those bits.
 struct vec3 {
   float e[3];
   vec3() : e{0, 0, 0} {}
   vec3(float x, float y, float z) : e{x, y, z} {}
+  vec3(float s) : e{s, s, s} {}  // NOLINT: implicit, as the reference's
   float x() const { return e[0]; }
   float y() const { return e[1]; }
   float z() const { return e[2]; }
+  float r() const { return e[0]; }
+  float g() const { return e[1]; }
+  float b() const { return e[2]; }
   float operator[](int i) const { return e[i]; }
+  float &operator[](int i) { return e[i]; }
+  const vec3 &operator+() const { return *this; }
+  vec3 operator-() const { return vec3(-e[0], -e[1], -e[2]); }
+  vec3 &operator+=(const vec3 &o) { return each(o, [](float &a, float b) { a += b; }); }
+  vec3 &operator-=(const vec3 &o) { return each(o, [](float &a, float b) { a -= b; }); }
+  vec3 &operator*=(const vec3 &o) { return each(o, [](float &a, float b) { a *= b; }); }
+  vec3 &operator/=(const vec3 &o) { return each(o, [](float &a, float b) { a /= b; }); }
+  vec3 &operator*=(const float t) { return each(vec3(t), [](float &a, float b) { a *= b; }); }
+  vec3 &operator/=(const float t) { return each(vec3(t), [](float &a, float b) { a /= b; }); }
+  float squared_length() const { return e[0] * e[0] + e[1] * e[1] + e[2] * e[2]; }
+  float length() const { return std::sqrt(squared_length()); }
+  void make_unit_vector() { *this *= (float)(1.0 / length()); }
+  void normalize() { make_unit_vector(); }
+
+ private:
+  template <class F>
+  vec3 &each(const vec3 &o, F f) {
+    for (int i = 0; i < 3; i++) f(e[i], o.e[i]);
+    return *this;
+  }
 };
+
+inline vec3 operator+(vec3 a, const vec3 &b) { return a += b; }
+inline vec3 operator-(vec3 a, const vec3 &b) { return a -= b; }
+inline vec3 operator*(vec3 a, const vec3 &b) { return a *= b; }
+inline vec3 operator/(vec3 a, const vec3 &b) { return a /= b; }
+inline vec3 operator*(vec3 a, float t) { return a *= t; }
+inline vec3 operator*(float t, vec3 a) { return a *= t; }
+inline vec3 operator/(vec3 a, float t) { return a /= t; }
+inline float dot(const vec3 &a, const vec3 &b) { return a.e[0] * b.e[0] + a.e[1] * b.e[1] + a.e[2] * b.e[2]; }
+inline vec3 cross(const vec3 &a, const vec3 &b) {
+  return vec3(a.e[1] * b.e[2] - b.e[1] * a.e[2], a.e[2] * b.e[0] - b.e[2] * a.e[0], a.e[0] * b.e[1] - b.e[0] * a.e[1]);
+}
+inline vec3 normalize(vec3 v) { return v / v.length(); }
+inline vec3 unit_vector(vec3 v) { return normalize(v); }
+inline vec3 vec_min(const vec3 &a, const vec3 &b) {
+  return vec3(std::min(a.e[0], b.e[0]), std::min(a.e[1], b.e[1]), std::min(a.e[2], b.e[2]));
+}
+inline vec3 vec_max(const vec3 &a, const vec3 &b) {
+  return vec3(std::max(a.e[0], b.e[0]), std::max(a.e[1], b.e[1]), std::max(a.e[2], b.e[2]));
+}
+inline std::istream &operator>>(std::istream &is, vec3 &v) { return is >> v.e[0] >> v.e[1] >> v.e[2]; }
+inline std::ostream &operator<<(std::ostream &os, const vec3 &v) {
+  return os << v.e[0] << " " << v.e[1] << " " << v.e[2];
+}
 
 // ---- textures (headers/texture.h)
 class texture {
@@ -207,6 +263,8 @@ class camera_with_blur {
       : lookfrom(lookfrom_), lookat(lookat_), vup(vup_), vfov(vfov_), aspect(aspect_), aperture(aperture_),
         focus_dist(focus_dist_), t0(t0_), t1(t1_) {}
 };
+
+using camera = camera_with_blur;  // camera.h:23
 
 // drand_r (utils.cc:28-32) on the current builder's stream.
 inline double drand_r(double min = 0.0, double max = 1.0) { return tpt_builder_drand(current_builder(), min, max); }

@@ -87,6 +87,17 @@ def ref_available() -> bool:
     return os.path.exists(REF_SO)
 
 
+def reference_dir() -> str | None:
+    """The reference checkout the harness was compiled from (recorded by
+    oracle/Makefile), if it is still there."""
+    try:
+        with open(os.path.join(HERE, "_ref", "reference_dir.txt")) as f:
+            d = f.read().strip()
+    except OSError:
+        return None
+    return d if os.path.isdir(os.path.join(d, "src")) else None
+
+
 def ref_lib():
     global _ref
     if _ref is None:
@@ -102,6 +113,9 @@ def ref_lib():
         L.ref_hardware_concurrency.restype = C.c_int32
         L.ref_frontend_bvh.restype = C.c_int32
         L.ref_frontend_bvh.argtypes = [C.c_int32, C.c_void_p, C.c_int32]
+        L.ref_scene_function_bvhs.restype = C.c_int32
+        L.ref_scene_function_bvhs.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                              C.POINTER(C.c_int32)]
         L.ref_config_parse.restype = None
         L.ref_config_parse.argtypes = [C.c_char_p, C.c_void_p]
         _ref = L
@@ -229,6 +243,25 @@ def ref_frontend_bvh(n: int):
     out = np.zeros((cap, 6), np.float32)
     k = ref_lib().ref_frontend_bvh(n, out.ctypes.data_as(C.c_void_p), cap)
     return out[:k]
+
+
+def ref_scene_function_bvhs(name: str):
+    """The bvh_nodes one of the reference's own scene functions
+    (utils.cc:96-414) builds, run on a fresh thread: a list of (boxes n x 6,
+    kids n x 2) per tree in build order, kids -1 for a leaf."""
+    nt = C.c_int32()
+    n = ref_lib().ref_scene_function_bvhs(name.encode(), None, None, None, 0, C.byref(nt))
+    if n < 0:
+        raise KeyError(name)
+    boxes = np.zeros((max(n, 1), 6), np.float32)
+    kids = np.zeros((max(n, 1), 2), np.int32)
+    sizes = np.zeros(max(nt.value, 1), np.int32)
+    ref_lib().ref_scene_function_bvhs(name.encode(), _ptr(boxes), _ptr(kids), _ptr(sizes), n, C.byref(nt))
+    out, off = [], 0
+    for k in sizes[:nt.value]:
+        out.append((boxes[off:off + k], kids[off:off + k]))
+        off += k
+    return out
 
 
 def ref_config_parse(text: str) -> list:

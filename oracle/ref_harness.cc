@@ -467,6 +467,95 @@ int32_t ref_frontend_bvh(int32_t n, float *boxes, int32_t cap) {
   return nodes;
 }
 
+}  // extern "C"
+
+hitable *two_checker_spheres();  // defined in utils.cc without a declaration in utils.h
+
+namespace {
+
+// Pre-order dump of one bvh_node tree: per node its box and, per child, the
+// child's pre-order index, or -1 for a leaf.
+void dump_preorder(const bvh_node *n, std::vector<float> &boxes, std::vector<int> &kids) {
+  const int me = (int)kids.size() / 2;
+  kids.push_back(-1);
+  kids.push_back(-1);
+  for (int i = 0; i < 3; i++) boxes.push_back(n->box_.min()[i]);
+  for (int i = 0; i < 3; i++) boxes.push_back(n->box_.max()[i]);
+  const hitable *ch[2] = {n->left_, n->right_};
+  for (int c = 0; c < 2; c++)
+    if (auto *b = dynamic_cast<const bvh_node *>(ch[c])) {
+      kids[2 * me + c] = (int)kids.size() / 2;
+      dump_preorder(b, boxes, kids);
+    }
+}
+
+// The bvh_nodes a scene function built itself (not their inner nodes), in
+// the order it built them: a depth-first walk of lists and wrappers.
+void find_bvh_roots(const hitable *h, std::vector<const bvh_node *> &out) {
+  if (!h) return;
+  if (auto *b = dynamic_cast<const bvh_node *>(h)) {
+    out.push_back(b);
+  } else if (auto *l = dynamic_cast<const hitable_list *>(h)) {
+    for (int i = 0; i < l->list_size_; i++) find_bvh_roots(l->list_[i], out);
+  } else if (auto *t = dynamic_cast<const translate *>(h)) {
+    find_bvh_roots(t->ptr_, out);
+  } else if (auto *r = dynamic_cast<const rotate_y *>(h)) {
+    find_bvh_roots(r->ptr_, out);
+  } else if (auto *f = dynamic_cast<const flip_normal *>(h)) {
+    find_bvh_roots(f->ptr_, out);
+  } else if (auto *m = dynamic_cast<const constant_medium *>(h)) {
+    find_bvh_roots(m->boundary_, out);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+// Runs one of the reference's own scene functions (utils.cc:96-414) on a
+// fresh thread (drand_r in its default state) and dumps the bvh_nodes it
+// built, concatenated: boxes (6 floats per node), kids (2 per node, see
+// dump_preorder), tree_nodes[k] = node count of tree k.  Returns the total
+// node count (the arrays are filled when it is <= cap), *n_trees the trees;
+// -1 for an unknown name.
+int32_t ref_scene_function_bvhs(const char *name, float *boxes, int32_t *kids, int32_t *tree_nodes, int32_t cap,
+                                int32_t *n_trees) {
+  const std::string nm(name ? name : "");
+  hitable *(*fn)() = nm == "random_scene"          ? random_scene
+                     : nm == "two_checker_spheres" ? two_checker_spheres
+                     : nm == "two_perlin_spheres"  ? two_perlin_spheres
+                     : nm == "light_spheres"       ? light_spheres
+                     : nm == "sphere_cornell_box"  ? sphere_cornell_box
+                     : nm == "cornell_box"         ? cornell_box
+                     : nm == "cornell_box_smoke"   ? cornell_box_smoke
+                     : nm == "oneweek_final"       ? oneweek_final
+                                                   : nullptr;
+  if (!fn) return -1;
+  std::vector<float> b;
+  std::vector<int> k, sizes;
+  std::thread th([&]() {
+    std::vector<const bvh_node *> roots;
+    find_bvh_roots(fn(), roots);
+    for (const bvh_node *r : roots) {
+      std::vector<float> tb;
+      std::vector<int> tk;
+      dump_preorder(r, tb, tk);
+      sizes.push_back((int)tk.size() / 2);
+      b.insert(b.end(), tb.begin(), tb.end());
+      k.insert(k.end(), tk.begin(), tk.end());
+    }
+  });
+  th.join();
+  const int n = (int)k.size() / 2;
+  *n_trees = (int32_t)sizes.size();
+  if (n <= cap) {
+    std::memcpy(boxes, b.data(), b.size() * sizeof(float));
+    std::memcpy(kids, k.data(), k.size() * sizeof(int));
+    std::memcpy(tree_nodes, sizes.data(), sizes.size() * sizeof(int));
+  }
+  return n;
+}
+
 // config.ini through the reference's own parser and the extraction calls of
 // main.cpp:42-56, from main.cpp:31-40's defaults.  out: width, height,
 // sample, recur_depth, fov, allow_bonus_pic, bonus_pic, aperture,
