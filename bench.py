@@ -19,9 +19,21 @@ cpu_baseline / --impl reference: the reference algorithm on the host cores
 learned_equal_time: the second half of the metric - relMSE against an FP64
         high-spp render of the learned renderers (path guiding on the small-
         light Cornell box, the radiance cache on the next-week scene) next to
-        the plain tracer at equal spp and at equal wall time (skip with
+        the plain tracer: at equal spp, at equal wall time, and the wall time
+        each needs to reach the plain tracer's relMSE (skip with
         --no-learned).
-Multi-GPU: N independent replicas (one frame each per step), scaling "weak".
+other_configs: the other throughput workloads of the benchmark definition,
+        each with its own CPU baseline - one weekend (400x400, 16 spp), the
+        64-scene batch (one persistent launch, the reference's BVH topology)
+        and the next-week scene (800x800, 256 spp, reference semantics)
+        (skip with --no-configs).
+roofline.flops: useful work - the arithmetic the reference's algorithm does
+        per ray segment, counted by the CPU oracle on a band of the same
+        frame - at the measured segment rate, against the FP32 peak.
+Multi-GPU (torchrun, N ranks): one frame split by sample ranges, rank r
+        rendering samples [r*spp/N, (r+1)*spp/N) of every pixel, the float4
+        accumulators summed across ranks (NCCL all-reduce) and resolved;
+        scaling "strong" (the frame's work is fixed).
 """
 from __future__ import annotations
 
@@ -60,6 +72,12 @@ NCU_WARP_INST_PER_SEGMENT = 3411932611 / 30416883
 # instruction issue peak: 152 SMs x 4 schedulers x 1 warp instruction per
 # cycle at the maximum SM clock (MEASURED_PEAKS.json sm_max_mhz)
 SMS, SCHEDULERS_PER_SM = 152, 4
+FP32_LANES_PER_SM = 128  # FP32 peak = 152 SMs x 128 lanes x 2 flops (FMA) x clock
+# Useful FLOPs per counted operation (the survey's work conventions): slab
+# test 12 (3 axes x 2 FMA), sphere 20, rect 10, instance transform 40,
+# lambertian / metal scatter 30, dielectric 60, light-pdf evaluation 40
+FLOPS_PER = {"aabb_tests": 12, "sphere_tests": 20, "rect_tests": 10, "instance_xforms": 40, "lambertian": 30,
+             "metal": 30, "dielectric": 60, "light_pdf_evals": 40}
 
 
 def _peaks() -> dict:
@@ -136,38 +154,79 @@ def host_cores() -> int:
     return n
 
 
-def cpu_leg(text: str, rows: tuple[int, int], spp: int, prefer_ref: bool = True, repeats: int = 2) -> dict:
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith(("model name", "cpu model")):
+                    return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def host_info() -> dict:
+    return {"cpu_model": cpu_model(), "hardware_concurrency": os.cpu_count() or 1, "cores_used": host_cores()}
+
+
+def useful_flops_per_segment(text: str, width: int, height: int, rows: tuple[int, int], spp: int,
+                             semantics: int = 0, background: int = 0) -> dict:
+    """The CPU oracle's operation counts over a band of the frame (the
+    reference's traversal: both children of every bvh_node whose box the
+    ray enters), weighted by FLOPS_PER, per ray segment."""
+    import pyoracle
+
+    _, cnt = pyoracle.Scene(text).render(width, height, spp, DEPTH, semantics=semantics, background=background,
+                                          seed=3, nthreads=host_cores(), rows=rows)
+    segs = max(1, cnt["segments"])
+    flops = sum(FLOPS_PER[k] * cnt[k] for k in FLOPS_PER)
+    return {"flops_per_segment": flops / segs, "counts_per_segment": {k: cnt[k] / segs for k in FLOPS_PER},
+            "oracle_segments_per_sample": segs / ((rows[1] - rows[0]) * width * spp),
+            "sample": f"rows {rows[0]}..{rows[1]} of {width}x{height} at {spp} spp"}
+
+
+def cpu_leg(text: str, rows: tuple[int, int], spp: int, prefer_ref: bool = True, repeats: int = 2, width: int = W,
+            height: int = H, background: int = 0) -> dict:
     """The reference algorithm on host cores over image rows [rows); the best
     of `repeats` runs (the host is shared, single runs vary)."""
     best = None
     for _ in range(repeats):
-        r = _cpu_leg_once(text, rows, spp, prefer_ref)
+        r = _cpu_leg_once(text, rows, spp, prefer_ref, width, height, background)
         if best is None or r["value"] > best["value"]:
             best = r
     return best
 
 
-def _cpu_leg_once(text: str, rows: tuple[int, int], spp: int, prefer_ref: bool) -> dict:
+def _cpu_leg_once(text: str, rows: tuple[int, int], spp: int, prefer_ref: bool, width: int = W, height: int = H,
+                  background: int = 0) -> dict:
     import pyoracle
 
-    n_samples = (rows[1] - rows[0]) * W * spp
+    n_samples = (rows[1] - rows[0]) * width * spp
     cores = host_cores()
-    if prefer_ref and pyoracle.ref_available():
+    if prefer_ref and pyoracle.ref_available() and background == 0:
         rs = pyoracle.RefScene(text)
         t0 = time.perf_counter()
-        _, secs = rs.render(W, H, spp, DEPTH, lean=1, rows=rows)
+        _, secs = rs.render(width, height, spp, DEPTH, lean=1, rows=rows)
         el = time.perf_counter() - t0
         kind, threads = "reference", pyoracle.ref_lib().ref_hardware_concurrency()
         note = "reference sources (oracle/_ref), one std::async task per row as main.cpp:157-159"
     else:
         os_ = pyoracle.Scene(text)
         t0 = time.perf_counter()
-        os_.render(W, H, spp, DEPTH, semantics=0, background=0, seed=9, nthreads=cores, rows=rows)
+        os_.render(width, height, spp, DEPTH, semantics=0, background=background, seed=9, nthreads=cores, rows=rows)
         el = time.perf_counter() - t0
         kind, threads = "port", cores
         note = "CPU oracle port of the reference algorithm, all host cores"
     return {"value": n_samples / el / 1e6, "unit": "Msamples/s", "cores": threads, "kind": kind,
-            "sample": f"rows {rows[0]}..{rows[1]} of 600x600 at {spp} spp ({n_samples} samples), {note}",
+            "sample": f"rows {rows[0]}..{rows[1]} of {width}x{height} at {spp} spp ({n_samples} samples), {note}",
             "seconds": el}
 
 
@@ -190,45 +249,43 @@ def reference_arm(args) -> None:
            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": {"workload": WORKLOAD},
            "cpu_baseline": {"value": v, "unit": "Msamples/s", "cores": leg["cores"], "kind": leg["kind"],
-                            "sample": leg["sample"]},
+                            "sample": leg["sample"], **host_info()},
            "e2e": {"value": v, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
 
-def batch_bench(args) -> None:
+def batch_leg(ctx, stream, steps: int, warmup: int, bvh: str = "reference", block: int = 0, wave: int = 0,
+              with_cpu: bool = True) -> dict:
     """64 seeded random-sphere scenes (50..5000 spheres, 256^2..1024^2, 8..64
-    spp) rendered in one persistent launch replayed from a CUDA graph."""
+    spp) rendered in one persistent launch replayed from a CUDA graph; CPU
+    baseline: the reference algorithm scene by scene on a band of rows of
+    four of the scenes (smallest to largest sphere count)."""
     import torch
     import tpt
     from tpt import scenes
 
-    torch.cuda.set_device(0)
-    ctx = tpt.Context(0)
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
-    ctx.set_stream(stream.cuda_stream)
     sds = scenes.batch_scenes(seed=2, count=64)
     texts = [sd.text() for sd in sds]
     t0 = time.perf_counter()
-    compiled = [tpt.Scene(t, bvh=args.bvh) for t in texts]  # host: parse, reference or SAH tree, flatten
+    compiled = [tpt.Scene(t, bvh=bvh) for t in texts]  # host: parse, reference or SAH tree, flatten
     t1 = time.perf_counter()
     slots = [ctx.upload(sc) for sc in compiled]  # device copy (+ the GPU build of an LBVH scene)
     t2 = time.perf_counter()
     jobs = [(slot, sd.meta["width"], sd.meta["height"], sd.meta["spp"]) for slot, sd in zip(slots, sds)]
     outs = [torch.empty((h, w, 3), dtype=torch.float32, device="cuda") for _, w, h, _ in jobs]
     ptrs = [o.data_ptr() for o in outs]
-    kw = dict(max_depth=50, background=tpt.BACKGROUND_SKY, seed=1, block=args.block, variant=args.wave)
+    kw = dict(max_depth=50, background=tpt.BACKGROUND_SKY, seed=1, block=block, variant=wave)
     tuned = None
-    if args.block == 0 and args.wave == 0:  # block, register variant, walk threshold by the autotuner (untimed)
+    if block == 0 and wave == 0:  # block, register variant, walk threshold by the autotuner (untimed)
         tuned = tpt.autotune_batch(ctx, jobs, ptrs, 8, max_depth=50, background=tpt.BACKGROUND_SKY, seed=1)
         kw.update(block=tuned[0], variant=tuned[1], flat_nodes=tuned[2])
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         tpt.render_batch(ctx, jobs, outs=ptrs, **kw)
     torch.cuda.synchronize()
     clocks = ClockSampler(0)
     clocks.start()
     times, st = [], None
-    for k in range(args.steps):
+    for k in range(steps):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         _, st = tpt.render_batch(ctx, jobs, outs=ptrs, **kw)
@@ -236,26 +293,117 @@ def batch_bench(args) -> None:
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))
     clk = clocks.stop()
+    for sl in slots:
+        ctx.release(sl)
     samples = st["samples"]
     ms = float(np.mean(times))
+    value = samples / (ms / 1e3) / 1e6
+    cpu = None
+    if with_cpu:
+        order = sorted(range(len(sds)), key=lambda k: sds[k].meta["n_spheres"])
+        picks = [order[0], order[len(order) // 3], order[2 * len(order) // 3], order[-1]]
+        tot_s, tot_n, kinds = 0.0, 0, set()
+        for k in picks:
+            sd = sds[k]
+            w, h, spp = sd.meta["width"], sd.meta["height"], sd.meta["spp"]
+            r = _cpu_leg_once(texts[k], (h // 2 - 4, h // 2 + 4), spp, False, w, h, 1)
+            tot_s += r["seconds"]
+            tot_n += 8 * w * spp
+            kinds.add(r["kind"])
+        cpu = {"value": tot_n / tot_s / 1e6, "unit": "Msamples/s", "cores": host_cores(), "kind": "port",
+               "sample": "8 rows through the middle of 4 of the 64 scenes (%s spheres) at their spp, scene by "
+                         "scene, CPU oracle port of the reference algorithm, all host cores" %
+                         "/".join(str(sds[k].meta["n_spheres"]) for k in picks)}
+    return {"workload": "batch_64_random_sphere_scenes", "value": value, "unit": "Msamples/s", "ms_per_step": ms,
+            "steps": steps, "scenes": len(jobs), "samples_per_step": samples, "bvh": bvh,
+            "launch": {"block": kw["block"], "variant": kw["variant"], "flat_nodes": kw.get("flat_nodes", 0),
+                       "autotuned": tuned is not None},
+            "segments_per_step": st["segments"], "scene_compile_s": t1 - t0, "scene_upload_s": t2 - t1,
+            "gpu_launches": st["kernel_launches"] * steps, "clocks": clk, "cpu_baseline": cpu,
+            "vs_cpu": value / cpu["value"] if cpu else None}
+
+
+def batch_bench(args) -> None:
+    """The batch workload alone (--workload batch)."""
+    import torch
+    import tpt
+
+    torch.cuda.set_device(0)
+    ctx = tpt.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    r = batch_leg(ctx, stream, args.steps, args.warmup, args.bvh, args.block, args.wave, not args.no_cpu)
     out = {"metric": "Msamples/s (64-scene random-sphere batch, one persistent launch, 1 GPU)",
-           "value": samples / (ms / 1e3) / 1e6, "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "value": r["value"], "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": "batch_64_random_sphere_scenes", "scenes": len(jobs), "samples_per_step": samples,
-                      "bvh": args.bvh,
-                      "launch": {"block": kw["block"], "variant": kw["variant"], "flat_nodes": kw.get("flat_nodes", 0),
-                                 "autotuned": tuned is not None},
-                      "spheres": [sd.meta["n_spheres"] for sd in sds][:8] + ["..."],
-                      "segments_per_step": st["segments"], "scene_compile_s": t1 - t0, "scene_upload_s": t2 - t1},
-           "gpu_launches": st["kernel_launches"] * args.steps, "clocks": clk}
+           "config": {k: r[k] for k in ("workload", "scenes", "samples_per_step", "bvh", "launch",
+                                         "segments_per_step", "scene_compile_s", "scene_upload_s")},
+           "gpu_launches": r["gpu_launches"], "clocks": r["clocks"], "cpu_baseline": r["cpu_baseline"]}
     print(json.dumps(out))
     ctx.close()
 
 
-def replica_seed(base: int, rank: int) -> int:
-    """Seed of rank `rank`'s replica: independent sample streams per GPU."""
-    return base + 1_000_003 * rank
+def plain_leg(ctx, stream, name: str, text: str, width: int, height: int, spp: int, background: int, steps: int,
+              cpu_rows: tuple[int, int], cpu_spp: int, with_cpu: bool = True) -> dict:
+    """One plain-tracer workload: autotuned launch, `steps` frames timed with
+    CUDA events on the library's stream (L2 flushed between frames), image
+    left in HBM; CPU baseline on a band of rows of the same frame."""
+    import torch
+    import tpt
+
+    slot = ctx.upload(tpt.Scene(text))
+    tuned = tpt.autotune(ctx, slot, width, height, 4, max_depth=DEPTH, background=background)
+    kw = dict(max_depth=DEPTH, background=background, engine=tuned[0], block=tuned[1], wave=tuned[2],
+              flat_nodes=tuned[3])
+    img = torch.empty((height, width, 3), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    ctx.render(slot, width, height, spp, out=img.data_ptr(), seed=1, **kw)
+    times, segs = [], 0
+    for k in range(steps):
+        flush.fill_(k & 0xff)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _, st = ctx.render(slot, width, height, spp, out=img.data_ptr(), seed=10 + k, **kw)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+        segs += st["segments"]
+    ctx.release(slot)
+    ms = float(np.mean(times))
+    value = width * height * spp / (ms / 1e3) / 1e6
+    cpu = None
+    if with_cpu:
+        cpu = cpu_leg(text, cpu_rows, cpu_spp, prefer_ref=True, width=width, height=height, background=background)
+        cpu.pop("seconds", None)
+    return {"workload": name, "value": value, "unit": "Msamples/s", "ms_per_step": ms, "steps": steps,
+            "width": width, "height": height, "spp": spp, "semantics": "reference",
+            "background": ["black", "sky"][background], "segments_per_sample": segs / steps / (width * height * spp),
+            "engine": "%s (autotuned: block %d, %s %d)" % (["auto", "wavefront", "persistent"][tuned[0]], tuned[1],
+                                                          "variant" if tuned[0] == 2 else "queue", tuned[2]),
+            "cpu_baseline": cpu, "vs_cpu": value / cpu["value"] if cpu else None}
+
+
+def other_configs(ctx, stream, with_cpu: bool) -> dict:
+    """The benchmark definition's other throughput workloads."""
+    from tpt import scenes
+
+    out = {}
+    for key, fn in (("one_weekend_400x400_16spp", lambda: plain_leg(
+                        ctx, stream, "one_weekend_400x400_16spp_depth50", scenes.one_weekend().text(), 400, 400, 16,
+                        1, 10, (0, 400), 16, with_cpu)),
+                    ("batch_64_scenes_reference_bvh", lambda: batch_leg(ctx, stream, 2, 1, "reference",
+                                                                        with_cpu=with_cpu)),
+                    ("next_week_800x800_256spp", lambda: plain_leg(
+                        ctx, stream, "next_week_800x800_256spp_depth50", scenes.next_week().text(), 800, 800, 256, 0,
+                        3, (368, 432), 16, with_cpu))):
+        try:
+            out[key] = fn()
+        except Exception as e:  # reported, never fatal to the headline line
+            out[key] = {"error": str(e)}
+    return out
 
 
 def max_over_ranks(ms: float, dist, device: str) -> float:
@@ -269,9 +417,10 @@ def max_over_ranks(ms: float, dist, device: str) -> float:
     return float(t.item())
 
 
-def job_msamples(samples_per_rank: int, world: int, t_max_ms: float) -> float:
-    """Whole-job throughput: every rank's samples over the slowest rank's time."""
-    return samples_per_rank * world / (t_max_ms / 1e3) / 1e6
+def frame_msamples(samples: int, t_max_ms: float) -> float:
+    """Whole-job throughput of a split frame: the frame's samples (all ranks'
+    shares together) over the slowest rank's time."""
+    return samples / (t_max_ms / 1e3) / 1e6
 
 
 def _relmse(x, ref, eps=1e-2) -> float:
@@ -296,9 +445,13 @@ def learned_equal_time(ctx, which: str) -> dict:
     nrc:    the seeded next-week scene, 800x800, plain at 256 spp against the
             cached renderer (paths terminated into the cache after 2 bounces)
             at the spp that takes the same time; FP64 reference 4096 spp.
-    The equal-time side is the mean over three seeds (each run trains its own
-    network online; the per-seed ratios are reported too).  The reference's
-    own noise adds ~spp/ref_spp of the plain relMSE to both."""
+    Every point (plain, learned at equal spp, at equal time, and the points
+    of the time-to-plain-relMSE search) is the mean over three seeds (each
+    learned run trains its own network online; per-seed values are reported
+    too).  time_to_plain_relmse_ratio = the learned renderer's wall time at
+    the spp where its relMSE equals the plain tracer's, over the plain
+    tracer's wall time.  The reference's own noise adds ~spp/ref_spp of the
+    plain relMSE to both."""
     import torch
     import tpt
     from tpt import scenes
@@ -323,28 +476,78 @@ def learned_equal_time(ctx, which: str) -> dict:
         return (time.perf_counter() - t0) * 1e3, r
 
     ref, _ = ctx.render(slot, w, h, ref_spp, semantics=tpt.SEMANTICS_PHYSICAL, seed=999, fp64=True)
-    plain = lambda n: ctx.render(slot, w, h, n, semantics=tpt.SEMANTICS_PHYSICAL, seed=5, out=dev.data_ptr())
-    plain(spp)  # warm-up
-    t_plain, _ = timed(lambda: plain(spp))
-    e_plain = _relmse(dev.cpu().numpy(), ref)
     passes = 8
-    seeds = (5, 6, 7)  # equal-time runs: the mean over three seeds (each run trains its own network)
+    seeds = (5, 6, 7)  # both sides: the mean over three seeds (each learned run trains its own network)
+    plain = lambda n, sd_: ctx.render(slot, w, h, n, semantics=tpt.SEMANTICS_PHYSICAL, seed=sd_,
+                                      out=dev.data_ptr())
+    plain(spp, seeds[0])  # warm-up
+    t_p, e_p = [], []
+    for sd_ in seeds:
+        t, _ = timed(lambda: plain(spp, sd_))
+        t_p.append(t)
+        e_p.append(_relmse(dev.cpu().numpy(), ref))
+    t_plain, e_plain = float(np.mean(t_p)), float(np.mean(e_p))
+
+    def at(run, n):
+        """mean wall time and relMSE over the seeds at n spp"""
+        ts, es, last = [], [], None
+        for sd_ in seeds:
+            t, last = timed(lambda: run(n, dev.data_ptr(), sd_))
+            ts.append(t)
+            es.append(_relmse(dev.cpu().numpy(), ref))
+        return float(np.mean(ts)), float(np.mean(es)), es, last
+
+    def time_to_plain(run, pts):
+        """Wall time the learned renderer needs to reach the plain tracer's
+        relMSE: secant steps on log(relMSE) against log(spp) from the points
+        measured so far (spp, ms, relMSE), three seeds per point, until a
+        point lands within 5 % of the target; the time at the target spp
+        is interpolated linearly between the two nearest points."""
+        for _ in range(3):
+            pts.sort()
+            if any(abs(np.log(e / e_plain)) < 0.05 for _, _, e in pts):
+                break
+            below = [p for p in pts if p[2] <= e_plain]
+            above = [p for p in pts if p[2] > e_plain]
+            a = max(above) if above else None
+            b = min(below) if below else None
+            if a is None or b is None:  # extrapolate from the two outermost points
+                a, b = (pts[-2], pts[-1]) if above else (pts[0], pts[1])
+            slope = (np.log(b[2]) - np.log(a[2])) / (np.log(b[0]) - np.log(a[0])) if b[0] != a[0] else -1.0
+            slope = min(slope, -0.25)
+            n = int(round(np.exp(np.log(a[0]) + (np.log(e_plain) - np.log(a[2])) / slope) / passes)) * passes
+            n = int(min(max(n, passes), 8 * spp))
+            if any(p[0] == n for p in pts):
+                break
+            t, e, _, _ = at(run, n)
+            pts.append((n, t, e))
+        pts.sort()
+        # log-log interpolation of spp at the target between the bracketing points, time linear in spp
+        lo = [p for p in pts if p[2] > e_plain]
+        hi = [p for p in pts if p[2] <= e_plain]
+        a = max(lo) if lo else pts[0]
+        b = min(hi) if hi else pts[-1]
+        if a[0] == b[0]:
+            n_star, t_star = float(a[0]), a[1]
+        else:
+            f = (np.log(e_plain) - np.log(a[2])) / (np.log(b[2]) - np.log(a[2]))
+            n_star = float(np.exp(np.log(a[0]) + f * (np.log(b[0]) - np.log(a[0]))))
+            t_star = a[1] + (n_star - a[0]) / (b[0] - a[0]) * (b[1] - a[1])
+        return {"spp": n_star, "ms": t_star, "ratio": t_star / t_plain, "reached": bool(hi),
+                "points": [{"spp": p[0], "ms": p[1], "relmse": p[2]} for p in pts]}
 
     def compare(run):
         run(spp, dev.data_ptr(), seeds[0])  # warm-up
-        t_eq, r = timed(lambda: run(spp, dev.data_ptr(), seeds[0]))
-        e_eq = _relmse(dev.cpu().numpy(), ref)
+        t_eq, e_eq, _, r = at(run, spp)
         spp_et = max(passes, int(round(spp * t_plain / t_eq / passes)) * passes)
-        t_et, e_et = [], []
-        for sd_ in seeds:
-            t, _ = timed(lambda: run(spp_et, dev.data_ptr(), sd_))
-            t_et.append(t)
-            e_et.append(_relmse(dev.cpu().numpy(), ref))
-        return ({"spp": spp, "ms": t_eq, "relmse": e_eq, "stats": r[2]},
-                {"spp": spp_et, "ms": float(np.mean(t_et)), "relmse": float(np.mean(e_et)), "seeds": list(seeds)},
-                {"equal_spp_relmse_ratio": e_eq / e_plain, "equal_time_relmse_ratio": float(np.mean(e_et)) / e_plain,
-                 "equal_time_relmse_ratio_per_seed": [e / e_plain for e in e_et],
-                 "time_ratio_at_equal_spp": t_eq / t_plain})
+        t_et, e_et, e_et_seeds, _ = at(run, spp_et)
+        ttp = time_to_plain(run, [(spp, t_eq, e_eq), (spp_et, t_et, e_et)])
+        return ({"spp": spp, "ms": t_eq, "relmse": e_eq, "stats": r[2], "seeds": list(seeds)},
+                {"spp": spp_et, "ms": t_et, "relmse": e_et, "seeds": list(seeds)},
+                {"equal_spp_relmse_ratio": e_eq / e_plain, "equal_time_relmse_ratio": e_et / e_plain,
+                 "equal_time_relmse_ratio_per_seed": [e / e_plain for e in e_et_seeds],
+                 "time_ratio_at_equal_spp": t_eq / t_plain,
+                 "time_to_plain_relmse": ttp, "time_to_plain_relmse_ratio": ttp["ratio"]})
 
     eq, et, ratios = compare(run)
     extra = {}
@@ -353,12 +556,13 @@ def learned_equal_time(ctx, which: str) -> dict:
                                                                         alpha=0.25))
         extra = {"guided_alpha_0.25": dict(alpha=0.25, equal_time_spp=et2["spp"], equal_time_ms=et2["ms"],
                                            equal_time_relmse=et2["relmse"], **ratios2)}
+    plain_rec = {"spp": spp, "ms": t_plain, "relmse": e_plain, "seeds": list(seeds),
+                 "ms_per_seed": t_p, "relmse_per_seed": e_p}
     ctx.release(slot)
     name = "cornell_40x40_light_two_boxes" if which == "guided" else "next_week_final_seeded"
     return {"scene": name, "width": w, "height": h, "ref_spp_fp64": ref_spp,
             "engine": ["auto", "wavefront", "persistent"][tuned[0]],
-            "plain": {"spp": spp, "ms": t_plain, "relmse": e_plain},
-            which: eq, which + "_equal_time": et, **ratios, **extra}
+            "plain": plain_rec, which: eq, which + "_equal_time": et, **ratios, **extra}
 
 
 def main() -> None:
@@ -376,6 +580,8 @@ def main() -> None:
                          "linear BVH (built on the GPU at upload)")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the equal-time guided / cached comparisons of the default line")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other throughput workloads (one weekend, batch, next week) of the default line")
     ap.add_argument("--spp", type=int, default=SPP, help="smaller cases for profiling only")
     ap.add_argument("--workload", default="cornell", choices=["cornell", "batch"],
                     help="cornell: the headline workload; batch: 64 seeded random-sphere scenes in one launch")
@@ -399,7 +605,7 @@ def main() -> None:
 
         dist.init_process_group("nccl")
     import tpt
-    from tpt import scenes
+    from tpt import frame_split, scenes
 
     text = scenes.cornell().text()
     ctx = tpt.Context(local)
@@ -427,8 +633,20 @@ def main() -> None:
     if rank == 0 and not args.no_cpu:
         cpu = cpu_leg(text, (0, 600), 32)
         cpu.pop("seconds", None)
+        cpu.update(host_info())
+    # one frame per step; with N ranks each renders its share of the samples
+    # and the float4 accumulators are summed across ranks (NCCL) and resolved
+    accum = torch.empty(W * H * 4, dtype=torch.float32, device="cuda") if world > 1 else None
+    rkw = {x: y for x, y in kw.items() if x != "seed"}
+
+    def frame(seed, profile=False):
+        if world == 1:
+            return ctx.render(slot, W, H, args.spp, out=img.data_ptr(), profile=profile, seed=seed, **rkw)[1]
+        return frame_split.render_split_frame(ctx, slot, W, H, args.spp, accum, rank, world, dist,
+                                              out=img.data_ptr(), seed=seed, profile=profile, **rkw)[1]
+
     for w in range(args.warmup):
-        ctx.render(slot, W, H, args.spp, out=img.data_ptr(), **kw)
+        frame(1)
     barrier()
     clocks = ClockSampler(local)
     clocks.start()
@@ -438,8 +656,7 @@ def main() -> None:
         barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        _, st = ctx.render(slot, W, H, args.spp, out=img.data_ptr(), profile=True,
-                           seed=replica_seed(100 + k, rank), **{x: y for x, y in kw.items() if x != "seed"})
+        st = frame(100 + k, profile=True)
         e1.record(stream)
         barrier()
         times.append(e0.elapsed_time(e1))
@@ -450,20 +667,25 @@ def main() -> None:
     clk = clocks.stop()
     ms = float(np.sum(times))
     t_max = max_over_ranks(ms, dist, "cuda")
-    value = job_msamples(W * H * args.spp * args.steps, world, t_max)
+    value = frame_msamples(W * H * args.spp * args.steps, t_max)
 
-    # e2e through the C ABI with host buffers
-    host_img = np.zeros((H, W, 3), np.float32)
+    # e2e through the C ABI with host buffers: compile + upload, render (this
+    # rank's share, the sum across ranks), resolve, image to the host
     e2e_times = []
     for k in range(max(1, min(args.steps, 3))):
         barrier()
         t0 = time.perf_counter()
         sc = tpt.Scene(text)
         s2 = ctx.upload(sc)
-        host_img, _ = ctx.render(s2, W, H, args.spp, seed=200 + k, **{x: y for x, y in kw.items() if x != "seed"})
+        if world == 1:
+            host_img, _ = ctx.render(s2, W, H, args.spp, seed=200 + k, **rkw)
+        else:
+            host_img, _ = frame_split.render_split_frame(ctx, s2, W, H, args.spp, accum, rank, world, dist,
+                                                         seed=200 + k, **rkw)
         ctx.release(s2)
         e2e_times.append(time.perf_counter() - t0)
-    e2e_value = W * H * args.spp / float(np.mean(e2e_times)) / 1e6
+    e2e_ms = max_over_ranks(1e3 * float(np.mean(e2e_times)), dist, "cuda")
+    e2e_value = frame_msamples(W * H * args.spp, e2e_ms)
 
     learned = None
     if rank == 0 and not args.no_learned and args.spp == SPP:
@@ -473,6 +695,9 @@ def main() -> None:
                 learned[which] = learned_equal_time(ctx, which)
             except Exception as e:  # reported, never fatal to the throughput line
                 learned[which] = {"error": str(e)}
+    configs = None
+    if rank == 0 and not args.no_configs and args.spp == SPP:
+        configs = other_configs(ctx, stream, not args.no_cpu)
 
     peaks = _peaks()
     roof = None
@@ -481,7 +706,8 @@ def main() -> None:
         wavefront = kw["engine"] == 1
         per_seg = TRAVERSE_BYTES_PER_SEGMENT if wavefront else BYTES_PER_SEGMENT
         algo_bytes = seg_per_launch * per_seg
-        achieved = algo_bytes / (tr_ms / tr_n / 1e3) / 1e9
+        launch_s = tr_ms / tr_n / 1e3
+        achieved = algo_bytes / launch_s / 1e9
         # DRAM bytes per segment from the ncu capture of the same kernel on the
         # 16 spp case (NCU_DRAM_BYTES_PER_SEGMENT), scaled to this launch's segments
         traffic = None if wavefront else seg_per_launch * NCU_DRAM_BYTES_PER_SEGMENT
@@ -493,32 +719,51 @@ def main() -> None:
                 "kernel_share": tr_ms / ms,
                 "note": ("algorithmic bytes = the wavefront traffic floor per ray segment (ray, hit and path "
                          "state written and read); the kernel keeps that state in registers and the scene in "
-                         "L1/L2, so it is issue-bound, not HBM-bound: see issue_roofline")}
+                         "L1/L2, so it is issue-bound, not HBM-bound: see issue_roofline and flops")}
+        if rank == 0 and args.spp == SPP:
+            # useful work: the reference algorithm's arithmetic per segment (oracle counts
+            # over a band of the frame) at the kernel's measured segment rate, against the
+            # FP32 peak (derived: 152 SMs x 128 lanes x 2 flops per FMA x maximum SM clock)
+            u = useful_flops_per_segment(text, W, H, (280, 320), 4)
+            peak_fp32 = SMS * FP32_LANES_PER_SM * 2 * peaks["sm_mhz"] / 1e6  # TFLOP/s
+            ach_fp32 = u["flops_per_segment"] * seg_per_launch / launch_s / 1e12
+            roof["flops"] = {"bound": "fp32", "achieved": ach_fp32, "peak": peak_fp32, "unit": "TFLOP/s",
+                             "frac": ach_fp32 / peak_fp32, "peak_source": "derived (152 x 128 x 2 x sm_max_mhz)",
+                             "useful_flops_per_segment": u["flops_per_segment"],
+                             "counts_per_segment": u["counts_per_segment"],
+                             "oracle_sample": u["sample"],
+                             "note": ("oracle-counted work of the reference's traversal (every child of every "
+                                      "bvh_node whose box the ray enters) and shading, weighted 12 per slab "
+                                      "test, 20 per sphere, 10 per rect, 40 per instance transform, 30 per "
+                                      "lambertian or metal scatter, 60 per dielectric, 40 per light pdf")}
         if not wavefront:
             peak_issue = SMS * SCHEDULERS_PER_SM * peaks["sm_mhz"] / 1e3  # G warp instructions / s
-            ach_issue = seg_per_launch * NCU_WARP_INST_PER_SEGMENT / (tr_ms / tr_n / 1e3) / 1e9
+            ach_issue = seg_per_launch * NCU_WARP_INST_PER_SEGMENT / launch_s / 1e9
             roof["issue_roofline"] = {
                 "bound": "issue", "achieved": ach_issue, "peak": peak_issue, "unit": "G warp-inst/s",
                 "frac": ach_issue / peak_issue, "warp_inst_per_segment": NCU_WARP_INST_PER_SEGMENT,
-                "note": ("the binding roof: instructions per segment from the ncu capture of the same kernel "
-                         "(16 spp case) x segments per second measured here; peak = 152 SMs x 4 schedulers x "
-                         "1 instruction per cycle at the maximum SM clock")}
+                "note": ("instructions per segment from the ncu capture of the same kernel (16 spp case, "
+                         "NCU_WARP_INST_PER_SEGMENT) x segments per second measured here; peak = 152 SMs x 4 "
+                         "schedulers x 1 instruction per cycle at the maximum SM clock")}
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
-               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic",
                "config": {"workload": WORKLOAD if args.spp == SPP else f"{WORKLOAD} (profiling case: {args.spp} spp)",
                           "width": W, "height": H, "spp": args.spp, "max_depth": DEPTH,
                           "semantics": "reference",
                           "engine": (["auto", "wavefront", "persistent"][tuned[0]] + " (autotuned: block %d, %s %d)" % (
                               tuned[1], "variant" if tuned[0] == 2 else "queue", tuned[2]) if tuned else
                               ["auto", "wavefront", "persistent"][args.engine]),
+                          "split": ("one frame, samples split across %d ranks, float4 accumulators "
+                                    "summed (NCCL all-reduce)" % world) if world > 1 else "one GPU",
                           "l2": "flushed between timed steps (256 MB write)",
                           "segments_per_step": segs / args.steps},
                "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": int(arena_bytes),
                        "d2h_bytes_per_step": int(W * H * 3 * 4)},
                "gpu_launches": int(launches), "clocks": clk, "roofline": roof, "cpu_baseline": cpu,
-               "learned_equal_time": learned}
+               "learned_equal_time": learned, "other_configs": configs}
         print(json.dumps(out))
     ctx.close()
     if dist is not None:

@@ -509,6 +509,23 @@ tpt_status tpt_scene_set_camera(tpt_scene *s, const float lookfrom[3], const flo
  * divides by zero).  Persistent engine; physical or reference semantics. */
 tpt_status tpt_render_snapshots(tpt_context *ctx, int32_t slot, const tpt_render_params *p, int32_t bonus_pic,
                                 float *out_rgb, float *snapshots_rgb, int32_t mem, tpt_render_stats *stats);
+/* A frame split across GPUs (the reference renders one frame in row tasks,
+ * main.cpp:157-159; here the split is over samples, so every rank renders
+ * the whole image).  tpt_render_range renders samples [sample_begin,
+ * sample_end) of every pixel (p->spp is ignored) with the persistent engine
+ * and writes the per-pixel SUMS, not the mean, into accum_dev: device
+ * memory of width*height float4 (16-byte aligned; xyz = radiance sum, w
+ * unused), cleared first.  Each sample draws from its own (pixel, sample
+ * index) stream, so the shares of any partition of [0, spp) add up - after
+ * a sum-reduce of the accumulators across ranks - to what one GPU
+ * accumulates for the whole frame, up to float summation order.
+ * tpt_resolve_sums turns summed accumulators of spp samples per pixel into
+ * the mean image (TPT_MEM_HOST or TPT_MEM_DEVICE output).  Both wait for the
+ * context's stream.  (No counterpart in the reference.) */
+tpt_status tpt_render_range(tpt_context *ctx, int32_t slot, const tpt_render_params *p, int32_t sample_begin,
+                            int32_t sample_end, float *accum_dev, tpt_render_stats *stats);
+tpt_status tpt_resolve_sums(tpt_context *ctx, const float *accum_dev, int32_t width, int32_t height, int32_t spp,
+                            float *out_rgb, int32_t mem);
 /* Reads a PPM image (P3 or P6, maxval <= 255, '#' comments) for
  * tpt_image_texture: the stand-in for the stb_image decode of
  * utils.cc:236-240.  Call with rgb8 = NULL to get the size; then with a

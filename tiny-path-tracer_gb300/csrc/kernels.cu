@@ -1620,6 +1620,68 @@ extern "C" tpt_status tpt_render_snapshots(tpt_context *c, int32_t slot, const t
   return TPT_OK;
 }
 
+// One share of a frame split across GPUs: samples [begin, end) of every
+// pixel, summed into the caller's float4 accumulators.  The persistent
+// engine's global sample counter starts at begin * npix, and every sample
+// draws from its own (pixel, sample index) stream, so the shares of any
+// partition of [0, spp) sum to the accumulators of the whole frame.
+extern "C" tpt_status tpt_render_range(tpt_context *c, int32_t slot, const tpt_render_params *p,
+                                       int32_t sample_begin, int32_t sample_end, float *accum_dev,
+                                       tpt_render_stats *stats) {
+  if (!c || !p || !accum_dev) return TPT_ERR_INVALID_ARGUMENT;
+  if (slot < 0 || slot >= (int32_t)c->slots.size() || !c->slots[slot].live) return TPT_ERR_BAD_HANDLE;
+  if (p->width <= 0 || p->height <= 0 || p->max_depth < 0 || sample_begin < 0 || sample_end < sample_begin)
+    return TPT_ERR_INVALID_ARGUMENT;
+  if (((uintptr_t)accum_dev & 15) != 0) return TPT_ERR_INVALID_ARGUMENT;  // float4 per pixel
+  const unsigned long long npix = (unsigned long long)p->width * p->height;
+  if (npix > 0x7fffffffull) return TPT_ERR_INVALID_ARGUMENT;
+  TPT_CUDA(cudaSetDevice(c->device));
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  TPT_CUDA(cudaMemsetAsync(accum_dev, 0, npix * sizeof(float4), c->stream));
+  if (sample_end > sample_begin) {
+    const Slot &sl = c->slots[slot];
+    int block = p->block > 0 ? p->block : 128, variant = p->wave;
+    if (p->engine == TPT_ENGINE_AUTO && sl.tuned && sl.tp.engine == TPT_ENGINE_PERSISTENT) {
+      block = sl.tp.block;
+      variant = sl.tp.wave;
+    }
+    DevScene S = sl.ds;
+    S.flat_max = p->flat_nodes > 0 ? p->flat_nodes : (sl.tuned ? sl.tp.flat_nodes : c->flat_nodes);
+    const RenderCfg cfg{p->max_depth, p->semantics, p->background, p->sky_scale,
+                        make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32)), p->refill > 0 ? p->refill : 1};
+    const FrameDesc F{p->width, p->height, sample_end, npix * (unsigned long long)sample_end, (float4 *)accum_dev,
+                      nullptr};
+    const tpt_status st = run_persistent(c, S, cfg, F, block, variant, p->profile != 0, stats,
+                                         npix * (unsigned long long)sample_begin);
+    if (st != TPT_OK) return st;
+  }
+  TPT_CUDA(cudaStreamSynchronize(c->stream));
+  if (stats) stats->samples = (int64_t)npix * (sample_end - sample_begin);
+  return TPT_OK;
+}
+
+// Mean image from summed float4 accumulators (after the sum across ranks).
+extern "C" tpt_status tpt_resolve_sums(tpt_context *c, const float *accum_dev, int32_t width, int32_t height,
+                                       int32_t spp, float *out_rgb, int32_t mem) {
+  if (!c || !accum_dev || !out_rgb || width <= 0 || height <= 0 || spp <= 0) return TPT_ERR_INVALID_ARGUMENT;
+  if (((uintptr_t)accum_dev & 15) != 0 || (mem != TPT_MEM_HOST && mem != TPT_MEM_DEVICE))
+    return TPT_ERR_INVALID_ARGUMENT;
+  const unsigned long long npix = (unsigned long long)width * height;
+  if (npix > 0x7fffffffull) return TPT_ERR_INVALID_ARGUMENT;
+  TPT_CUDA(cudaSetDevice(c->device));
+  tpt_status st;
+  if (mem == TPT_MEM_HOST && (st = ensure(c->staging, npix * 3 * sizeof(float))) != TPT_OK) return st;
+  const FrameDesc R{width, height, spp, npix * (unsigned long long)spp, (float4 *)accum_dev, nullptr};
+  float *dst = mem == TPT_MEM_HOST ? (float *)c->staging.p : out_rgb;
+  const int rgrid = (int)std::min<unsigned long long>((npix + 255) / 256, (unsigned long long)c->sm_count * 16);
+  k_resolve<<<rgrid, 256, 0, c->stream>>>(R, dst);
+  TPT_CUDA(cudaGetLastError());
+  if (mem == TPT_MEM_HOST)
+    TPT_CUDA(cudaMemcpyAsync(out_rgb, dst, npix * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  TPT_CUDA(cudaStreamSynchronize(c->stream));
+  return TPT_OK;
+}
+
 extern "C" tpt_status tpt_render_batch(tpt_context *c, const tpt_batch_item *items, int32_t n,
                                        const tpt_render_params *p, int32_t mem, tpt_render_stats *stats) {
   if (!c || !items || !p || n < 1 || n > TPT_MAX_BATCH) return TPT_ERR_INVALID_ARGUMENT;

@@ -202,6 +202,10 @@ _SIGS = {
                                          C.c_float, C.c_float]),
     "tpt_render_snapshots": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.c_int32, C.c_void_p,
                                          C.c_void_p, C.c_int32, C.POINTER(RenderStats)]),
+    "tpt_render_range": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.c_int32, C.c_int32,
+                                     C.c_void_p, C.POINTER(RenderStats)]),
+    "tpt_resolve_sums": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                     C.c_int32]),
     "tpt_write_ppm_strip": (C.c_int32, [C.c_char_p, C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_int32]),
     "tpt_read_ppm": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "tpt_render_nrc": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.POINTER(NrcParams),
@@ -376,6 +380,31 @@ class Context:
         check(lib().tpt_render(self._h, slot, C.byref(p), C.c_void_p(int(out)), TPT_MEM_DEVICE, C.byref(st)),
               "render")
         return None, st.as_dict()
+
+    def render_range(self, slot: int, width: int, height: int, sample_begin: int, sample_end: int, accum_ptr: int,
+                     max_depth: int = 50, semantics: int = SEMANTICS_REFERENCE, background: int = BACKGROUND_BLACK,
+                     sky_scale: float = 1.0, seed: int = 1, block: int = 0, wave: int = 0, flat_nodes: int = 0,
+                     engine: int = ENGINE_AUTO, profile: bool = False) -> dict:
+        """Samples [sample_begin, sample_end) of every pixel, summed into the
+        device float4 accumulators at accum_ptr (width*height*4 floats)."""
+        p = make_params(width, height, max(1, sample_end - sample_begin), max_depth, semantics, background,
+                        sky_scale, seed, engine, block, wave, False, profile, flat_nodes)
+        st = RenderStats()
+        check(lib().tpt_render_range(self._h, slot, C.byref(p), sample_begin, sample_end, C.c_void_p(int(accum_ptr)),
+                                     C.byref(st)), "render_range")
+        return st.as_dict()
+
+    def resolve_sums(self, accum_ptr: int, width: int, height: int, spp: int, out=None):
+        """Mean image of summed accumulators: a host array, or written to the
+        device pointer `out`."""
+        if out is None:
+            img = np.zeros((height, width, 3), np.float32)
+            check(lib().tpt_resolve_sums(self._h, C.c_void_p(int(accum_ptr)), width, height, spp, _ptr(img),
+                                         TPT_MEM_HOST), "resolve_sums")
+            return img
+        check(lib().tpt_resolve_sums(self._h, C.c_void_p(int(accum_ptr)), width, height, spp,
+                                     C.c_void_p(int(out)), TPT_MEM_DEVICE), "resolve_sums")
+        return None
 
 
 def render_guided(ctx: "Context", slot: int, width: int, height: int, spp: int, max_depth: int = 50,
