@@ -2,14 +2,14 @@
 // tensor-core MLPs with FP32 accumulation) and their C ABI.
 //
 // Training step of a batch of `rows` samples (rows a multiple of 16):
-//   k_mlp_train   forward (activations in registers; each layer's input also
-//                 written transposed to Ht), per-row loss gradient dY, and the
-//                 backward pass through the layers (ReLU masks from the saved
-//                 activations, transposed weights in shared memory), writing
-//                 each layer's output gradient transposed to dZt;
-//   k_mlp_wgrad   dW_l = dZt_l * Ht_l^T as a tensor-core GEMM over the batch
-//                 (split into row chunks, f32 atomics into the gradient);
-//   k_adam        Adam on f32 master weights, refreshing the f16 copy.
+//   k_mlp_train_tc  forward, per-row loss gradient dY, backward and the weight
+//                   gradients of 128-row tiles, fused, on tcgen05 with tensor-
+//                   memory accumulators (one CTA per SM, weight-gradient sums
+//                   per CTA);
+//   k_grad_reduce   adds the CTAs' sums into the f32 gradient;
+//   k_adam          Adam on f32 master weights, refreshing the f16 copy.
+// Inference (k_mlp_forward) keeps register-resident mma.sync chains: 16 rows
+// per warp, no tensor-memory round trip between layers.
 // Shapes are template parameters: <IN, NH, OUT> with hidden width 64.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -24,6 +24,7 @@
 #include "../../include/tpt.h"
 #include "arena.h"
 #include "mlp.cuh"
+#include "tc05.cuh"
 
 namespace tpt {
 namespace mlp {
@@ -76,213 +77,278 @@ __global__ void __launch_bounds__(WARPS * 32) k_mlp_forward(Net n, const __half 
   }
 }
 
-// Writes the 16 x K block held in A fragments, transposed, into T (row
-// stride `rows`): T[col][r0 + row].
-template <int K>
-__device__ __forceinline__ void store_frag_t(const uint32_t (&a)[K / 16][4], __half *T, int rows, int r0) {
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll
-  for (int kk = 0; kk < K / 16; kk++) {
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-      const int row = r0 + g + 8 * (i & 1);
-      const int col = kk * 16 + 2 * t + 8 * (i >> 1);
-      const __half2 v = *reinterpret_cast<const __half2 *>(&a[kk][i]);
-      T[(size_t)col * rows + row] = __low2half(v);
-      T[(size_t)(col + 1) * rows + row] = __high2half(v);
-    }
+// ------------------------------------------- fused training (tcgen05) ---
+// One training step of a batch on the 5th-generation tensor cores: every CTA
+// (one warpgroup, 128 threads; thread t owns row t of the tile and tensor-
+// memory lane t) takes 128-row tiles of the batch and runs, per tile,
+//   forward   Z_l = H_l W_l^T  (tcgen05.mma, M = 128, f32 in tensor memory);
+//             ReLU and f16 rounding in registers, H_{l+1} back to shared memory
+//   loss      dY of the tile's rows from the f32 outputs (one row per thread)
+//   backward  dW_l += dZ_l^T H_l (M = 64: the layer's outputs, zero-padded;
+//             N = its inputs; K = the tile's rows), accumulated over all of the
+//             CTA's tiles in tensor memory; dH_l = dZ_l W_l (M = 128), masked
+//             by H_l > 0 into dZ_{l-1}.
+// The MMAs read the swizzled shared-memory tiles of tc05.cuh: the forward
+// tiles (X, H_l, W_l) serve K-major in the forward pass and, through MN-major
+// descriptors, as the transposed operands of the backward pass and of the
+// weight gradients, so nothing is transposed or written to HBM between the
+// passes.  One thread issues the MMAs and commits them to an mbarrier; the
+// warpgroup waits on it (with a time limit) and reads the accumulators with
+// tcgen05.ld.  At the end each CTA writes its dW sums to its slice of
+// `partial`, which k_grad_reduce adds into the gradient.
+template <int IN, int NH, int OUT>
+struct TrainLayout {
+  static_assert(IN % 16 == 0 && IN <= 128 && OUT % 16 == 0 && OUT <= 64 && NH >= 1, "supported shapes");
+  static constexpr int KB0 = (IN + 63) / 64;  // 64-column blocks of the input tile
+  __host__ __device__ static constexpr int in_(int l) { return l == 0 ? IN : HID; }
+  __host__ __device__ static constexpr int out_(int l) { return l == NH ? OUT : HID; }
+  __host__ __device__ static constexpr uint32_t w_off(int l) {  // weight tile of layer l: its input blocks of out_(l) rows
+    uint32_t o = 0;
+    for (int j = 0; j < l; j++) o += (uint32_t)((in_(j) + 63) / 64) * out_(j) * 128;
+    return o;
   }
-}
+  static constexpr uint32_t X_OFF = w_off(NH + 1);
+  static constexpr uint32_t H_OFF = X_OFF + KB0 * 16384;  // H_1 .. H_NH
+  static constexpr uint32_t DZ_OFF = H_OFF + NH * 16384;
+  static constexpr uint32_t BAR_OFF = DZ_OFF + 16384;
+  static constexpr uint32_t SMEM = BAR_OFF + 64 + 1024;  // + slack for the 1024-byte alignment
+  __host__ __device__ static constexpr int dw_col(int l) {  // tensor-memory column of layer l's weight gradient
+    int c = 64;                         // columns 0..63: the forward / backward accumulator
+    for (int j = 0; j < l; j++) c += in_(j);
+    return c;
+  }
+  static constexpr uint32_t TMEM_COLS = 512;
+  static_assert(X_OFF % 1024 == 0, "operand tiles start on 1024-byte boundaries");
+  static_assert(dw_col(NH + 1) <= (int)TMEM_COLS, "tensor memory");
+  static_assert(SMEM <= 227 * 1024, "shared memory");
+};
+
+// ~2 s at 2 GHz: an MMA completion that has not arrived by then never will
+constexpr long long TC_WAIT_LIMIT = 4000000000LL;
 
 template <int IN, int NH, int OUT, class Loss>
-__global__ void __launch_bounds__(WARPS * 32)
-    k_mlp_train(Net n, const __half *__restrict__ X, int rows, Loss loss, __half *__restrict__ Ht,
-                __half *__restrict__ dZt, float *loss_sum) {
-  extern __shared__ __half smem[];
-  __half *sw = smem;
-  __half *swt = sw + smem_w_halves(n);
-  float *sy = reinterpret_cast<float *>(swt + smem_wt_halves(n));  // [warp][16][OUT]
-  float *sdy = sy + WARPS * 16 * OUT;                               // [warp][16][OUT]
-  load_weights(n, sw, swt);
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  float *my_y = sy + warp * 16 * OUT, *my_dy = sdy + warp * 16 * OUT;
-  // transposed activation / gradient buffers per layer
-  size_t ht_off[NH + 1], dz_off[NH + 1];
-  {
-    size_t a = 0, b = 0;
-    for (int l = 0; l <= NH; l++) {
-      ht_off[l] = a;
-      dz_off[l] = b;
-      a += (size_t)(l == 0 ? IN : HID) * rows;
-      b += (size_t)(l == NH ? OUT : HID) * rows;
+__global__ void __launch_bounds__(128, 1)
+    k_mlp_train_tc(Net n, const __half *__restrict__ X, int rows, Loss loss, float *__restrict__ partial,
+                   float *loss_sum, int *err) {
+  using T = TrainLayout<IN, NH, OUT>;
+  using namespace tc05;
+  extern __shared__ uint8_t tc_raw[];
+  uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~uintptr_t(1023));
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + T::BAR_OFF + 8);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int n_params = param_count(n);
+
+  // weights: asynchronous 16-byte copies, all in flight at once.  Padding
+  // columns of the tiles (past IN) are never read: the forward MMAs stop at
+  // K = IN and the weight-gradient MMAs at N = IN.
+#pragma unroll 1
+  for (int l = 0; l <= NH; l++) {
+    const int K = T::in_(l), N = T::out_(l);
+    const __half *g = n.w16 + layer_offset(n, l);
+    for (int c = t; c < N * K / 8; c += 128) {
+      const int o = (c * 8) / K, i = c * 8 - o * K;
+      cp_async16(sm + T::w_off(l) + (uint32_t)(i / 64) * N * 128 + sw128_chunk(o, (i % 64) / 8), g + c * 8, 16);
     }
   }
+  cp_async_wait_all();
+  const uint32_t base = smem_addr(sm), bar = base + T::BAR_OFF;
+  if (t == 0) bar_init(bar, 1);
+  if (warp == 0) tmem_alloc(tslot, T::TMEM_COLS);
+  fence_async_smem();
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tm = *tslot;
+  const uint32_t lane_base = tm + ((uint32_t)(warp * 32) << 16);
+  uint32_t phase = 0;
+  bool ok = true, first = true;
   float lsum = 0.f;
-  for (int tile = blockIdx.x * WARPS + warp; tile * 16 < rows; tile += gridDim.x * WARPS) {
-    const int r0 = tile * 16;
-    // ---- forward
-    uint32_t a0[IN / 16][4];
-    load_frag_rows<IN>(X + (size_t)r0 * IN, IN, a0);
-    store_frag_t<IN>(a0, Ht + ht_off[0], rows, r0);
-    float acc[HID / 8][4];
-    layer_mma<IN, HID>(a0, sw + smem_w_offset(n, 0), acc);
-    uint32_t h[HID / 16][4];
-    relu_to_frag<HID>(acc, h);
-    // ReLU masks: bit (kk*4 + i)*2 + half of mask[l-1] says whether this
-    // lane's value of H_l (the input of layer l) is positive
-    uint32_t mask[NH];
+  const int n_tiles = (rows + 127) / 128;
+
+  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int r0 = tile * 128;
+    // ---- the input tile (rows past the batch are zero)
+    constexpr int CH = IN / 8;
+    for (int c = t; c < 128 * CH; c += 128) {
+      const int r = c / CH, k8 = c - r * CH;
+      const bool in = r0 + r < rows;  // rows past the batch: zero-filled copies
+      cp_async16(sm + T::X_OFF + (uint32_t)(k8 / 8) * 16384 + sw128_chunk(r, k8 % 8),
+                 X + (size_t)(in ? r0 + r : 0) * IN + k8 * 8, in ? 16 : 0);
+    }
+    cp_async_wait_all();
+    fence_async_smem();
+    __syncthreads();
+    // ---- forward (loops rolled: each CTA runs its code for a tile or two,
+    // so a compact body keeps instruction fetch off the critical path)
+#pragma unroll 1
+    for (int l = 0; l <= NH; l++) {
+      if (t == 0) {
+        fence_after();
+        const uint32_t a0 = base + (l == 0 ? T::X_OFF : T::H_OFF + (uint32_t)(l - 1) * 16384);
+        const uint32_t b0 = base + T::w_off(l);
+        constexpr uint32_t sbo = 1024;
+        const uint32_t id = idesc_f16(128, T::out_(l), false, false);
+#pragma unroll 1
+        for (int s = 0; s < T::in_(l) / 16; s++)
+          mma_f16(tm, desc(a0 + (uint32_t)(s / 4) * 16384 + (uint32_t)(s % 4) * 32, 16, sbo),
+                  desc(b0 + (uint32_t)(s / 4) * T::out_(l) * 128 + (uint32_t)(s % 4) * 32, 16, sbo), id, s > 0);
+        commit(bar);
+      }
+      const bool got = bar_wait(bar, phase, TC_WAIT_LIMIT);
+      phase ^= 1;
+      if (!__syncthreads_and(got)) {
+        ok = false;
+        break;
+      }
+      fence_after();
+      float v[64];
+      tmem_ld64(lane_base, v);
+      uint8_t *dst = l < NH ? sm + T::H_OFF + (uint32_t)l * 16384 : sm + T::DZ_OFF;
+      if (l < NH) {  // ReLU, f16: row t of H_{l+1}
 #pragma unroll
-    for (int l = 1; l <= NH; l++) {
-      // h = H_l (input of layer l): keep its mask and store it for the weight gradient
-      uint32_t m = 0;
-#pragma unroll
-      for (int kk = 0; kk < HID / 16; kk++)
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-          const uint32_t v = h[kk][i];
-          m |= (uint32_t)((v & 0x7fffu) != 0 && !(v & 0x8000u)) << ((kk * 4 + i) * 2);
-          m |= (uint32_t)((v & 0x7fff0000u) != 0 && !(v & 0x80000000u)) << ((kk * 4 + i) * 2 + 1);
+        for (int c = 0; c < 8; c++) {
+          uint4 q;
+          q.x = pack2(fmaxf(v[8 * c], 0.f), fmaxf(v[8 * c + 1], 0.f));
+          q.y = pack2(fmaxf(v[8 * c + 2], 0.f), fmaxf(v[8 * c + 3], 0.f));
+          q.z = pack2(fmaxf(v[8 * c + 4], 0.f), fmaxf(v[8 * c + 5], 0.f));
+          q.w = pack2(fmaxf(v[8 * c + 6], 0.f), fmaxf(v[8 * c + 7], 0.f));
+          *reinterpret_cast<uint4 *>(dst + sw128_chunk(t, c)) = q;
         }
-      mask[l - 1] = m;
-      store_frag_t<HID>(h, Ht + ht_off[l], rows, r0);
-      if (l < NH) {
-        layer_mma<HID, HID>(h, sw + smem_w_offset(n, l), acc);
-        relu_to_frag<HID>(acc, h);
+      } else {  // the loss of row t; dZ of the output layer (zero past OUT and past the batch)
+        float dy[OUT];
+        if (r0 + t < rows) {
+          lsum += loss.template grad<OUT>(r0 + t, v, dy);
+        } else {
+#pragma unroll
+          for (int o = 0; o < OUT; o++) dy[o] = 0.f;
+        }
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+          float e[8];
+#pragma unroll
+          for (int j = 0; j < 8; j++) e[j] = 8 * c + j < OUT ? dy[(8 * c + j) % OUT] : 0.f;
+          uint4 q;
+          q.x = pack2_sat(e[0], e[1]);
+          q.y = pack2_sat(e[2], e[3]);
+          q.z = pack2_sat(e[4], e[5]);
+          q.w = pack2_sat(e[6], e[7]);
+          *reinterpret_cast<uint4 *>(dst + sw128_chunk(t, c)) = q;
+        }
+      }
+      fence_async_smem();
+      fence_before();
+      __syncthreads();
+    }
+    if (!ok) break;
+    // ---- backward
+#pragma unroll 1
+    for (int l = NH; l >= 0; l--) {
+      if (t == 0) {
+        fence_after();
+        const uint32_t dz = base + T::DZ_OFF;
+        const uint32_t hb = base + (l == 0 ? T::X_OFF : T::H_OFF + (uint32_t)(l - 1) * 16384);
+        // dW_l (+)= dZ_l^T H_l: A = dZ (MN-major, 64 outputs), B = H_l (MN-major,
+        // blocks of 64 inputs 16384 bytes apart), K = 128 rows in steps of 16
+        const uint32_t idw = idesc_f16(64, T::in_(l), true, true);
+#pragma unroll 1
+        for (int s = 0; s < 8; s++)
+          mma_f16(tm + (uint32_t)T::dw_col(l), desc(dz + 2048u * s, 16384, 1024), desc(hb + 2048u * s, 16384, 1024),
+                  idw, !first || s > 0);
+        if (l > 0) {  // dH_l = dZ_l W_l: A = dZ (K-major over the outputs), B = W_l (MN-major)
+          const uint32_t idh = idesc_f16(128, HID, false, true);
+#pragma unroll 1
+          for (int s = 0; s < T::out_(l) / 16; s++)
+            mma_f16(tm, desc(dz + 32u * s, 16, 1024), desc(base + T::w_off(l) + 2048u * s, 16384, 1024), idh, s > 0);
+        }
+        commit(bar);
+      }
+      const bool got = bar_wait(bar, phase, TC_WAIT_LIMIT);
+      phase ^= 1;
+      if (!__syncthreads_and(got)) {
+        ok = false;
+        break;
+      }
+      fence_after();
+      if (l > 0) {  // dZ_{l-1} = dH_l masked by H_l > 0 (the MMAs reading dZ_l are complete)
+        float v[64];
+        tmem_ld64(lane_base, v);
+        const uint8_t *h = sm + T::H_OFF + (uint32_t)(l - 1) * 16384;
+        uint8_t *dz = sm + T::DZ_OFF;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+          const uint4 hv = *reinterpret_cast<const uint4 *>(h + sw128_chunk(t, c));
+          const uint32_t hw[4] = {hv.x, hv.y, hv.z, hv.w};
+          uint32_t q[4];
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            const float2 hf = unpack2(hw[j]);
+            q[j] = pack2_sat(hf.x > 0.f ? v[8 * c + 2 * j] : 0.f, hf.y > 0.f ? v[8 * c + 2 * j + 1] : 0.f);
+          }
+          *reinterpret_cast<uint4 *>(dz + sw128_chunk(t, c)) = make_uint4(q[0], q[1], q[2], q[3]);
+        }
+        fence_async_smem();
+      }
+      fence_before();
+      __syncthreads();
+    }
+    if (!ok) break;
+    first = false;
+  }
+  // ---- this CTA's weight-gradient sums: layer l's row o in lane 32 (o / 16) + o % 16
+  if (ok) {
+    fence_after();
+    const int o = warp * 16 + lane;
+#pragma unroll 1
+    for (int l = 0; l <= NH; l++) {
+      const int K = T::in_(l), N = T::out_(l);
+#pragma unroll 1
+      for (int c0 = 0; c0 < K; c0 += 64) {
+        float v[64];
+        tmem_ld64(lane_base + (uint32_t)(T::dw_col(l) + c0), v);
+        if (lane < 16 && o < N) {
+          float *dst = partial + (size_t)blockIdx.x * n_params + layer_offset(n, l) + (size_t)o * K + c0;
+#pragma unroll
+          for (int i = 0; i < 64; i += 4)
+            if (c0 + i < K)
+              *reinterpret_cast<float4 *>(dst + i) = first ? make_float4(0.f, 0.f, 0.f, 0.f)
+                                                           : make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+        }
       }
     }
-    float out[OUT / 8][4];
-    layer_mma<HID, OUT>(h, sw + smem_w_offset(n, NH), out);
-    // ---- loss: rows through shared memory
-#pragma unroll
-    for (int j = 0; j < OUT / 8; j++) {
-      my_y[g * OUT + j * 8 + 2 * t] = out[j][0];
-      my_y[g * OUT + j * 8 + 2 * t + 1] = out[j][1];
-      my_y[(g + 8) * OUT + j * 8 + 2 * t] = out[j][2];
-      my_y[(g + 8) * OUT + j * 8 + 2 * t + 1] = out[j][3];
-    }
-    __syncwarp();
-    if (lane < 16) lsum += loss.template grad<OUT>(r0 + lane, my_y + lane * OUT, my_dy + lane * OUT);
-    __syncwarp();
-    // ---- backward: dZ of the output layer as A fragments (k = output index)
-    uint32_t dz_out[OUT / 16][4];
-#pragma unroll
-    for (int kk = 0; kk < OUT / 16; kk++) {
-      const float *d0 = my_dy + g * OUT + kk * 16 + 2 * t, *d1 = d0 + 8 * OUT;
-      dz_out[kk][0] = pack2_sat(d0[0], d0[1]);
-      dz_out[kk][1] = pack2_sat(d1[0], d1[1]);
-      dz_out[kk][2] = pack2_sat(d0[8], d0[9]);
-      dz_out[kk][3] = pack2_sat(d1[8], d1[9]);
-    }
-    store_frag_t<OUT>(dz_out, dZt + dz_off[NH], rows, r0);
-    // dH_NH = dZ_out * W_out, then through the hidden layers
-    layer_mma<OUT, HID>(dz_out, swt + smem_wt_offset(n, NH), acc);
-    uint32_t dz[HID / 16][4];
-#pragma unroll
-    for (int l = NH - 1; l >= 0; l--) {
-      // mask with H_{l+1} > 0 (the ReLU output of layer l)
-      const uint32_t m = mask[l];
-#pragma unroll
-      for (int kk = 0; kk < HID / 16; kk++) {
-        const int b = kk * 8;
-        dz[kk][0] = pack2_sat((m >> (b + 0)) & 1 ? acc[2 * kk][0] : 0.f, (m >> (b + 1)) & 1 ? acc[2 * kk][1] : 0.f);
-        dz[kk][1] = pack2_sat((m >> (b + 2)) & 1 ? acc[2 * kk][2] : 0.f, (m >> (b + 3)) & 1 ? acc[2 * kk][3] : 0.f);
-        dz[kk][2] = pack2_sat((m >> (b + 4)) & 1 ? acc[2 * kk + 1][0] : 0.f,
-                              (m >> (b + 5)) & 1 ? acc[2 * kk + 1][1] : 0.f);
-        dz[kk][3] = pack2_sat((m >> (b + 6)) & 1 ? acc[2 * kk + 1][2] : 0.f,
-                              (m >> (b + 7)) & 1 ? acc[2 * kk + 1][3] : 0.f);
-      }
-      store_frag_t<HID>(dz, dZt + dz_off[l], rows, r0);
-      if (l > 0) layer_mma<HID, HID>(dz, swt + smem_wt_offset(n, l), acc);
-    }
+  } else if (t == 0) {
+    atomicExch(err, 1);
   }
   if (loss_sum) {
-    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    for (int k = 16; k > 0; k >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, k);
     if (lane == 0) atomicAdd(loss_sum, lsum);
   }
-}
-
-// ldmatrix: four 8x8 b16 matrices from shared memory (lane l gives the
-// address of row l & 7 of matrix l >> 3).
-__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const __half *p) {
-  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-               : "r"(a));
-}
-
-// dW_l[o][i] += sum over rows r of dZt_l[o][r] * Ht_l[i][r].  One block per
-// (layer, chunk of WG_ROWS rows): the chunk of Ht_l (all inputs) and of dZt_l
-// (all outputs) is staged in shared memory with 16-byte loads (each read once
-// per block), then warp w forms output rows 16w..16w+15 with ldmatrix-fed
-// m16n8k16 MMAs and adds its tile to the f32 gradient.
-constexpr int WG_ROWS = 256, WG_LD = WG_ROWS + 8;  // shared row stride (halves): conflict-free ldmatrix
-
-__host__ __device__ inline size_t wgrad_smem(int max_in, int max_out) {
-  return (size_t)(max_in + max_out) * WG_LD * sizeof(__half);
-}
-
-template <int IN, int NH, int OUT>
-__global__ void __launch_bounds__(128) k_mlp_wgrad(Net n, const __half *__restrict__ Ht,
-                                                   const __half *__restrict__ dZt, int rows) {
-  extern __shared__ __half wsm[];
-  const int n_chunks = (rows + WG_ROWS - 1) / WG_ROWS;
-  const int layer = blockIdx.x / n_chunks, ck = blockIdx.x - layer * n_chunks;
-  if (layer > NH) return;
-  const int K = layer == 0 ? IN : HID;   // layer inputs
-  const int N = layer == NH ? OUT : HID;  // layer outputs
-  size_t ht_off = 0, dz_off = 0;
-  for (int l = 0; l < layer; l++) {
-    ht_off += (size_t)(l == 0 ? IN : HID) * rows;
-    dz_off += (size_t)(l == NH ? OUT : HID) * rows;
-  }
-  const int r0 = ck * WG_ROWS, nr = min(WG_ROWS, rows - r0);  // nr: a multiple of 16
-  __half *sH = wsm, *sZ = wsm + (size_t)K * WG_LD;
-  // stage: row q of (Ht | dZt) holds chunk rows r0 .. r0+nr of input (output)
-  // q, as asynchronous 16-byte global-to-shared copies (every row start is
-  // 16-byte aligned: rows, r0 and the row stride are multiples of 8 halves),
-  // so a thread keeps all its copies in flight instead of a load-store chain
-  const int vec = nr / 8;  // 16-byte pieces per row
-  for (int idx = threadIdx.x; idx < (K + N) * vec; idx += blockDim.x) {
-    const int q = idx / vec, v = idx - q * vec;
-    const __half *src = q < K ? Ht + ht_off + (size_t)q * rows + r0 + v * 8
-                              : dZt + dz_off + (size_t)(q - K) * rows + r0 + v * 8;
-    __half *dst = (q < K ? sH + (size_t)q * WG_LD : sZ + (size_t)(q - K) * WG_LD) + v * 8;
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
-  }
-  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+  fence_before();
   __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  if (warp * 16 >= N) return;
-  const int o0 = warp * 16;
-  float acc[MAX_IN / 8][4];
+  if (warp == 0) tmem_free(tm, T::TMEM_COLS);
+}
+
+// gradient += the CTAs' partial sums (parts x count, CTA-major; count a
+// multiple of 4).  Thread (x, y) sums parts [16 y, 16 y + 16) of four
+// consecutive parameters with independent 16-byte loads, all in flight, and
+// adds the four sums with one vector atomic.
+constexpr int REDUCE_PARTS = 16;
+__global__ void k_grad_reduce(const float4 *__restrict__ partial, int parts, int count4, float4 *__restrict__ grad) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c0 = blockIdx.y * REDUCE_PARTS;
+  if (q >= count4) return;
+  float4 v[REDUCE_PARTS];
 #pragma unroll
-  for (int j = 0; j < MAX_IN / 8; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-  for (int k0 = 0; k0 < nr; k0 += 16) {
-    uint32_t a[4];  // dZ^T tile: rows o0.., columns (chunk rows) k0..
-    ldsm_x4(a, sZ + (size_t)(o0 + (lane & 7) + ((lane >> 3) & 1) * 8) * WG_LD + k0 + (lane >> 4) * 8);
+  for (int k = 0; k < REDUCE_PARTS; k++)
+    v[k] = c0 + k < parts ? __ldcs(partial + (size_t)(c0 + k) * count4 + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-    for (int j = 0; j < MAX_IN / 8; j += 2) {
-      if (j < K / 8) {  // B fragments of input tiles j, j+1 (rows i of Ht, columns k0..)
-        uint32_t b[4];
-        ldsm_x4(b, sH + (size_t)(j * 8 + (lane & 7) + (lane >> 4) * 8) * WG_LD + k0 + ((lane >> 3) & 1) * 8);
-        mma16816(acc[j], a[0], a[1], a[2], a[3], b[0], b[1]);
-        mma16816(acc[j + 1], a[0], a[1], a[2], a[3], b[2], b[3]);
-      }
-    }
+  for (int k = 0; k < REDUCE_PARTS; k++) {
+    s.x += v[k].x;
+    s.y += v[k].y;
+    s.z += v[k].z;
+    s.w += v[k].w;
   }
-  float *G = n.grad + layer_offset(n, layer);
-#pragma unroll
-  for (int j = 0; j < MAX_IN / 8; j++) {
-    if (j < K / 8) {
-      const int oo = o0 + g, i0 = j * 8 + 2 * t;
-      atomicAdd(G + (size_t)oo * K + i0, acc[j][0]);
-      atomicAdd(G + (size_t)oo * K + i0 + 1, acc[j][1]);
-      atomicAdd(G + (size_t)(oo + 8) * K + i0, acc[j][2]);
-      atomicAdd(G + (size_t)(oo + 8) * K + i0 + 1, acc[j][3]);
-    }
-  }
+  atomicAdd(grad + q, s);
 }
 
 // Adam (Kingma & Ba, ICLR 2015) on the f32 master weights; the gradient is
@@ -652,9 +718,10 @@ struct tpt_mlp {
   int params = 0;
   float *w32 = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
   __half *w16 = nullptr;
-  __half *ht = nullptr, *dzt = nullptr;
+  float *partial = nullptr;  // per-CTA weight-gradient sums of the training kernel [parts][params]
+  int parts = 0;             // CTAs the partial buffer holds (the SM count)
   float *loss = nullptr;
-  int ws_rows = 0;
+  int *err = nullptr;        // set by the training kernel when an MMA completion wait timed out
   int steps = 0;
 };
 
@@ -677,10 +744,6 @@ bool supported(int in, int nh, int out) {
   return (in == 112 && nh == 3 && out == 48) || (in == 64 && nh == 5 && out == 16) || (in == 32 && nh == 2 && out == 16);
 }
 
-size_t train_smem(const Net &n) {
-  return (size_t)(smem_w_halves(n) + smem_wt_halves(n)) * 2 + (size_t)2 * WARPS * 16 * n.out_dim * 4;
-}
-
 template <int IN, int NH, int OUT>
 tpt_status launch_forward(tpt_mlp *M, const __half *x, int rows, float *y, cudaStream_t s) {
   const size_t smem = (size_t)smem_w_halves(M->net) * 2;
@@ -695,38 +758,46 @@ tpt_status launch_forward(tpt_mlp *M, const __half *x, int rows, float *y, cudaS
   return mlp_cuda(cudaGetLastError());
 }
 
+// The workspace of the training kernel: one slice of weight-gradient sums
+// per CTA, at most one CTA per SM.
+tpt_status ensure_ws(tpt_mlp *M, int rows) {
+  (void)rows;
+  if (M->partial) return TPT_OK;
+  int sms = 0;
+  MLP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, M->device));
+  MLP_CUDA(cudaMalloc(&M->partial, (size_t)sms * M->params * sizeof(float)));
+  M->parts = sms;
+  return TPT_OK;
+}
+
 template <int IN, int NH, int OUT, class Loss>
 tpt_status launch_train(tpt_mlp *M, const __half *x, int rows, const Loss &loss, cudaStream_t s) {
-  const size_t smem = train_smem(M->net);
-  MLP_CUDA(cudaFuncSetAttribute(k_mlp_train<IN, NH, OUT, Loss>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem));
-  int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, M->device);
-  const int tiles = rows / 16;
-  int grid = (tiles + WARPS - 1) / WARPS;
-  if (grid > sms * 2) grid = sms * 2;
-  if (grid < 1) grid = 1;
+  using L = TrainLayout<IN, NH, OUT>;
+  tpt_status st = ensure_ws(M, rows);
+  if (st != TPT_OK) return st;
+  MLP_CUDA(cudaFuncSetAttribute(k_mlp_train_tc<IN, NH, OUT, Loss>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)L::SMEM));
+  const int tiles = (rows + 127) / 128;
+  const int grid = tiles < M->parts ? tiles : M->parts;
   MLP_CUDA(cudaMemsetAsync(M->loss, 0, sizeof(float), s));
-  k_mlp_train<IN, NH, OUT, Loss><<<grid, WARPS * 32, smem, s>>>(M->net, x, rows, loss, M->ht, M->dzt, M->loss);
+  k_mlp_train_tc<IN, NH, OUT, Loss><<<grid, 128, L::SMEM, s>>>(M->net, x, rows, loss, M->partial, M->loss, M->err);
   MLP_CUDA(cudaGetLastError());
-  const int n_chunks = (rows + WG_ROWS - 1) / WG_ROWS;
-  const size_t wsm = wgrad_smem(IN > HID ? IN : HID, OUT > HID ? OUT : HID);
-  MLP_CUDA(cudaFuncSetAttribute(k_mlp_wgrad<IN, NH, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
-  k_mlp_wgrad<IN, NH, OUT><<<(NH + 1) * n_chunks, 128, wsm, s>>>(M->net, M->ht, M->dzt, rows);
+  const int count4 = M->params / 4;  // every supported shape has a multiple of 4 parameters
+  const dim3 rgrid((count4 + 127) / 128, (grid + REDUCE_PARTS - 1) / REDUCE_PARTS);
+  k_grad_reduce<<<rgrid, 128, 0, s>>>(reinterpret_cast<const float4 *>(M->partial), grid, count4,
+                                      reinterpret_cast<float4 *>(M->grad));
   return mlp_cuda(cudaGetLastError());
 }
 
-tpt_status ensure_ws(tpt_mlp *M, int rows) {
-  if (rows <= M->ws_rows) return TPT_OK;
-  if (M->ht) cudaFree(M->ht);
-  if (M->dzt) cudaFree(M->dzt);
-  M->ht = M->dzt = nullptr;
-  const size_t hh = (size_t)(M->in_dim + M->n_hidden * HID) * rows;
-  const size_t dd = (size_t)(M->n_hidden * HID + M->out_dim) * rows;
-  MLP_CUDA(cudaMalloc(&M->ht, hh * sizeof(__half)));
-  MLP_CUDA(cudaMalloc(&M->dzt, dd * sizeof(__half)));
-  M->ws_rows = rows;
-  return TPT_OK;
+// An MMA completion the training kernel waited for in vain: reported once.
+tpt_status check_train_err(tpt_mlp *M, cudaStream_t s) {
+  int e = 0;
+  MLP_CUDA(cudaMemcpyAsync(&e, M->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MLP_CUDA(cudaStreamSynchronize(s));
+  if (!e) return TPT_OK;
+  MLP_CUDA(cudaMemsetAsync(M->err, 0, sizeof(int), s));
+  std::snprintf(g_mlp_err, sizeof(g_mlp_err), "tensor-core training kernel: an MMA completion wait timed out");
+  return TPT_ERR_CUDA;
 }
 
 }  // namespace
@@ -806,7 +877,7 @@ tpt_status guide_train(GuideNet *G, const float4 *rec, int count, int steps, int
   MLP_CUDA(cudaMemcpyAsync(&l, G->net->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
   MLP_CUDA(cudaStreamSynchronize(s));
   G->last_loss = l;  // weighted mean NLL of the last batch
-  return TPT_OK;
+  return check_train_err(G->net, s);
 }
 
 // Evaluates the network at every (cell, normal bin) of a res^3 grid and
@@ -892,7 +963,7 @@ tpt_status cache_train(CacheNet *G, const float4 *rec, int count, int steps, int
   MLP_CUDA(cudaMemcpyAsync(&l, G->net->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
   MLP_CUDA(cudaStreamSynchronize(s));
   G->last_loss = l / (float)batch;
-  return TPT_OK;
+  return check_train_err(G->net, s);
 }
 
 // Evaluates the cache for `count` queries (6 float4 each: the 4 feature
@@ -964,6 +1035,8 @@ tpt_status tpt_mlp_create(int32_t device, int32_t in_dim, int32_t n_hidden, int3
   if (e == cudaSuccess) e = cudaMalloc(&M->v, P * 4);
   if (e == cudaSuccess) e = cudaMalloc(&M->w16, P * 2);
   if (e == cudaSuccess) e = cudaMalloc(&M->loss, 4);
+  if (e == cudaSuccess) e = cudaMalloc(&M->err, 4);
+  if (e == cudaSuccess) e = cudaMemset(M->err, 0, 4);
   if (e != cudaSuccess) {
     tpt_mlp_destroy(M);
     return mlp_cuda(e);
@@ -992,7 +1065,7 @@ tpt_status tpt_mlp_create(int32_t device, int32_t in_dim, int32_t n_hidden, int3
 void tpt_mlp_destroy(tpt_mlp *M) {
   if (!M) return;
   cudaSetDevice(M->device);
-  void *ptrs[] = {M->w32, M->grad, M->m, M->v, M->w16, M->ht, M->dzt, M->loss};
+  void *ptrs[] = {M->w32, M->grad, M->m, M->v, M->w16, M->partial, M->loss, M->err};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete M;
@@ -1026,7 +1099,7 @@ tpt_status tpt_mlp_get_grad(const tpt_mlp *M, float *host) {
   if (!M || !host) return TPT_ERR_INVALID_ARGUMENT;
   MLP_CUDA(cudaSetDevice(M->device));
   MLP_CUDA(cudaMemcpy(host, M->grad, (size_t)M->params * 4, cudaMemcpyDeviceToHost));
-  return TPT_OK;
+  return check_train_err(const_cast<tpt_mlp *>(M), nullptr);
 }
 
 tpt_status tpt_mlp_forward(tpt_mlp *M, const void *x_f16, int64_t rows, float *y, void *stream) {
@@ -1067,6 +1140,7 @@ tpt_status tpt_mlp_backward_vmf(tpt_mlp *M, const void *x_f16, const float *targ
   if (loss_out) {
     MLP_CUDA(cudaMemcpyAsync(loss_out, M->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
     MLP_CUDA(cudaStreamSynchronize(s));
+    return check_train_err(M, s);
   }
   return TPT_OK;
 }
@@ -1085,6 +1159,7 @@ tpt_status tpt_mlp_backward_rel_l2(tpt_mlp *M, const void *x_f16, const float *t
   if (loss_out) {
     MLP_CUDA(cudaMemcpyAsync(loss_out, M->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
     MLP_CUDA(cudaStreamSynchronize(s));
+    return check_train_err(M, s);
   }
   return TPT_OK;
 }
