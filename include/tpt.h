@@ -353,6 +353,16 @@ tpt_status tpt_mlp_backward_vmf(tpt_mlp *m, const void *x_f16, const float *targ
  * NULL) receives the unscaled loss sum. */
 tpt_status tpt_mlp_backward_rel_l2(tpt_mlp *m, const void *x_f16, const float *target, int64_t rows, float scale,
                                    float *loss_out, void *stream);
+/* The radiance cache's training step as the cached renderer runs it: row r
+ * of the `rows`-row batch is record h(r) mod count of `records` (device, 5
+ * float4 per record: the four feature float4 of tpt_nrc_encode, then the
+ * target radiance), h the 32-bit mix of r, `step` and `key` the renderer
+ * uses; the rows are encoded inside the training kernel (no input matrix in
+ * memory) and the gradient of the relative L2 loss is accumulated as
+ * tpt_mlp_backward_rel_l2 would for the same rows. */
+tpt_status tpt_mlp_backward_rel_l2_records(tpt_mlp *m, const float *records, int64_t count, uint32_t key,
+                                           uint32_t step, const float *lo, const float *extent, int64_t rows,
+                                           float scale, float *loss_out, void *stream);
 /* The learned parts' input encodings, one row per record (device buffers).
  * tpt_guide_encode: records of 3 float4 (position, weight), (normal, -),
  * (sampled direction, -) -> f16 rows of 112: the position normalised to the

@@ -206,3 +206,50 @@ def test_rel_l2_loss_gradient_matches_reference(built):
         err = np.abs(a - b).max() / np.abs(b).max()
         print("rel_l2 layer", (o, i), err)
         assert err < GRAD_RTOL, (o, i, err)
+
+
+def _record_index(rows, count, key, step):
+    """The cache's row sampler (learn.cu nrc_record_index), in uint32 arithmetic."""
+    r = np.arange(rows, dtype=np.uint64)
+    m = np.uint64(0xFFFFFFFF)
+    h = ((r * np.uint64(0x9E3779B1)) & m) ^ np.uint64((step * 0x85EBCA77) & 0xFFFFFFFF) ^ np.uint64(key)
+    h ^= h >> np.uint64(15)
+    h = (h * np.uint64(0x2C1B3C6D)) & m
+    h ^= h >> np.uint64(12)
+    h = (h * np.uint64(0x297A2D39)) & m
+    h ^= h >> np.uint64(15)
+    return (h % np.uint64(count)).astype(np.int64)
+
+
+def test_cache_training_from_records_matches_the_encoded_batch(built):
+    """The cached renderer's training step, which samples and encodes its rows
+    inside the tensor-core training kernel (tpt_mlp_backward_rel_l2_records),
+    gives the gradient and loss of the same rows encoded first
+    (tpt_nrc_encode) and trained through tpt_mlp_backward_rel_l2, and both
+    match the float64 reference."""
+    import torch
+
+    rows, count, key, step = 4000, 2500, 0x1234567, 7
+    rec = _records(count, 6, 5)
+    idx = _record_index(rows, count, key, step)
+    sampled = rec[idx]
+    target = sampled[:, 4].copy()
+    target[~np.isfinite(target).all(axis=1)] = 0
+    x = tpt.nrc_encode(sampled, LO, EXT)
+    a = tpt.Mlp(64, 5, 16, seed=21)
+    b = tpt.Mlp(64, 5, 16, seed=21)
+    dr = torch.from_numpy(np.ascontiguousarray(rec)).cuda()
+    xd = torch.from_numpy(x).cuda()
+    td = torch.from_numpy(np.ascontiguousarray(target)).cuda()
+    torch.cuda.synchronize()
+    scale = 1024.0 / rows
+    la = a.backward_rel_l2_records(dr.data_ptr(), count, key, step, LO, EXT, rows, scale)
+    lb = b.backward_rel_l2(xd.data_ptr(), td.data_ptr(), rows, scale)
+    ga, gb = a.get_grad(), b.get_grad()
+    assert abs(la - lb) <= 1e-6 * abs(lb)
+    np.testing.assert_allclose(ga, gb, rtol=1e-5, atol=1e-6 * np.abs(gb).max())
+    p16 = a.get_params().astype(np.float16).astype(np.float32)
+    y, acts = mlp_ref.forward(p16, x.astype(np.float64), 64, 5, 16)
+    gr = mlp_ref.backward(p16, acts, mlp_ref.rel_l2_grad(y, target.astype(np.float64), 16).astype(np.float32)
+                          .astype(np.float64), 64, 5, 16)
+    assert np.abs(ga / scale - gr).max() < GRAD_RTOL * np.abs(gr).max()

@@ -4,10 +4,10 @@
 // Training step of a batch of `rows` samples (rows a multiple of 16):
 //   k_mlp_train_tc  forward, per-row loss gradient dY, backward and the weight
 //                   gradients of 128-row tiles, fused, on tcgen05 with tensor-
-//                   memory accumulators (one CTA per SM, weight-gradient sums
-//                   per CTA);
-//   k_grad_reduce   adds the CTAs' sums into the f32 gradient;
-//   k_adam          Adam on f32 master weights, refreshing the f16 copy.
+//                   memory accumulators (at most one CTA per SM; each adds its
+//                   weight-gradient sums to the f32 gradient);
+//   k_adam          Adam on f32 master weights, refreshing the f16 copy and
+//                   the training kernel's swizzled weight image.
 // Inference (k_mlp_forward) keeps register-resident mma.sync chains: 16 rows
 // per warp, no tensor-memory round trip between layers.
 // Shapes are template parameters: <IN, NH, OUT> with hidden width 64.
@@ -32,11 +32,16 @@ namespace mlp {
 // ------------------------------------------------------------ losses ----
 // Each loss writes dL/dy for one row (already multiplied by `scale`, the
 // loss scale over the batch size) and returns the row's loss.
+// Every loss also has preload(row): the row's loss inputs, read when the
+// tile starts so their latency overlaps the forward pass (passed to grad).
 struct LossGiven {  // dY supplied by the caller (tests)
   const float *dy;
   float scale;
+  static constexpr bool kEncodes = false;
+  using Pre = int;
+  __device__ Pre preload(int) const { return 0; }
   template <int OUT>
-  __device__ float grad(int row, const float *y, float *dy_out) const {
+  __device__ float grad(int row, const float *y, float *dy_out, Pre) const {
     for (int o = 0; o < OUT; o++) dy_out[o] = dy[(size_t)row * OUT + o] * scale;
     return 0.f;
   }
@@ -84,18 +89,23 @@ __global__ void __launch_bounds__(WARPS * 32) k_mlp_forward(Net n, const __half 
 //   forward   Z_l = H_l W_l^T  (tcgen05.mma, M = 128, f32 in tensor memory);
 //             ReLU and f16 rounding in registers, H_{l+1} back to shared memory
 //   loss      dY of the tile's rows from the f32 outputs (one row per thread)
-//   backward  dW_l += dZ_l^T H_l (M = 64: the layer's outputs, zero-padded;
-//             N = its inputs; K = the tile's rows), accumulated over all of the
-//             CTA's tiles in tensor memory; dH_l = dZ_l W_l (M = 128), masked
-//             by H_l > 0 into dZ_{l-1}.
+//   backward  dH_l = dZ_l W_l (M = 128), masked by H_l > 0 into dZ_{l-1};
+//             dW_l += dZ_l^T H_l (M = 64: the layer's outputs, zero-padded;
+//             N = its inputs; K = the tile's rows), accumulated over all of
+//             the CTA's tiles in tensor memory.
 // The MMAs read the swizzled shared-memory tiles of tc05.cuh: the forward
 // tiles (X, H_l, W_l) serve K-major in the forward pass and, through MN-major
 // descriptors, as the transposed operands of the backward pass and of the
 // weight gradients, so nothing is transposed or written to HBM between the
-// passes.  One thread issues the MMAs and commits them to an mbarrier; the
-// warpgroup waits on it (with a time limit) and reads the accumulators with
-// tcgen05.ld.  At the end each CTA writes its dW sums to its slice of
-// `partial`, which k_grad_reduce adds into the gradient.
+// passes.  A fifth warp issues the MMAs (one thread); completions arrive on
+// mbarriers the four rows warps wait on (with a time limit).  The weight-
+// gradient MMAs of layer l + 1 are issued after dH_l, so they run off the
+// critical path while the rows warps form dZ_{l-1}; dZ_l rotates through
+// three shared-memory tiles (l mod 3) so that neither pass overwrites a tile
+// an MMA in flight still reads.  The weights arrive by one bulk copy of the
+// network's pre-swizzled weight image (written by the Adam step); at the end
+// each CTA stages its dW sums in shared memory and adds them to the gradient
+// with coalesced vector reductions.
 template <int IN, int NH, int OUT>
 struct TrainLayout {
   static_assert(IN % 16 == 0 && IN <= 128 && OUT % 16 == 0 && OUT <= 64 && NH >= 1, "supported shapes");
@@ -107,10 +117,11 @@ struct TrainLayout {
     for (int j = 0; j < l; j++) o += (uint32_t)((in_(j) + 63) / 64) * out_(j) * 128;
     return o;
   }
-  static constexpr uint32_t X_OFF = w_off(NH + 1);
+  static constexpr uint32_t W_BYTES = w_off(NH + 1);  // the weight image
+  static constexpr uint32_t X_OFF = W_BYTES;
   static constexpr uint32_t H_OFF = X_OFF + KB0 * 16384;  // H_1 .. H_NH
-  static constexpr uint32_t DZ_OFF = H_OFF + NH * 16384;
-  static constexpr uint32_t BAR_OFF = DZ_OFF + 16384;
+  static constexpr uint32_t DZ_OFF = H_OFF + NH * 16384;  // three rotating dZ tiles: dZ_l in tile l % 3
+  static constexpr uint32_t BAR_OFF = DZ_OFF + 3 * 16384;
   static constexpr uint32_t SMEM = BAR_OFF + 64 + 1024;  // + slack for the 1024-byte alignment
   __host__ __device__ static constexpr int dw_col(int l) {  // tensor-memory column of layer l's weight gradient
     int c = 64;                         // columns 0..63: the forward / backward accumulator
@@ -118,184 +129,260 @@ struct TrainLayout {
     return c;
   }
   static constexpr uint32_t TMEM_COLS = 512;
-  static_assert(X_OFF % 1024 == 0, "operand tiles start on 1024-byte boundaries");
+  static_assert(X_OFF % 1024 == 0 && W_BYTES % 16 == 0, "operand tiles start on 1024-byte boundaries");
   static_assert(dw_col(NH + 1) <= (int)TMEM_COLS, "tensor memory");
   static_assert(SMEM <= 227 * 1024, "shared memory");
 };
 
+// Byte offset of weight p (layer-major, [out][in] per layer) in the weight
+// image: layer l's tile at TrainLayout::w_off(l), its 64-input blocks of
+// out rows one after the other, each row 128-byte swizzled.
+__host__ __device__ inline uint32_t wimg_offset(const Net &n, int p) {
+  int l = 0, off = 0;
+  uint32_t img = 0;
+  for (;;) {
+    const int K = layer_in(n, l), N = layer_out(n, l);
+    if (p < off + N * K || l == n_layers(n) - 1) break;
+    off += N * K;
+    img += (uint32_t)((K + 63) / 64) * N * 128;
+    l++;
+  }
+  const int K = layer_in(n, l), N = layer_out(n, l), q = p - off, o = q / K, i = q - o * K;
+  return img + (uint32_t)(i / 64) * N * 128 + tc05::sw128(o, i % 64);
+}
+__host__ __device__ inline uint32_t wimg_bytes(const Net &n) {
+  uint32_t img = 0;
+  for (int l = 0; l < n_layers(n); l++) img += (uint32_t)((layer_in(n, l) + 63) / 64) * layer_out(n, l) * 128;
+  return img;
+}
+
 // ~2 s at 2 GHz: an MMA completion that has not arrived by then never will
 constexpr long long TC_WAIT_LIMIT = 4000000000LL;
 
+// Position of float4 i4 of row o in the staged weight-gradient sums: XOR
+// swizzled by o mod 8 within each full group of 8 float4, so the 16 rows a
+// warp stores at once fall into different banks.
+__device__ __forceinline__ int stage_slot(int o, int i4, int k4) {
+  return i4 < (k4 & ~7) ? (i4 ^ (o & 7)) : i4;
+}
+
+constexpr int TC_THREADS = 160;  // warps 0-3: rows / tensor-memory lanes; warp 4: issues the MMAs
+
 template <int IN, int NH, int OUT, class Loss>
-__global__ void __launch_bounds__(128, 1)
-    k_mlp_train_tc(Net n, const __half *__restrict__ X, int rows, Loss loss, float *__restrict__ partial,
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_mlp_train_tc(Net n, const uint8_t *__restrict__ wimg, const __half *__restrict__ X, int rows, Loss loss,
                    float *loss_sum, int *err) {
   using T = TrainLayout<IN, NH, OUT>;
   using namespace tc05;
+  static_assert(T::BAR_OFF - T::H_OFF >= (uint32_t)((IN * HID + (NH - 1) * HID * HID + HID * OUT) * 4),
+                "the weight-gradient sums are staged where H and dZ lived");
   extern __shared__ uint8_t tc_raw[];
   uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~uintptr_t(1023));
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + T::BAR_OFF + 8);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + T::BAR_OFF + 32);
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const int n_params = param_count(n);
+  const bool rows_warp = warp < 4;           // epilogue: thread t owns row t and lane t
+  const bool issuer = warp == 4 && lane == 0;  // the one thread that issues MMAs
+  const uint32_t base = smem_addr(sm);
+  // barA: forward and dH MMAs; barW[p]: the weight-gradient MMAs of the
+  // layers l with l & 1 == p (each has at most one phase outstanding when it
+  // is waited on); barL: the weight image
+  const uint32_t barA = base + T::BAR_OFF, barW0 = barA + 8, barL = barA + 24;
+  uint32_t phA = 0, phW0 = 0, phW1 = 0;
+  bool ok = true;
 
-  // weights: asynchronous 16-byte copies, all in flight at once.  Padding
-  // columns of the tiles (past IN) are never read: the forward MMAs stop at
-  // K = IN and the weight-gradient MMAs at N = IN.
-#pragma unroll 1
-  for (int l = 0; l <= NH; l++) {
-    const int K = T::in_(l), N = T::out_(l);
-    const __half *g = n.w16 + layer_offset(n, l);
-    for (int c = t; c < N * K / 8; c += 128) {
-      const int o = (c * 8) / K, i = c * 8 - o * K;
-      cp_async16(sm + T::w_off(l) + (uint32_t)(i / 64) * N * 128 + sw128_chunk(o, (i % 64) / 8), g + c * 8, 16);
-    }
+  // the weight image: one bulk copy (in 16 KB pieces) completing on barL.
+  // Padding columns of the tiles (past IN) are never read: the forward MMAs
+  // stop at K = IN and the weight-gradient MMAs at N = IN.
+  if (issuer) {
+    bar_init(barA, 1);
+    bar_init(barW0, 1);
+    bar_init(barW0 + 8, 1);
+    bar_init(barL, 1);
+    bar_expect_bytes(barL, T::W_BYTES);
+    for (uint32_t o = 0; o < T::W_BYTES; o += 16384)
+      bulk_copy(base + o, wimg + o, T::W_BYTES - o < 16384 ? T::W_BYTES - o : 16384, barL);
   }
-  cp_async_wait_all();
-  const uint32_t base = smem_addr(sm), bar = base + T::BAR_OFF;
-  if (t == 0) bar_init(bar, 1);
   if (warp == 0) tmem_alloc(tslot, T::TMEM_COLS);
-  fence_async_smem();
   fence_before();
   __syncthreads();
   fence_after();
   const uint32_t tm = *tslot;
-  const uint32_t lane_base = tm + ((uint32_t)(warp * 32) << 16);
-  uint32_t phase = 0;
-  bool ok = true, first = true;
+  const uint32_t lane_base = tm + ((uint32_t)((warp & 3) * 32) << 16);
+  bool weights = false;  // the issuer has seen the weight image arrive
+  // descriptors of the tiles' first bytes; a K step adds an offset
+  const uint64_t dX = desc(base + T::X_OFF, 16, 1024), dXmn = desc(base + T::X_OFF, 16384, 1024);
+  const uint64_t dW = desc(base, 16, 1024), dWmn = desc(base, 16384, 1024);
+  const uint64_t dH = desc(base + T::H_OFF, 16, 1024), dHmn = desc(base + T::H_OFF, 16384, 1024);
+  const uint64_t dZ = desc(base + T::DZ_OFF, 16, 1024), dZmn = desc(base + T::DZ_OFF, 16384, 1024);
   float lsum = 0.f;
+  bool first = true;
   const int n_tiles = (rows + 127) / 128;
+  // a rows warp waits for an MMA completion; the whole warp agrees on the
+  // outcome (its tensor-memory loads are warp-collective)
+  auto wait_rows = [&](uint32_t bar, uint32_t &ph) {
+    const bool got = __all_sync(0xffffffffu, bar_wait(bar, ph, TC_WAIT_LIMIT));
+    ph ^= 1;
+    ok = ok && got;
+    return got;
+  };
 
-  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+  for (int tile = blockIdx.x; ok && tile < n_tiles; tile += gridDim.x) {
     const int r0 = tile * 128;
-    // ---- the input tile (rows past the batch are zero)
-    constexpr int CH = IN / 8;
-    for (int c = t; c < 128 * CH; c += 128) {
-      const int r = c / CH, k8 = c - r * CH;
-      const bool in = r0 + r < rows;  // rows past the batch: zero-filled copies
-      cp_async16(sm + T::X_OFF + (uint32_t)(k8 / 8) * 16384 + sw128_chunk(r, k8 % 8),
-                 X + (size_t)(in ? r0 + r : 0) * IN + k8 * 8, in ? 16 : 0);
+    typename Loss::Pre pre{};
+    if (rows_warp) {
+      if constexpr (Loss::kEncodes) {  // the loss builds its input row t itself (row past the batch: zeros)
+        pre = loss.encode(r0 + t, r0 + t < rows, sm + T::X_OFF, t);
+      } else {
+        if (r0 + t < rows) pre = loss.preload(r0 + t);
+        // ---- the input tile (rows past the batch are zero-filled)
+        constexpr int CH = IN / 8;
+        for (int c = t; c < 128 * CH; c += 128) {
+          const int r = c / CH, k8 = c - r * CH;
+          const bool in = r0 + r < rows;
+          cp_async16(sm + T::X_OFF + (uint32_t)(k8 / 8) * 16384 + sw128_chunk(r, k8 % 8),
+                     X + (size_t)(in ? r0 + r : 0) * IN + k8 * 8, in ? 16 : 0);
+        }
+        cp_async_wait_all();
+      }
+      fence_async_smem();
     }
-    cp_async_wait_all();
-    fence_async_smem();
-    __syncthreads();
-    // ---- forward (loops rolled: each CTA runs its code for a tile or two,
+    if (issuer && !weights) weights = ok = bar_wait(barL, 0, TC_WAIT_LIMIT);  // overlapped with the first tile's copies
+    if (!__syncthreads_and(ok)) break;
+    // ---- forward (loops rolled: each CTA runs its body for a tile or two,
     // so a compact body keeps instruction fetch off the critical path)
 #pragma unroll 1
     for (int l = 0; l <= NH; l++) {
-      if (t == 0) {
+      if (issuer) {
         fence_after();
-        const uint32_t a0 = base + (l == 0 ? T::X_OFF : T::H_OFF + (uint32_t)(l - 1) * 16384);
-        const uint32_t b0 = base + T::w_off(l);
-        constexpr uint32_t sbo = 1024;
+        const uint64_t a0 = l == 0 ? dX : desc_add(dH, (uint32_t)(l - 1) * 16384);
+        const uint64_t b0 = desc_add(dW, T::w_off(l));
         const uint32_t id = idesc_f16(128, T::out_(l), false, false);
+        const uint32_t bstride = T::out_(l) * 128;  // between the weight tile's 64-input blocks
 #pragma unroll 1
         for (int s = 0; s < T::in_(l) / 16; s++)
-          mma_f16(tm, desc(a0 + (uint32_t)(s / 4) * 16384 + (uint32_t)(s % 4) * 32, 16, sbo),
-                  desc(b0 + (uint32_t)(s / 4) * T::out_(l) * 128 + (uint32_t)(s % 4) * 32, 16, sbo), id, s > 0);
-        commit(bar);
+          mma_f16(tm, desc_add(a0, (uint32_t)(s >> 2) * 16384 + (uint32_t)(s & 3) * 32),
+                  desc_add(b0, (uint32_t)(s >> 2) * bstride + (uint32_t)(s & 3) * 32), id, s > 0);
+        commit(barA);
       }
-      const bool got = bar_wait(bar, phase, TC_WAIT_LIMIT);
-      phase ^= 1;
-      if (!__syncthreads_and(got)) {
-        ok = false;
-        break;
-      }
-      fence_after();
-      float v[64];
-      tmem_ld64(lane_base, v);
-      uint8_t *dst = l < NH ? sm + T::H_OFF + (uint32_t)l * 16384 : sm + T::DZ_OFF;
-      if (l < NH) {  // ReLU, f16: row t of H_{l+1}
-#pragma unroll
-        for (int c = 0; c < 8; c++) {
-          uint4 q;
-          q.x = pack2(fmaxf(v[8 * c], 0.f), fmaxf(v[8 * c + 1], 0.f));
-          q.y = pack2(fmaxf(v[8 * c + 2], 0.f), fmaxf(v[8 * c + 3], 0.f));
-          q.z = pack2(fmaxf(v[8 * c + 4], 0.f), fmaxf(v[8 * c + 5], 0.f));
-          q.w = pack2(fmaxf(v[8 * c + 6], 0.f), fmaxf(v[8 * c + 7], 0.f));
-          *reinterpret_cast<uint4 *>(dst + sw128_chunk(t, c)) = q;
-        }
-      } else {  // the loss of row t; dZ of the output layer (zero past OUT and past the batch)
-        float dy[OUT];
-        if (r0 + t < rows) {
-          lsum += loss.template grad<OUT>(r0 + t, v, dy);
-        } else {
-#pragma unroll
-          for (int o = 0; o < OUT; o++) dy[o] = 0.f;
-        }
-#pragma unroll
-        for (int c = 0; c < 8; c++) {
-          float e[8];
-#pragma unroll
-          for (int j = 0; j < 8; j++) e[j] = 8 * c + j < OUT ? dy[(8 * c + j) % OUT] : 0.f;
-          uint4 q;
-          q.x = pack2_sat(e[0], e[1]);
-          q.y = pack2_sat(e[2], e[3]);
-          q.z = pack2_sat(e[4], e[5]);
-          q.w = pack2_sat(e[6], e[7]);
-          *reinterpret_cast<uint4 *>(dst + sw128_chunk(t, c)) = q;
-        }
-      }
-      fence_async_smem();
-      fence_before();
-      __syncthreads();
-    }
-    if (!ok) break;
-    // ---- backward
-#pragma unroll 1
-    for (int l = NH; l >= 0; l--) {
-      if (t == 0) {
+      if (rows_warp && wait_rows(barA, phA)) {
         fence_after();
-        const uint32_t dz = base + T::DZ_OFF;
-        const uint32_t hb = base + (l == 0 ? T::X_OFF : T::H_OFF + (uint32_t)(l - 1) * 16384);
-        // dW_l (+)= dZ_l^T H_l: A = dZ (MN-major, 64 outputs), B = H_l (MN-major,
-        // blocks of 64 inputs 16384 bytes apart), K = 128 rows in steps of 16
-        const uint32_t idw = idesc_f16(64, T::in_(l), true, true);
-#pragma unroll 1
-        for (int s = 0; s < 8; s++)
-          mma_f16(tm + (uint32_t)T::dw_col(l), desc(dz + 2048u * s, 16384, 1024), desc(hb + 2048u * s, 16384, 1024),
-                  idw, !first || s > 0);
-        if (l > 0) {  // dH_l = dZ_l W_l: A = dZ (K-major over the outputs), B = W_l (MN-major)
-          const uint32_t idh = idesc_f16(128, HID, false, true);
-#pragma unroll 1
-          for (int s = 0; s < T::out_(l) / 16; s++)
-            mma_f16(tm, desc(dz + 32u * s, 16, 1024), desc(base + T::w_off(l) + 2048u * s, 16384, 1024), idh, s > 0);
-        }
-        commit(bar);
-      }
-      const bool got = bar_wait(bar, phase, TC_WAIT_LIMIT);
-      phase ^= 1;
-      if (!__syncthreads_and(got)) {
-        ok = false;
-        break;
-      }
-      fence_after();
-      if (l > 0) {  // dZ_{l-1} = dH_l masked by H_l > 0 (the MMAs reading dZ_l are complete)
         float v[64];
         tmem_ld64(lane_base, v);
-        const uint8_t *h = sm + T::H_OFF + (uint32_t)(l - 1) * 16384;
-        uint8_t *dz = sm + T::DZ_OFF;
+        if (l < NH) {  // ReLU, f16: row t of H_{l+1}
+          uint8_t *dst = sm + T::H_OFF + (uint32_t)l * 16384;
 #pragma unroll
-        for (int c = 0; c < 8; c++) {
-          const uint4 hv = *reinterpret_cast<const uint4 *>(h + sw128_chunk(t, c));
-          const uint32_t hw[4] = {hv.x, hv.y, hv.z, hv.w};
-          uint32_t q[4];
-#pragma unroll
-          for (int j = 0; j < 4; j++) {
-            const float2 hf = unpack2(hw[j]);
-            q[j] = pack2_sat(hf.x > 0.f ? v[8 * c + 2 * j] : 0.f, hf.y > 0.f ? v[8 * c + 2 * j + 1] : 0.f);
+          for (int c = 0; c < 8; c++) {
+            uint4 q;
+            q.x = pack2(fmaxf(v[8 * c], 0.f), fmaxf(v[8 * c + 1], 0.f));
+            q.y = pack2(fmaxf(v[8 * c + 2], 0.f), fmaxf(v[8 * c + 3], 0.f));
+            q.z = pack2(fmaxf(v[8 * c + 4], 0.f), fmaxf(v[8 * c + 5], 0.f));
+            q.w = pack2(fmaxf(v[8 * c + 6], 0.f), fmaxf(v[8 * c + 7], 0.f));
+            *reinterpret_cast<uint4 *>(dst + sw128_chunk(t, c)) = q;
           }
-          *reinterpret_cast<uint4 *>(dz + sw128_chunk(t, c)) = make_uint4(q[0], q[1], q[2], q[3]);
+        } else {  // the loss of row t; dZ of the output layer (zero past OUT and past the batch)
+          uint8_t *dst = sm + T::DZ_OFF + (uint32_t)(NH % 3) * 16384;
+          float dy[OUT];
+          if (r0 + t < rows) {
+            lsum += loss.template grad<OUT>(r0 + t, v, dy, pre);
+          } else {
+#pragma unroll
+            for (int o = 0; o < OUT; o++) dy[o] = 0.f;
+          }
+#pragma unroll
+          for (int c = 0; c < 8; c++) {
+            float e[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) e[j] = 8 * c + j < OUT ? dy[(8 * c + j) % OUT] : 0.f;
+            uint4 q;
+            q.x = pack2_sat(e[0], e[1]);
+            q.y = pack2_sat(e[2], e[3]);
+            q.z = pack2_sat(e[4], e[5]);
+            q.w = pack2_sat(e[6], e[7]);
+            *reinterpret_cast<uint4 *>(dst + sw128_chunk(t, c)) = q;
+          }
         }
         fence_async_smem();
+        fence_before();
       }
-      fence_before();
-      __syncthreads();
+      if (!__syncthreads_and(ok)) break;
     }
     if (!ok) break;
+    // ---- backward, step l = NH .. 0: the issuer launches dH_l (critical
+    // path) and then dW_{l+1}; the rows warps form dZ_{l-1} into tile
+    // (l - 1) % 3 once dH_l is done and dW_{l+2}, the last reader of that
+    // tile, has completed.  dW_j commits to barW[j & 1]; both of the last
+    // two (dW_1, dW_0) commit to barA at step 0.
+#pragma unroll 1
+    for (int l = NH; l >= 0; l--) {
+      if (issuer) {
+        fence_after();
+        if (l > 0) {  // dH_l = dZ_l W_l: A = dZ_l (K-major over the outputs), B = W_l (MN-major)
+          const uint32_t idh = idesc_f16(128, HID, false, true);
+          const uint64_t b0 = desc_add(dWmn, T::w_off(l));
+          const uint32_t zb = (uint32_t)(l % 3) * 16384;
+#pragma unroll 1
+          for (int s = 0; s < T::out_(l) / 16; s++)
+            mma_f16(tm, desc_add(dZ, zb + 32u * s), desc_add(b0, 2048u * s), idh, s > 0);
+          commit(barA);
+        }
+        // dW_j (+)= dZ_j^T H_j: A = dZ_j (MN-major, 64 outputs), B = H_j (MN-major,
+        // blocks of 64 inputs 16384 bytes apart), K = the 128 rows in steps of 16
+#pragma unroll 1
+        for (int j = l + 1; j >= (l == 0 ? 0 : l + 1); j--) {
+          if (j > NH) continue;
+          const uint32_t idw = idesc_f16(64, T::in_(j), true, true);
+          const uint64_t bh = j == 0 ? dXmn : desc_add(dHmn, (uint32_t)(j - 1) * 16384);
+          const uint32_t dcol = tm + (uint32_t)T::dw_col(j), zb = (uint32_t)(j % 3) * 16384;
+#pragma unroll 1
+          for (int s = 0; s < 8; s++)
+            mma_f16(dcol, desc_add(dZmn, zb + 2048u * s), desc_add(bh, 2048u * s), idw, !first || s > 0);
+          if (l > 0) commit(barW0 + 8u * (uint32_t)(j & 1));
+        }
+        if (l == 0) commit(barA);
+      }
+      if (l > 0 && rows_warp && wait_rows(barA, phA)) {  // dZ_{l-1} = dH_l masked by H_l > 0
+        fence_after();
+        float v[64];
+        tmem_ld64(lane_base, v);
+        // dW_{l+2} (committed to barW[l & 1]) last read tile (l - 1) % 3
+        if (l + 2 > NH || ((l & 1) ? wait_rows(barW0 + 8, phW1) : wait_rows(barW0, phW0))) {
+          const uint8_t *h = sm + T::H_OFF + (uint32_t)(l - 1) * 16384;
+          uint8_t *dz = sm + T::DZ_OFF + (uint32_t)((l - 1) % 3) * 16384;
+#pragma unroll
+          for (int c = 0; c < 8; c++) {
+            const uint4 hv = *reinterpret_cast<const uint4 *>(h + sw128_chunk(t, c));
+            const uint32_t hw[4] = {hv.x, hv.y, hv.z, hv.w};
+            uint32_t q[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+              const float2 hf = unpack2(hw[j]);
+              q[j] = pack2_sat(hf.x > 0.f ? v[8 * c + 2 * j] : 0.f, hf.y > 0.f ? v[8 * c + 2 * j + 1] : 0.f);
+            }
+            *reinterpret_cast<uint4 *>(dz + sw128_chunk(t, c)) = make_uint4(q[0], q[1], q[2], q[3]);
+          }
+          fence_async_smem();
+          fence_before();
+        }
+      }
+      // step 0: dW_2's phase of barW[0] (if any) is consumed here
+      if (l == 0 && NH >= 2 && rows_warp) wait_rows(barW0, phW0);
+      if (!__syncthreads_and(ok)) break;
+    }
+    if (!ok) break;
+    // dW_1 and dW_0 (barA) read X, H_1 and two dZ tiles: complete before the
+    // next tile overwrites them
+    if (rows_warp) wait_rows(barA, phA);
+    ok = __syncthreads_and(ok);
     first = false;
   }
-  // ---- this CTA's weight-gradient sums: layer l's row o in lane 32 (o / 16) + o % 16
-  if (ok) {
+  // ---- this CTA's weight-gradient sums into the gradient.  Layer l's row o
+  // is in lane 32 (o / 16) + o % 16 (M = 64 accumulator layout); the rows
+  // warps stage every layer in the gradient's own layout in shared memory
+  // (H and dZ are free now), then all warps add it to the gradient with
+  // coalesced vector reductions.
+  float *stage = reinterpret_cast<float *>(sm + T::H_OFF);
+  const bool sums = ok && !first;
+  if (sums && rows_warp) {
     fence_after();
     const int o = warp * 16 + lane;
 #pragma unroll 1
@@ -306,19 +393,28 @@ __global__ void __launch_bounds__(128, 1)
         float v[64];
         tmem_ld64(lane_base + (uint32_t)(T::dw_col(l) + c0), v);
         if (lane < 16 && o < N) {
-          float *dst = partial + (size_t)blockIdx.x * n_params + layer_offset(n, l) + (size_t)o * K + c0;
+          float4 *dst = reinterpret_cast<float4 *>(stage + layer_offset(n, l)) + o * (K / 4);
 #pragma unroll
           for (int i = 0; i < 64; i += 4)
-            if (c0 + i < K)
-              *reinterpret_cast<float4 *>(dst + i) = first ? make_float4(0.f, 0.f, 0.f, 0.f)
-                                                           : make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+            if (c0 + i < K) dst[stage_slot(o, (c0 + i) / 4, K / 4)] = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
         }
       }
     }
-  } else if (t == 0) {
-    atomicExch(err, 1);
   }
-  if (loss_sum) {
+  __syncthreads();
+  if (sums) {
+#pragma unroll 1
+    for (int l = 0; l <= NH; l++) {
+      const int K4 = T::in_(l) / 4, count4 = T::out_(l) * K4, off = layer_offset(n, l);
+      const float4 *src = reinterpret_cast<const float4 *>(stage + off);
+      for (int q = t; q < count4; q += TC_THREADS) {
+        const int o = q / K4, i4 = q - o * K4;
+        red_add_v4(n.grad + off + 4 * q, src[o * K4 + stage_slot(o, i4, K4)]);
+      }
+    }
+  }
+  if (!ok && t == 0) atomicExch(err, 1);
+  if (loss_sum && rows_warp) {
     for (int k = 16; k > 0; k >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, k);
     if (lane == 0) atomicAdd(loss_sum, lsum);
   }
@@ -327,35 +423,18 @@ __global__ void __launch_bounds__(128, 1)
   if (warp == 0) tmem_free(tm, T::TMEM_COLS);
 }
 
-// gradient += the CTAs' partial sums (parts x count, CTA-major; count a
-// multiple of 4).  Thread (x, y) sums parts [16 y, 16 y + 16) of four
-// consecutive parameters with independent 16-byte loads, all in flight, and
-// adds the four sums with one vector atomic.
-constexpr int REDUCE_PARTS = 16;
-__global__ void k_grad_reduce(const float4 *__restrict__ partial, int parts, int count4, float4 *__restrict__ grad) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  const int c0 = blockIdx.y * REDUCE_PARTS;
-  if (q >= count4) return;
-  float4 v[REDUCE_PARTS];
-#pragma unroll
-  for (int k = 0; k < REDUCE_PARTS; k++)
-    v[k] = c0 + k < parts ? __ldcs(partial + (size_t)(c0 + k) * count4 + q) : make_float4(0.f, 0.f, 0.f, 0.f);
-  float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-  for (int k = 0; k < REDUCE_PARTS; k++) {
-    s.x += v[k].x;
-    s.y += v[k].y;
-    s.z += v[k].z;
-    s.w += v[k].w;
-  }
-  atomicAdd(grad + q, s);
+// The weight image the training kernel copies: every f16 weight at its
+// swizzled position (after set_params / load_state; Adam keeps it current).
+__global__ void k_pack_wimg(Net n, int count, uint8_t *__restrict__ wimg) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+    *reinterpret_cast<__half *>(wimg + wimg_offset(n, i)) = n.w16[i];
 }
 
 // Adam (Kingma & Ba, ICLR 2015) on the f32 master weights; the gradient is
 // divided by the loss scale first and cleared afterwards.
 __global__ void k_adam(int count, float *__restrict__ w32, __half *__restrict__ w16, float *__restrict__ grad,
                        float *__restrict__ m, float *__restrict__ v, float lr, float b1, float b2, float eps,
-                       float inv_scale, float bc1, float bc2) {
+                       float inv_scale, float bc1, float bc2, Net n, uint8_t *__restrict__ wimg) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
     float gr = grad[i] * inv_scale;
     if (!isfinite(gr)) gr = 0.f;  // an overflowed element skips this step
@@ -365,7 +444,9 @@ __global__ void k_adam(int count, float *__restrict__ w32, __half *__restrict__ 
     v[i] = vi;
     const float wi = w32[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
     w32[i] = wi;
-    w16[i] = __float2half_rn(wi);
+    const __half h = __float2half_rn(wi);
+    w16[i] = h;
+    *reinterpret_cast<__half *>(wimg + wimg_offset(n, i)) = h;  // the training kernel's weight image
     grad[i] = 0.f;
   }
 }
@@ -410,9 +491,15 @@ struct LossVmf {
   const float *wsum;     // if set: weights are normalised by the batch sum
   float clip;            // if > 0: per-row bound on the gradient's L2 norm (before `scale`)
   static constexpr float KAPPA_MAX = 500.f;
+  static constexpr bool kEncodes = false;
+  using Pre = float4;  // (omega.xyz, the weight normalised by the batch sum)
+  __device__ Pre preload(int row) const {
+    float4 tg = target[row];
+    tg.w = wsum ? tg.w / fmaxf(*wsum, 1e-30f) : tg.w;
+    return tg;
+  }
   template <int OUT>
-  __device__ float grad(int row, const float *y, float *dy) const {
-    const float4 tg = target[row];
+  __device__ float grad(int, const float *y, float *dy, Pre tg) const {
     const float3 w = make_float3(tg.x, tg.y, tg.z);
     float logit[GUIDE_LOBES], kap[GUIDE_LOBES], cs[GUIDE_LOBES], f[GUIDE_LOBES], mn[GUIDE_LOBES];
     float3 mu[GUIDE_LOBES];
@@ -437,7 +524,7 @@ struct LossVmf {
       p += logit[i] * f[i];
     }
     p = fmaxf(p, 1e-30f);
-    const float wn = wsum ? tg.w / fmaxf(*wsum, 1e-30f) : tg.w;
+    const float wn = tg.w;
     if (wn == 0.f) {  // no contribution, no gradient (whatever the outputs)
       for (int o = 0; o < OUT; o++) dy[o] = 0.f;
       return 0.f;
@@ -640,9 +727,11 @@ __device__ __forceinline__ void nrc_encode(const float4 *f, float3 lo, float3 in
 struct LossRelL2 {
   const float4 *target;
   float scale;
+  static constexpr bool kEncodes = false;
+  using Pre = float4;
+  __device__ Pre preload(int row) const { return target[row]; }
   template <int OUT>
-  __device__ float grad(int row, const float *y, float *dy) const {
-    const float4 t = target[row];
+  __device__ float grad(int, const float *y, float *dy, Pre t) const {
     const float tv[3] = {t.x, t.y, t.z};
     float loss = 0.f;
     for (int c = 0; c < 3; c++) {
@@ -656,13 +745,54 @@ struct LossRelL2 {
   }
 };
 
+// The record a training row draws (with replacement): a hash of the row,
+// the Adam step and the render's key.
+__device__ __forceinline__ int nrc_record_index(int row, int count, uint32_t key, uint32_t step) {
+  uint32_t h = (uint32_t)row * 0x9E3779B1u ^ (step * 0x85EBCA77u) ^ key;
+  h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12; h *= 0x297A2D39u; h ^= h >> 15;
+  return (int)(h % (uint32_t)count);
+}
+
+// The cache's training loss with its input built inside the training kernel:
+// row r of the batch is record nrc_record_index(r) (the sampling of
+// k_nrc_encode_records), encoded by nrc_encode straight into row t of the
+// swizzled input tile; the target is the record's radiance (non-finite: 0).
+struct LossRelL2Records {
+  const float4 *rec;
+  int count;
+  uint32_t key, step;
+  float3 lo, inv_ext;
+  float scale;
+  static constexpr bool kEncodes = true;
+  using Pre = float4;
+  __device__ Pre encode(int row, bool valid, uint8_t *xtile, int t) const {
+    __align__(16) __half x[NRC_IN];
+    float4 tg = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid) {
+      const int idx = nrc_record_index(row, count, key, step);
+      nrc_encode(rec + 5 * (size_t)idx, lo, inv_ext, x);
+      const float4 tt = rec[5 * (size_t)idx + 4];
+      if (finite4(tt)) tg = tt;
+    } else {
+#pragma unroll
+      for (int i = 0; i < NRC_IN; i++) x[i] = __float2half_rn(0.f);
+    }
+#pragma unroll
+    for (int c = 0; c < NRC_IN / 8; c++)
+      *reinterpret_cast<uint4 *>(xtile + tc05::sw128_chunk(t, c)) = reinterpret_cast<const uint4 *>(x)[c];
+    return tg;
+  }
+  template <int OUT>
+  __device__ float grad(int row, const float *y, float *dy, Pre t) const {
+    return LossRelL2{nullptr, scale}.template grad<OUT>(row, y, dy, t);
+  }
+};
+
 __global__ void k_nrc_encode_records(const float4 *__restrict__ rec, int count, int rows, uint32_t key,
                                      uint32_t step, float3 lo, float3 inv_ext, __half *__restrict__ X,
                                      float4 *__restrict__ target) {
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
-    uint32_t h = (uint32_t)r * 0x9E3779B1u ^ (step * 0x85EBCA77u) ^ key;
-    h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12; h *= 0x297A2D39u; h ^= h >> 15;
-    const int idx = (int)(h % (uint32_t)count);
+    const int idx = nrc_record_index(r, count, key, step);
     __align__(16) __half row[NRC_IN];
     nrc_encode(rec + 5 * (size_t)idx, lo, inv_ext, row);
     store_row(row, X + (size_t)r * NRC_IN);
@@ -718,8 +848,8 @@ struct tpt_mlp {
   int params = 0;
   float *w32 = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
   __half *w16 = nullptr;
-  float *partial = nullptr;  // per-CTA weight-gradient sums of the training kernel [parts][params]
-  int parts = 0;             // CTAs the partial buffer holds (the SM count)
+  uint8_t *wimg = nullptr;   // the f16 weights as the training kernel's swizzled shared-memory image
+  int wimg_bytes = 0;
   float *loss = nullptr;
   int *err = nullptr;        // set by the training kernel when an MMA completion wait timed out
   int steps = 0;
@@ -758,34 +888,20 @@ tpt_status launch_forward(tpt_mlp *M, const __half *x, int rows, float *y, cudaS
   return mlp_cuda(cudaGetLastError());
 }
 
-// The workspace of the training kernel: one slice of weight-gradient sums
-// per CTA, at most one CTA per SM.
-tpt_status ensure_ws(tpt_mlp *M, int rows) {
-  (void)rows;
-  if (M->partial) return TPT_OK;
-  int sms = 0;
-  MLP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, M->device));
-  MLP_CUDA(cudaMalloc(&M->partial, (size_t)sms * M->params * sizeof(float)));
-  M->parts = sms;
-  return TPT_OK;
-}
-
 template <int IN, int NH, int OUT, class Loss>
 tpt_status launch_train(tpt_mlp *M, const __half *x, int rows, const Loss &loss, cudaStream_t s) {
   using L = TrainLayout<IN, NH, OUT>;
-  tpt_status st = ensure_ws(M, rows);
-  if (st != TPT_OK) return st;
+  static_assert(L::W_BYTES % 16 == 0, "bulk copies move 16-byte multiples");
+  if ((int)L::W_BYTES != M->wimg_bytes) return TPT_ERR_INVALID_ARGUMENT;
+  int sms = 0;
+  MLP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, M->device));
   MLP_CUDA(cudaFuncSetAttribute(k_mlp_train_tc<IN, NH, OUT, Loss>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)L::SMEM));
   const int tiles = (rows + 127) / 128;
-  const int grid = tiles < M->parts ? tiles : M->parts;
+  const int grid = tiles < sms ? tiles : sms;
   MLP_CUDA(cudaMemsetAsync(M->loss, 0, sizeof(float), s));
-  k_mlp_train_tc<IN, NH, OUT, Loss><<<grid, 128, L::SMEM, s>>>(M->net, x, rows, loss, M->partial, M->loss, M->err);
-  MLP_CUDA(cudaGetLastError());
-  const int count4 = M->params / 4;  // every supported shape has a multiple of 4 parameters
-  const dim3 rgrid((count4 + 127) / 128, (grid + REDUCE_PARTS - 1) / REDUCE_PARTS);
-  k_grad_reduce<<<rgrid, 128, 0, s>>>(reinterpret_cast<const float4 *>(M->partial), grid, count4,
-                                      reinterpret_cast<float4 *>(M->grad));
+  k_mlp_train_tc<IN, NH, OUT, Loss><<<grid, TC_THREADS, L::SMEM, s>>>(M->net, M->wimg, x, rows, loss, M->loss,
+                                                                      M->err);
   return mlp_cuda(cudaGetLastError());
 }
 
@@ -859,7 +975,6 @@ tpt_status guide_train(GuideNet *G, const float4 *rec, int count, int steps, int
   batch = (batch + 15) / 16 * 16;
   tpt_status st = guide_ws(G, batch);
   if (st != TPT_OK) return st;
-  if ((st = ensure_ws(G->net, batch)) != TPT_OK) return st;
   const float3 inv = make_float3(1.f / ext.x, 1.f / ext.y, 1.f / ext.z);
   const float loss_scale = 256.f;  // weights are normalised to sum 1 per batch
   for (int k = 0; k < steps; k++) {
@@ -948,14 +1063,12 @@ tpt_status cache_train(CacheNet *G, const float4 *rec, int count, int steps, int
   batch = (batch + 15) / 16 * 16;
   tpt_status st = cache_ws(G, batch);
   if (st != TPT_OK) return st;
-  if ((st = ensure_ws(G->net, batch)) != TPT_OK) return st;
   const float3 inv = make_float3(1.f / ext.x, 1.f / ext.y, 1.f / ext.z);
   const float loss_scale = 1024.f;
   for (int k = 0; k < steps; k++) {
-    k_nrc_encode_records<<<(batch + 255) / 256, 256, 0, s>>>(rec, count, batch, key, (uint32_t)(G->net->steps + 1),
-                                                             lo, inv, G->x, G->target);
-    LossRelL2 L{G->target, loss_scale / (float)batch};
-    st = launch_train<NRC_IN, NRC_NH, NRC_OUT>(G->net, G->x, batch, L, s);
+    // the rows are sampled and encoded inside the training kernel
+    LossRelL2Records L{rec, count, key, (uint32_t)(G->net->steps + 1), lo, inv, loss_scale / (float)batch};
+    st = launch_train<NRC_IN, NRC_NH, NRC_OUT>(G->net, nullptr, batch, L, s);
     if (st != TPT_OK) return st;
     if ((st = tpt_mlp_adam(G->net, lr, 1.f / loss_scale, s)) != TPT_OK) return st;
   }
@@ -1035,6 +1148,9 @@ tpt_status tpt_mlp_create(int32_t device, int32_t in_dim, int32_t n_hidden, int3
   if (e == cudaSuccess) e = cudaMalloc(&M->v, P * 4);
   if (e == cudaSuccess) e = cudaMalloc(&M->w16, P * 2);
   if (e == cudaSuccess) e = cudaMalloc(&M->loss, 4);
+  M->wimg_bytes = (int)wimg_bytes(M->net);
+  if (e == cudaSuccess) e = cudaMalloc(&M->wimg, (size_t)M->wimg_bytes);
+  if (e == cudaSuccess) e = cudaMemset(M->wimg, 0, (size_t)M->wimg_bytes);
   if (e == cudaSuccess) e = cudaMalloc(&M->err, 4);
   if (e == cudaSuccess) e = cudaMemset(M->err, 0, 4);
   if (e != cudaSuccess) {
@@ -1065,7 +1181,7 @@ tpt_status tpt_mlp_create(int32_t device, int32_t in_dim, int32_t n_hidden, int3
 void tpt_mlp_destroy(tpt_mlp *M) {
   if (!M) return;
   cudaSetDevice(M->device);
-  void *ptrs[] = {M->w32, M->grad, M->m, M->v, M->w16, M->partial, M->loss, M->err};
+  void *ptrs[] = {M->w32, M->grad, M->m, M->v, M->w16, M->wimg, M->loss, M->err};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete M;
@@ -1081,6 +1197,8 @@ tpt_status tpt_mlp_set_params(tpt_mlp *M, const float *host) {
   for (size_t i = 0; i < P; i++) h[i] = __float2half_rn(host[i]);
   MLP_CUDA(cudaMemcpy(M->w32, host, P * 4, cudaMemcpyHostToDevice));
   MLP_CUDA(cudaMemcpy(M->w16, h.data(), P * 2, cudaMemcpyHostToDevice));
+  k_pack_wimg<<<(M->params + 255) / 256, 256>>>(M->net, M->params, M->wimg);
+  MLP_CUDA(cudaGetLastError());
   MLP_CUDA(cudaMemset(M->grad, 0, P * 4));
   MLP_CUDA(cudaMemset(M->m, 0, P * 4));
   MLP_CUDA(cudaMemset(M->v, 0, P * 4));
@@ -1116,8 +1234,6 @@ tpt_status tpt_mlp_backward_given(tpt_mlp *M, const void *x_f16, const float *dy
                                   void *stream) {
   if (!M || !x_f16 || !dy || rows <= 0 || rows % 16 || rows > (1 << 26)) return TPT_ERR_INVALID_ARGUMENT;
   MLP_CUDA(cudaSetDevice(M->device));
-  tpt_status st = ensure_ws(M, (int)rows);
-  if (st != TPT_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
   const __half *x = (const __half *)x_f16;
   LossGiven L{dy, scale};
@@ -1131,8 +1247,7 @@ tpt_status tpt_mlp_backward_vmf(tpt_mlp *M, const void *x_f16, const float *targ
   if (!M || !x_f16 || !target || rows <= 0 || rows % 16 || rows > (1 << 26)) return TPT_ERR_INVALID_ARGUMENT;
   if (M->in_dim != GUIDE_IN || M->n_hidden != GUIDE_NH || M->out_dim != GUIDE_OUT) return TPT_ERR_INVALID_ARGUMENT;
   MLP_CUDA(cudaSetDevice(M->device));
-  tpt_status st = ensure_ws(M, (int)rows);
-  if (st != TPT_OK) return st;
+  tpt_status st = TPT_OK;
   cudaStream_t s = (cudaStream_t)stream;
   LossVmf L{(const float4 *)target, scale, nullptr, 0.f};
   st = launch_train<GUIDE_IN, GUIDE_NH, GUIDE_OUT>(M, (const __half *)x_f16, (int)rows, L, s);
@@ -1150,11 +1265,34 @@ tpt_status tpt_mlp_backward_rel_l2(tpt_mlp *M, const void *x_f16, const float *t
   if (!M || !x_f16 || !target || rows <= 0 || rows % 16 || rows > (1 << 26)) return TPT_ERR_INVALID_ARGUMENT;
   if (M->in_dim != NRC_IN || M->n_hidden != NRC_NH || M->out_dim != NRC_OUT) return TPT_ERR_INVALID_ARGUMENT;
   MLP_CUDA(cudaSetDevice(M->device));
-  tpt_status st = ensure_ws(M, (int)rows);
-  if (st != TPT_OK) return st;
+  tpt_status st = TPT_OK;
   cudaStream_t s = (cudaStream_t)stream;
   LossRelL2 L{(const float4 *)target, scale};
   st = launch_train<NRC_IN, NRC_NH, NRC_OUT>(M, (const __half *)x_f16, (int)rows, L, s);
+  if (st != TPT_OK) return st;
+  if (loss_out) {
+    MLP_CUDA(cudaMemcpyAsync(loss_out, M->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+    MLP_CUDA(cudaStreamSynchronize(s));
+    return check_train_err(M, s);
+  }
+  return TPT_OK;
+}
+
+tpt_status tpt_mlp_backward_rel_l2_records(tpt_mlp *M, const float *records, int64_t count, uint32_t key,
+                                           uint32_t step, const float *lo, const float *extent, int64_t rows,
+                                           float scale, float *loss_out, void *stream) {
+  if (!M || !records || !lo || !extent || count <= 0 || count > (1 << 28) || rows <= 0 || rows % 16 ||
+      rows > (1 << 26))
+    return TPT_ERR_INVALID_ARGUMENT;
+  if (M->in_dim != NRC_IN || M->n_hidden != NRC_NH || M->out_dim != NRC_OUT) return TPT_ERR_INVALID_ARGUMENT;
+  for (int a = 0; a < 3; a++)
+    if (!(extent[a] > 0.f) || !std::isfinite(lo[a]) || !std::isfinite(extent[a])) return TPT_ERR_INVALID_ARGUMENT;
+  MLP_CUDA(cudaSetDevice(M->device));
+  cudaStream_t s = (cudaStream_t)stream;
+  const float3 l = make_float3(lo[0], lo[1], lo[2]);
+  const float3 inv = make_float3(1.f / extent[0], 1.f / extent[1], 1.f / extent[2]);
+  LossRelL2Records L{(const float4 *)records, (int)count, key, step, l, inv, scale};
+  tpt_status st = launch_train<NRC_IN, NRC_NH, NRC_OUT>(M, nullptr, (int)rows, L, s);
   if (st != TPT_OK) return st;
   if (loss_out) {
     MLP_CUDA(cudaMemcpyAsync(loss_out, M->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
@@ -1200,7 +1338,8 @@ tpt_status tpt_mlp_adam(tpt_mlp *M, float lr, float inv_loss_scale, void *stream
   const float b1 = 0.9f, b2 = 0.999f;
   const float bc1 = 1.f - std::pow(b1, (float)M->steps), bc2 = 1.f - std::pow(b2, (float)M->steps);
   k_adam<<<(M->params + 255) / 256, 256, 0, (cudaStream_t)stream>>>(M->params, M->w32, M->w16, M->grad, M->m, M->v,
-                                                                     lr, b1, b2, 1e-8f, inv_loss_scale, bc1, bc2);
+                                                                     lr, b1, b2, 1e-8f, inv_loss_scale, bc1, bc2,
+                                                                     M->net, M->wimg);
   return mlp_cuda(cudaGetLastError());
 }
 

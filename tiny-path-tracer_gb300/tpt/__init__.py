@@ -178,6 +178,9 @@ _SIGS = {
                                          C.c_void_p]),
     "tpt_mlp_backward_rel_l2": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float,
                                             C.c_void_p, C.c_void_p]),
+    "tpt_mlp_backward_rel_l2_records": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_uint32, C.c_uint32,
+                                                    C.c_void_p, C.c_void_p, C.c_int64, C.c_float, C.c_void_p,
+                                                    C.c_void_p]),
     "tpt_guide_encode": (C.c_int32, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_void_p]),
     "tpt_nrc_encode": (C.c_int32, [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -640,6 +643,16 @@ class Mlp:
         loss = C.c_float()
         check(lib().tpt_mlp_backward_rel_l2(self._h, C.c_void_p(x_f16_ptr), C.c_void_p(target_ptr), rows, scale,
                                             C.byref(loss), None), "mlp_backward_rel_l2")
+        return loss.value
+
+    def backward_rel_l2_records(self, rec_ptr: int, count: int, key: int, step: int, lo, extent, rows: int,
+                                scale: float = 1.0) -> float:
+        loss = C.c_float()
+        lo_a = np.ascontiguousarray(lo, np.float32)
+        ext_a = np.ascontiguousarray(extent, np.float32)
+        check(lib().tpt_mlp_backward_rel_l2_records(self._h, C.c_void_p(rec_ptr), count, key, step, _ptr(lo_a),
+                                                    _ptr(ext_a), rows, scale, C.byref(loss), None),
+              "mlp_backward_rel_l2_records")
         return loss.value
 
     def adam(self, lr: float, inv_loss_scale: float = 1.0) -> None:
