@@ -278,7 +278,7 @@ def batch_leg(ctx, stream, steps: int, warmup: int, bvh: str = "reference", bloc
     tuned = None
     if block == 0 and wave == 0:  # block, register variant, walk threshold by the autotuner (untimed)
         tuned = tpt.autotune_batch(ctx, jobs, ptrs, 8, max_depth=50, background=tpt.BACKGROUND_SKY, seed=1)
-        kw.update(block=tuned[0], variant=tuned[1], flat_nodes=tuned[2])
+        kw.update(block=tuned[0], variant=tuned[1], flat_nodes=tuned[2], refill=tuned[3])
     for _ in range(warmup):
         tpt.render_batch(ctx, jobs, outs=ptrs, **kw)
     torch.cuda.synchronize()
@@ -317,6 +317,8 @@ def batch_leg(ctx, stream, steps: int, warmup: int, bvh: str = "reference", bloc
     return {"workload": "batch_64_random_sphere_scenes", "value": value, "unit": "Msamples/s", "ms_per_step": ms,
             "steps": steps, "scenes": len(jobs), "samples_per_step": samples, "bvh": bvh,
             "launch": {"block": kw["block"], "variant": kw["variant"], "flat_nodes": kw.get("flat_nodes", 0),
+                       "refill": kw.get("refill", 1), "kernel": ("stepped walk" if kw["variant"] >= 14 else
+                                                                 "whole-segment walk"),
                        "autotuned": tuned is not None},
             "segments_per_step": st["segments"], "scene_compile_s": t1 - t0, "scene_upload_s": t2 - t1,
             "gpu_launches": st["kernel_launches"] * steps, "clocks": clk, "cpu_baseline": cpu,

@@ -311,10 +311,16 @@ tpt_status tpt_render_batch(tpt_context *ctx, const tpt_batch_item *items, int32
 tpt_status tpt_autotune(tpt_context *ctx, int32_t slot, tpt_render_params *p, int32_t probe_spp, double *best_msps);
 /* Autotuner of a batch: renders the batch with every item's spp divided by
  * spp_divisor (at least 1) for each candidate block size, register variant
- * and stackless-walk threshold of the batched persistent launch, times them
- * with CUDA events, times the three fastest again (fastest of three runs)
- * and writes the winner into p (block, wave, flat_nodes) for
- * tpt_render_batch.  best_msps (may be NULL) receives its Msamples/s. */
+ * and stackless-walk threshold of the batched persistent launch - and, when
+ * every item is sphere-only, the stepped-walk kernel (wave 14-16) with 16 or
+ * 24 waiting lanes per shading round (refill) - times them with CUDA
+ * events, times the three fastest again (fastest of three runs) and writes
+ * the winner into p (block, wave, flat_nodes, refill) for tpt_render_batch.
+ * best_msps (may be NULL) receives its Msamples/s.
+ * In tpt_render_batch, wave 14, 15 or 16 selects the stepped walk for
+ * sphere-only batches (4, 5 or 6 resident blocks per SM): each lane advances
+ * its BVH walk a few nodes per round and the lanes that finished shade
+ * together once `refill` of them wait; other batches ignore it. */
 tpt_status tpt_autotune_batch(tpt_context *ctx, const tpt_batch_item *items, int32_t n, tpt_render_params *p,
                               int32_t spp_divisor, double *best_msps);
 

@@ -601,6 +601,176 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
   if (e) atomicExch(&C->err, e);
 }
 
+// Batched persistent engine for sphere-only scenes, with the BVH walk split
+// into steps.  In k_persistent_batch a lane traces a whole segment inside one
+// call, so a warp runs the walk as long as its longest lane and the others
+// idle (4.7 of 32 lanes per instruction on the 64-scene batch).  Here every
+// lane keeps its walk's state (stack depth, best hit) in registers: each
+// round the traversing lanes advance up to STEP_NODES nodes, and a lane
+// whose walk ends waits; once at least `cfg.refill` lanes of the warp wait
+// (or none is walking), they shade together, continue or finish their paths,
+// claim new camera samples, and start their next walks.  The walk visits the
+// same nodes with the same tests, pruning and tie order as trace_closest's
+// stack walk (a node's children: boxes by the slab test, sphere leaves by the
+// reference's quadratic, inline in the node's record), so every sample's
+// radiance is the same; a scene that is not one top-level BVH item takes
+// trace_closest for its segments.
+enum { STEP_NODES = 6 };
+enum { LANE_IDLE = 0, LANE_WALK = 1, LANE_READY = 2, LANE_DONE = 3 };
+
+template <int MIN_BLOCKS>
+__global__ void __launch_bounds__(128, MIN_BLOCKS)
+    k_persistent_batch_step(const BatchItem *__restrict__ items, int n_items, unsigned long long total_all,
+                            RenderCfg cfg, WfCounters *C) {
+  extern __shared__ int2 stack_smem[];
+  __shared__ unsigned long long s_first[TPT_MAX_BATCH];
+  for (int i = threadIdx.x; i < n_items; i += blockDim.x) s_first[i] = items[i].first;
+  __syncthreads();
+  int2 *stk = stack_smem + threadIdx.x;
+  const int stride = blockDim.x;
+  const float tmin = 0.001f, tmax = 3.402823466e38f;
+  int e = 0;
+  unsigned long long segs = 0;
+  int state = LANE_IDLE;
+  Ray r{};
+  RayPre W{};
+  float3 T = v3(0.f, 0.f, 0.f), L = v3(0.f, 0.f, 0.f);
+  uint32_t pixel = 0, sample = 0;
+  int depth = 0, item = 0;
+  // walk state
+  int sp = 0, bl = -1;
+  float bt = CUDART_INF_F;
+  const f4 *kids = nullptr;
+  const int never_pruned = __float_as_int(-CUDART_INF_F);
+  const int threshold = cfg.refill < 1 ? 1 : (cfg.refill > 32 ? 32 : cfg.refill);
+  for (;;) {
+    const unsigned waiting = __ballot_sync(0xffffffffu, state == LANE_IDLE || state == LANE_READY);
+    const unsigned walking = __ballot_sync(0xffffffffu, state == LANE_WALK);
+    if (waiting && ((int)__popc(waiting) >= threshold || !walking)) {
+      // ---- shade the finished walks; continue or finish the paths
+      bool start = false;
+      if (state == LANE_READY) {
+        const DevScene &S = items[item].scene;
+        const HitRef h{bt, bl, -1, -1};
+        if (shade_vertex(S, cfg, r, bl >= 0, h, T, L, depth, pixel, sample)) {
+          depth++;
+          start = true;
+        } else {
+          accumulate(items[item].frame, pixel, L);
+          state = LANE_IDLE;
+        }
+      }
+      // ---- idle lanes claim the next camera samples (one atomic per warp)
+      const bool want = state == LANE_IDLE;
+      unsigned long long base;
+      int rank;
+      warp_claim(want, &C->issued, base, rank);
+      if (want) {
+        const unsigned long long sidx = base + (unsigned long long)rank;
+        if (sidx < total_all) {
+          int lo = 0, hi = n_items - 1;  // last item with first <= sidx
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_first[mid] <= sidx) lo = mid; else hi = mid - 1;
+          }
+          item = lo;
+          const BatchItem &B = items[item];
+          int i, j;
+          sample_coords(B.frame, sidx - s_first[item], pixel, sample, i, j);
+          r = camera_ray(B.scene.cam, i, j, B.frame.nx, B.frame.ny, pixel, sample, cfg.key);
+          T = v3(1.f, 1.f, 1.f);
+          L = v3(0.f, 0.f, 0.f);
+          depth = 0;
+          start = true;
+        } else {
+          state = LANE_DONE;
+        }
+      }
+      // ---- start the next walk: the root box, or the whole segment by
+      // trace_closest where the scene is not one top-level BVH
+      if (start) {
+        segs++;
+        const DevScene &S = items[item].scene;
+        const int2 it0 = *reinterpret_cast<const int2 *>(S.items);
+        bt = CUDART_INF_F;
+        bl = -1;
+        sp = 0;
+        if (S.n_items == 1 && it0.x == ITEM_BVH) {
+          W = precompute(r);
+          kids = S.node_kids;
+          float en;
+          const f4 rlo = ldg4(S.node_lo + it0.y), rhi = ldg4(S.node_hi + it0.y);
+          if (slab(W, rlo, rhi, tmin, tmax, en)) {
+            stk[0] = make_int2(it0.y, never_pruned);
+            sp = 1;
+          }
+          state = sp ? LANE_WALK : LANE_READY;
+        } else {
+          MediumRng m{make_uint4(pixel, sample, (uint32_t)depth, 0u), cfg.key, 1};
+          HitRef h;
+          const bool hit = trace_closest<FEAT_SPHERES>(S, r, tmin, stk, stride, m, h, e);
+          bt = h.t;
+          bl = hit ? h.leaf : -1;
+          state = LANE_READY;
+        }
+      }
+    }
+    if (__all_sync(0xffffffffu, state == LANE_DONE)) break;
+    // ---- walk: up to STEP_NODES nodes per lane (the stack walk of trace_closest)
+#pragma unroll 1
+    for (int k = 0; k < STEP_NODES && state == LANE_WALK; k++) {
+      const int2 en = stk[(sp - 1) * stride];
+      --sp;
+      if (!(__int_as_float(en.y) > bt)) {
+        const f4 *kid = kids + 4 * (size_t)en.x;
+        const f4 k0 = ldg4(kid), k1 = ldg4(kid + 1), k2 = ldg4(kid + 2), k3 = ldg4(kid + 3);
+        const int left = __float_as_int(k0.w), right = __float_as_int(k2.w);
+        int2 q[2];
+        float ent[2];
+        int nq = 0;
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+          const int ref = c == 0 ? left : right;
+          if (c == 1 && right == left) break;  // n == 1 node: left_ == right_
+          if (ref >= 0) {
+            float entry;
+            const f4 clo = c == 0 ? k0 : k2, chi = c == 0 ? k1 : k3;
+            if (slab(W, clo, chi, tmin, tmax, entry)) {
+              ent[nq] = entry;
+              q[nq++] = make_int2(ref, __float_as_int(prune_key_ext(W, chi.w, entry)));
+            }
+          } else {  // a sphere leaf, carried in the child's slot
+            const f4 sc = c == 0 ? k0 : k2;
+            const int leaf = ~ref;
+            float t;
+            if (sphere_t(v3(sc.x, sc.y, sc.z), (c == 0 ? k1 : k3).x, r, tmin, tmax, t) &&
+                (t < bt || (t == bt && leaf > bl))) {  // ties: the larger leaf order (hitable.cc:71)
+              bt = t;
+              bl = leaf;
+            }
+          }
+        }
+        if (nq == 2 && ent[1] > ent[0]) {
+          const int2 tq = q[0];
+          q[0] = q[1];
+          q[1] = tq;
+        }
+        for (int k2i = 0; k2i < nq; k2i++) {
+          if (sp >= TRAVERSAL_STACK) {
+            e = TPT_ERR_STACK_OVERFLOW;
+          } else {
+            stk[sp * stride] = q[k2i];
+            sp++;
+          }
+        }
+      }
+      if (sp == 0) state = LANE_READY;
+    }
+  }
+  if (segs) atomicAdd(&C->segments, segs);
+  if (e) atomicExch(&C->err, e);
+}
+
 // Guided persistent engine: as k_persistent, with guided diffuse vertices
 // and one training record per recorded path (every `rec_stride`-th sample).
 // A recording path parks the state of its first diffuse vertex in `pend`
@@ -1539,9 +1709,14 @@ static uint64_t fnv1a(uint64_t h, const void *data, size_t n) {
 }
 
 typedef void (*BatchKernel)(const BatchItem *, int, unsigned long long, RenderCfg, WfCounters *);
+// Register variants 4-6 (and 8): k_persistent_batch; 14-16: the stepped walk
+// (k_persistent_batch_step), sphere-only batches only.
 static BatchKernel batch_variant(int v, int feat = FEAT_ALL) {
   if (feat == FEAT_SPHERES) {  // every item sphere-only
     switch (v) {
+      case 14: return k_persistent_batch_step<4>;
+      case 15: return k_persistent_batch_step<5>;
+      case 16: return k_persistent_batch_step<6>;
       case 5: return k_persistent_batch<5, FEAT_SPHERES>;
       case 6: return k_persistent_batch<6, FEAT_SPHERES>;
       default: return k_persistent_batch<4, FEAT_SPHERES>;
@@ -1790,12 +1965,21 @@ extern "C" tpt_status tpt_autotune_batch(tpt_context *c, const tpt_batch_item *i
   std::vector<tpt_batch_item> probe(items, items + n);
   for (auto &it : probe) it.spp = std::max(1, it.spp / spp_divisor);
   struct Cand {
-    int block, variant, flat;
+    int block, variant, flat, refill;
   };
   std::vector<Cand> cands;
   for (int block : {64, 128})
     for (int var : {4, 5, 6})
-      for (int flat : {16, 48}) cands.push_back({block, var, flat});
+      for (int flat : {16, 48}) cands.push_back({block, var, flat, 1});
+  bool spheres_only = true;
+  for (int k = 0; k < n; k++) {
+    const tpt_batch_item &it = items[k];
+    if (it.slot < 0 || it.slot >= (int32_t)c->slots.size() || !c->slots[it.slot].live) return TPT_ERR_BAD_HANDLE;
+    if (c->slots[it.slot].ds.feat != FEAT_SPHERES) spheres_only = false;
+  }
+  if (spheres_only)  // the stepped walk, and how many lanes wait before they shade
+    for (int var : {14, 15})
+      for (int refill : {16, 24}) cands.push_back({64, var, 16, refill});
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaError_t ce = cudaEventCreate(&e0);
   if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
@@ -1811,6 +1995,7 @@ extern "C" tpt_status tpt_autotune_batch(tpt_context *c, const tpt_batch_item *i
     q.block = cd.block;
     q.wave = cd.variant;
     q.flat_nodes = cd.flat;
+    q.refill = cd.refill;
     q.profile = 0;
     tpt_render_stats rs{};
     float best_ms = 1e30f;
@@ -1856,6 +2041,7 @@ extern "C" tpt_status tpt_autotune_batch(tpt_context *c, const tpt_batch_item *i
   p->block = win.block;
   p->wave = win.variant;
   p->flat_nodes = win.flat;
+  p->refill = win.refill;
   if (best_msps) *best_msps = best;
   return TPT_OK;
 }

@@ -526,7 +526,8 @@ def render_nrc(ctx: "Context", slot: int, width: int, height: int, spp: int, max
 def autotune_batch(ctx: "Context", jobs, outs, spp_divisor=8, max_depth=50, semantics=SEMANTICS_REFERENCE,
                    background=BACKGROUND_BLACK, sky_scale=1.0, seed=1):
     """tpt_autotune_batch over jobs (slot, width, height, spp) rendering into
-    the device pointers outs; returns (block, variant, flat_nodes, Msamples/s)."""
+    the device pointers outs; returns (block, variant, flat_nodes, refill,
+    Msamples/s)."""
     n = len(jobs)
     arr = (BatchItem * n)()
     for k, (slot, w, h, spp) in enumerate(jobs):
@@ -534,11 +535,11 @@ def autotune_batch(ctx: "Context", jobs, outs, spp_divisor=8, max_depth=50, sema
     p = make_params(1, 1, 1, max_depth, semantics, background, sky_scale, seed, ENGINE_PERSISTENT)
     best = C.c_double()
     check(lib().tpt_autotune_batch(ctx._h, arr, n, C.byref(p), spp_divisor, C.byref(best)), "autotune_batch")
-    return p.block, p.wave, p.flat_nodes, best.value
+    return p.block, p.wave, p.flat_nodes, p.refill, best.value
 
 
 def render_batch(ctx: "Context", jobs, max_depth=50, semantics=SEMANTICS_REFERENCE, background=BACKGROUND_BLACK,
-                 sky_scale=1.0, seed=1, block=0, variant=0, flat_nodes=0, profile=False, outs=None):
+                 sky_scale=1.0, seed=1, block=0, variant=0, flat_nodes=0, profile=False, outs=None, refill=0):
     """jobs: list of (slot, width, height, spp).  outs: None -> host images are
     returned; else a list of device pointers (one per job)."""
     n = len(jobs)
@@ -554,7 +555,7 @@ def render_batch(ctx: "Context", jobs, max_depth=50, semantics=SEMANTICS_REFEREN
             ptr = int(outs[k])
         arr[k] = BatchItem(slot, w, h, spp, ptr)
     p = make_params(1, 1, 1, max_depth, semantics, background, sky_scale, seed, ENGINE_PERSISTENT, block, variant,
-                    False, profile, flat_nodes)
+                    False, profile, flat_nodes, refill)
     st = RenderStats()
     check(lib().tpt_render_batch(ctx._h, arr, n, C.byref(p), TPT_MEM_HOST if host else TPT_MEM_DEVICE,
                                  C.byref(st)), "render_batch")
