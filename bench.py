@@ -445,8 +445,11 @@ def learned_equal_time(ctx, which: str) -> dict:
             the guide's share lowered to alpha 0.25 (the rest is the plain
             light/cosine mixture), which measured best on this scene.
     nrc:    the seeded next-week scene, 800x800, plain at 256 spp against the
-            cached renderer (paths terminated into the cache after 2 bounces)
-            at the spp that takes the same time; FP64 reference 4096 spp.
+            cached renderer at its default settings (an uncached 8-spp first
+            pass, then paths end into the cache by the path-spread rule,
+            c = 0.01, at the third bounce at the latest; 512 Adam steps after
+            each of the 4 passes) at the spp that takes the same time; FP64
+            reference 4096 spp.
     Every point (plain, learned at equal spp, at equal time, and the points
     of the time-to-plain-relMSE search) is the mean over three seeds (each
     learned run trains its own network online; per-seed values are reported

@@ -434,23 +434,25 @@ tpt_status tpt_guide_records(tpt_context *ctx, float *out, int64_t cap, int64_t 
 /* Neural radiance cache (no counterpart in the reference).  Rendered in
  * `passes` passes; in every pass after the first, a path stops at its first
  * diffuse vertex (lambertian, or isotropic in physical semantics) whose
- * vertex number is at least terminate_depth (0 = camera hit) and adds
- * throughput x cache(position, outgoing direction, normal, albedo,
- * roughness), the cache being an MLP of shape (64, 5, 16) evaluated on the
- * tensor cores for all such vertices at once; specular vertices and lights
- * are traced through.  Every train_stride-th path is a training path: it is
- * traced to full depth (contributing its unbiased estimate) and records its
- * first three diffuse vertices with their measured outgoing radiance; after
- * each pass the cache takes train_steps Adam steps on them (relative L2
- * loss).  The first pass traces every path to full depth.
+ * vertex number is at least terminate_depth (0 = camera hit), or earlier
+ * (past the camera hit) once its path spread exceeds spread_c x the camera
+ * vertex's, and adds throughput x cache(position, outgoing direction,
+ * normal, albedo, roughness), the cache being an MLP of shape (64, 5, 16)
+ * evaluated on the tensor cores for all such vertices at once; specular
+ * vertices and lights are traced through.  Every train_stride-th path is a
+ * training path: it is traced to full depth (contributing its unbiased
+ * estimate) and records its first three diffuse vertices with their
+ * measured outgoing radiance; after each pass the cache takes train_steps
+ * Adam steps on them (relative L2 loss).  The first pass, first_pass_spp
+ * samples per pixel, traces every path to full depth.
  * The estimator is biased by the cache's error; the plain tracer is its
- * fallback and the yardstick for that error. */
+ * fallback and the yardstick for that error.  Defaults in parentheses. */
 typedef struct {
-  int32_t passes;           /* >= 1 (8) */
-  int32_t train_steps;      /* Adam steps after each pass (256) */
+  int32_t passes;           /* >= 1 (4) */
+  int32_t train_steps;      /* Adam steps after each pass (512) */
   int32_t batch;            /* training rows per step (16384) */
   float lr;                 /* Adam learning rate (3e-3) */
-  int32_t terminate_depth;  /* 2: two bounces, then the cache */
+  int32_t terminate_depth;  /* the latest vertex a path ends at into the cache (3) */
   int32_t train_stride;     /* every n-th path trains the cache (16) */
   int32_t record_cap;       /* training records per pass */
   int32_t query_cap;        /* cache queries per launch (paths are launched in chunks) */
@@ -458,6 +460,14 @@ typedef struct {
   int32_t warm_start;       /* 0: a fresh cache (seed); 1: continue from the context's
                                cache (the last cached render's, or tpt_learned_load's),
                                querying it from the first pass */
+  int32_t first_pass_spp;   /* spp of the uncached first pass (8; 0: spp / passes, like
+                               the others); the other passes share the rest */
+  int32_t first_train_steps; /* Adam steps after the first pass (0: train_steps) */
+  float spread_c;           /* > 0: a path also ends into the cache at a diffuse vertex
+                               past the camera hit once its path spread (Mueller et
+                               al. 2021, section 5) exceeds spread_c x the camera
+                               vertex's; terminate_depth stays the latest end (0.01;
+                               0: off) */
 } tpt_nrc_params;
 typedef struct {
   double render_ms, infer_ms, train_ms;

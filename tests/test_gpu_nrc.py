@@ -28,7 +28,8 @@ def test_uncached_nrc_render_equals_plain_tracer(ctx, engine):
     w = h = 24
     k = 6
     a = np.stack([tpt.render_nrc(ctx, slot, w, h, 32, seed=10 + i, passes=2, terminate_depth=1 << 20,
-                                 train_steps=4, batch=1024, engine=engine)[0] for i in range(k)]).astype(np.float64)
+                                 spread_c=0.0, train_steps=4, batch=1024, engine=engine)[0]
+                  for i in range(k)]).astype(np.float64)
     b = np.stack([ctx.render(slot, w, h, 32, semantics=tpt.SEMANTICS_PHYSICAL, seed=200 + i)[0]
                   for i in range(k)]).astype(np.float64)
     ma, mb = a.mean(axis=(1, 2, 3)), b.mean(axis=(1, 2, 3))
@@ -62,6 +63,44 @@ def test_cached_render_gains_at_equal_spp(ctx):
     ctx.release(slot)
 
 
+@pytest.mark.parametrize("engine", [tpt.ENGINE_WAVEFRONT, tpt.ENGINE_PERSISTENT], ids=["wavefront", "persistent"])
+def test_first_pass_has_its_own_spp(ctx, engine):
+    """The uncached first pass takes first_pass_spp samples per pixel and the
+    other passes share the rest, rounded up: 5 + 3 x ceil(27 / 3) = 32."""
+    slot = _slot(ctx)
+    w, h = 40, 24
+    for first, passes, spp, total in ((5, 4, 32, 32), (5, 4, 30, 32), (0, 4, 30, 32), (3, 1, 16, 16)):
+        _, st, _ = tpt.render_nrc(ctx, slot, w, h, spp, passes=passes, first_pass_spp=first, train_steps=2,
+                                  batch=1024, seed=4, engine=engine)
+        assert st["samples"] == w * h * total, (first, passes, spp, st["samples"])
+    ctx.release(slot)
+
+
+@pytest.mark.parametrize("engine", [tpt.ENGINE_WAVEFRONT, tpt.ENGINE_PERSISTENT], ids=["wavefront", "persistent"])
+def test_path_spread_rule_ends_paths_between_the_fixed_depths(ctx, engine):
+    """Paths are a deterministic function of (pixel, sample, depth) draws, so
+    the segment counts order exactly.  The spread rule only adds earlier ends
+    (at diffuse vertices past the camera hit), so with a huge c it never
+    fires (the same segments as with the rule off); with a tiny c it fires
+    after every non-specular bounce, so paths are at least as long as with
+    terminate_depth 1 and at most as long as with the rule off."""
+    slot = _slot(ctx)
+    w = h = 48
+
+    def segs(**kw):
+        return tpt.render_nrc(ctx, slot, w, h, 16, passes=2, first_pass_spp=4, train_steps=2, batch=1024, seed=6,
+                              engine=engine, **kw)[1]["segments"]
+
+    off = segs(terminate_depth=3, spread_c=0.0)
+    assert segs(terminate_depth=3, spread_c=1e30) == off
+    tiny = segs(terminate_depth=3, spread_c=1e-12)
+    one = segs(terminate_depth=1, spread_c=0.0)
+    default = segs(terminate_depth=3, spread_c=0.01)
+    assert one <= tiny <= default <= off, (one, tiny, default, off)
+    assert tiny < off
+    ctx.release(slot)
+
+
 def test_nrc_argument_errors(ctx):
     import ctypes as C
 
@@ -69,7 +108,8 @@ def test_nrc_argument_errors(ctx):
     img = np.zeros((8, 8, 3), np.float32)
     p = tpt.make_params(8, 8, 4, 50, tpt.SEMANTICS_PHYSICAL)
     for field, bad in (("passes", 0), ("terminate_depth", -1), ("train_stride", 0), ("query_cap", 16),
-                       ("batch", 8)):
+                       ("batch", 8), ("first_pass_spp", -1), ("first_train_steps", -1), ("spread_c", -1.0),
+                       ("spread_c", float("nan"))):
         n = tpt.NrcParams()
         tpt.lib().tpt_nrc_params_default(C.byref(n))
         setattr(n, field, bad)

@@ -968,11 +968,39 @@ __device__ __forceinline__ void vertex_info(const DevScene &S, const Ray &ray, c
   }
 }
 
+// Path spread (Mueller et al. 2021, "Real-time Neural Radiance Caching for
+// Path Tracing", section 5): the footprint a(x_1..x_n) = (sum over i >= 2 of
+// sqrt(|x_{i-1} - x_i|^2 / (p(w_i) |cos theta_i|)))^2 of a path grows with
+// its bounces; the path may end into the radiance cache once a exceeds
+// c a_0, where a_0 = |x_0 - x_1|^2 / (4 pi cos theta_1) is the camera
+// vertex's footprint.  Kept as square roots: thr = sqrt(c a_0), sum =
+// sqrt(a).  Specular bounces (metal, dielectric) leave the spread as it is;
+// a medium vertex has no normal (|cos| = 1) and samples 1 / (4 pi).
+struct Spread {
+  float thr;  // sqrt(c) until the camera hit, sqrt(c a_0) after it
+  float sum;  // sqrt(a) of the vertices so far
+  float pdf;  // solid-angle density the last direction was sampled with (0: specular)
+};
+
+__device__ __forceinline__ bool spread_step(Spread &sp, const Ray &ray, const HitRef &h, const Surface &sf,
+                                            bool medium, int depth) {
+  const float dl = length3(ray.d);
+  const float dist = h.t * dl;
+  const float cs = medium ? 1.f : fmaxf(fabsf(dot3(sf.n, ray.d)) / dl, 1e-4f);
+  if (depth == 0) {
+    sp.thr *= dist * rsqrtf(12.566370614359172954f * cs);
+    sp.sum = 0.f;
+    return false;
+  }
+  if (sp.pdf > 0.f) sp.sum += dist * rsqrtf(sp.pdf * cs);
+  return sp.sum > sp.thr;
+}
+
 template <bool GUIDED>
 __device__ bool shade_vertex_t(const DevScene &S, const RenderCfg &cfg, Ray &ray, bool hit, const HitRef &h,
                                float3 &T, float3 &L, int depth, uint32_t pixel, uint32_t sample, const GuideView &gv,
                                GuideRec &rec, VertexInfo *vi = nullptr, int query_depth = 1 << 30,
-                               bool *queried = nullptr) {
+                               bool *queried = nullptr, Spread *sp = nullptr) {
   if (!hit) {
     L = L + T * background(cfg, ray);
     return false;
@@ -988,11 +1016,15 @@ __device__ bool shade_vertex_t(const DevScene &S, const RenderCfg &cfg, Ray &ray
     return false;
   }
   // radiance-cache query: the path ends here at a diffuse vertex (no
-  // emission there) and the cache supplies its outgoing radiance
-  if (queried && depth >= query_depth && (mi.x == MT_LAMBERTIAN || (mi.x == MT_ISOTROPIC && cfg.semantics == 1))) {
+  // emission there) and the cache supplies its outgoing radiance; past
+  // query_depth, or earlier once the path's spread is wide enough
+  const bool spread_end = sp && spread_step(*sp, ray, h, sf, mi.x == MT_ISOTROPIC, depth);
+  if (queried && (depth >= query_depth || spread_end) &&
+      (mi.x == MT_LAMBERTIAN || (mi.x == MT_ISOTROPIC && cfg.semantics == 1))) {
     *queried = true;
     return false;
   }
+  if (sp) sp->pdf = 0.f;  // specular unless a diffuse lobe below samples
   const float4 r = uniforms(make_uint4(pixel, sample, (uint32_t)depth, RNG_SCATTER), cfg.key);
   float3 dir, wgt;
   float time = ray.time;
@@ -1047,6 +1079,7 @@ __device__ bool shade_vertex_t(const DevScene &S, const RenderCfg &cfg, Ray &ray
       dir = in_unit_sphere(r.x, r.y, r.z);
       wgt = tex_value(S, mi.y, sf.u, sf.v, sf.p);
       time = 0.f;  // ray(rec.point, random_in_unit_sphere()) keeps the default time
+      if (sp) sp->pdf = 0.0795774715459476679f;  // a point in the unit ball: uniform direction
       break;
     }
     case MT_LAMBERTIAN: {  // material.cc:3-17 + mixture_pdf (rect_box.h:118-131)
@@ -1073,6 +1106,7 @@ __device__ bool shade_vertex_t(const DevScene &S, const RenderCfg &cfg, Ray &ray
         if (GUIDED && lob) pdf = gv.alpha * guide_pdf(lob, unit3(dir)) + (1.f - gv.alpha) * pdf;
       }
       if (GUIDED && !rec.valid) rec = GuideRec{sf.p, sf.n, unit3(dir), T, L, true};
+      if (sp) sp->pdf = pdf;
       const float cs = dot3(sf.n, unit3(dir));
       const float spdf = cs < 0.f ? 0.f : cs * 0.318309886183790671538f;
       wgt = atten * __fdividef(spdf, pdf);

@@ -258,6 +258,7 @@ struct WfLearn {
   float4 *pend;                       // guided: 5 float4 per recording path; cache: T_k, L_k per record
   unsigned *pend_count;
   int term_depth;                     // cache
+  float spread_sqrt_c;                // cache: sqrt(c) of the path-spread rule (0: off)
   float4 *queries;                    // cache: 6 float4 per query
   unsigned *q_count;
   unsigned q_cap;
@@ -269,10 +270,14 @@ __device__ __forceinline__ bool wf_training(const FrameDesc &F, const WfLearn &W
 }
 // A path's aux.w: the training flag (decided once, when the path is
 // generated: the 64-bit modulo above is too costly per vertex) and, for the
-// cache, the count of its records in the low bits.
+// cache, the count of its records in the low bits.  aux.xyz: a training
+// path's record slots; for the cache's other paths, under the path-spread
+// rule, the Spread state (thr, sum, pdf as float bits).
 enum { AUX_TRAIN = 1 << 8, AUX_COUNT = 0xff };
 __device__ __forceinline__ int4 fresh_aux(const FrameDesc &F, const WfLearn &W, uint32_t pixel, uint32_t sample) {
-  return make_int4(-1, -1, -1, wf_training(F, W, pixel, sample) ? AUX_TRAIN : 0);
+  const bool training = wf_training(F, W, pixel, sample);
+  if (!training && W.spread_sqrt_c > 0.f) return make_int4(__float_as_int(W.spread_sqrt_c), 0, 0, 0);
+  return make_int4(-1, -1, -1, training ? AUX_TRAIN : 0);
 }
 // Path guiding needs only the pending-record slot and the training flag: one
 // int per path instead of the int4 (bits 0-29: slot + 1, bit 30: training),
@@ -354,12 +359,15 @@ __global__ void k_wf_shade_learn(DevScene S, RenderCfg cfg, FrameDesc F, PathBuf
         cont = shade_vertex_t<true>(S, cfg, r, hv.y >= 0, h, T, L, depth, pixel, sample, W.gv, grec);
         new_rec = !had && grec.valid && finite3(grec.x) && finite3(grec.n) && finite3(grec.d);
       } else {
-        const bool may_query = !training && depth >= W.term_depth;
+        const bool spread = !training && W.spread_sqrt_c > 0.f;
+        const bool may_query = !training && (depth >= W.term_depth || spread);
         const bool rec_here = training && hv.y >= 0 && (aux.w & AUX_COUNT) < 3;
         bool queried = false;
+        Spread sp{__int_as_float(aux.x), __int_as_float(aux.y), __int_as_float(aux.z)};
         cont = shade_vertex_t<false>(S, cfg, r, hv.y >= 0, h, T, L, depth, pixel, sample, W.gv, grec,
-                                     (rec_here || may_query) ? &vi : nullptr, may_query ? W.term_depth : (1 << 30),
-                                     &queried);
+                                     (rec_here || may_query) ? &vi : nullptr, training ? (1 << 30) : W.term_depth,
+                                     &queried, spread ? &sp : nullptr);
+        if (spread) aux = make_int4(__float_as_int(sp.thr), __float_as_int(sp.sum), __float_as_int(sp.pdf), aux.w);
         want_q = queried;
         want_r = !queried && rec_here && (vi.kind == MT_LAMBERTIAN || vi.kind == MT_ISOTROPIC);
       }
@@ -882,7 +890,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
     k_persistent_nrc(DevScene S, RenderCfg cfg, FrameDesc F, WfCounters *C, unsigned long long sample_offset,
                      int term_depth, uint32_t train_stride, float4 *__restrict__ records, unsigned *rec_count,
                      unsigned rec_cap, float4 *__restrict__ queries, unsigned *q_count, unsigned q_cap,
-                     float4 *__restrict__ pend) {
+                     float4 *__restrict__ pend, float spread_sqrt_c) {
   extern __shared__ int2 stack_smem[];
   int2 *stk = stack_smem + threadIdx.x;
   int e = 0;
@@ -893,6 +901,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
   uint32_t pixel = 0, sample = 0;
   int depth = 0;
   int4 rslot = make_int4(-1, -1, -1, 0);  // record slots, count in .w
+  Spread sp{};
   GuideView gv{};
   GuideRec grec{};
   for (;;) {
@@ -912,6 +921,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
           depth = 0;
           training = ((s + sample_offset) % train_stride) == 0;
           rslot = make_int4(-1, -1, -1, 0);
+          sp = Spread{spread_sqrt_c, 0.f, 0.f};
           alive = true;
         } else {
           done = true;
@@ -927,12 +937,13 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
       HitRef h;
       const bool hit = trace_closest(S, r, 0.001f, stk, blockDim.x, m, h, e);
       segs++;
-      const bool may_query = !training && depth >= term_depth;
+      const bool spread = !training && spread_sqrt_c > 0.f;
+      const bool may_query = !training && (depth >= term_depth || spread);
       const bool rec_here = training && hit && rslot.w < 3;
       bool queried = false;
       const bool cont = shade_vertex_t<false>(S, cfg, r, hit, h, T, L, depth, pixel, sample, gv, grec,
                                               (rec_here || may_query) ? &vi : nullptr,
-                                              may_query ? term_depth : (1 << 30), &queried);
+                                              training ? (1 << 30) : term_depth, &queried, spread ? &sp : nullptr);
       if (queried) {  // ends at a diffuse vertex: the cache adds T x radiance
         want_q = true;
         accumulate(F, pixel, L);
@@ -2341,16 +2352,19 @@ extern "C" tpt_status tpt_guide_records(tpt_context *c, float *out, int64_t cap,
 
 extern "C" void tpt_nrc_params_default(tpt_nrc_params *n) {
   if (!n) return;
-  n->passes = 8;
-  n->train_steps = 256;
+  n->passes = 4;
+  n->train_steps = 512;
   n->batch = 16384;
   n->lr = 3e-3f;
-  n->terminate_depth = 2;
+  n->terminate_depth = 3;
   n->train_stride = 16;
   n->record_cap = 1 << 20;
   n->query_cap = 1 << 22;
   n->seed = 1;
   n->warm_start = 0;
+  n->first_pass_spp = 8;
+  n->first_train_steps = 0;
+  n->spread_c = 0.01f;
 }
 
 extern "C" tpt_status tpt_learned_save(tpt_context *c, int32_t which, float *out, int64_t cap, int64_t *count) {
@@ -2393,17 +2407,26 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
   if (!c || !p || !n || !out_rgb) return TPT_ERR_INVALID_ARGUMENT;
   if (slot < 0 || slot >= (int32_t)c->slots.size() || !c->slots[slot].live) return TPT_ERR_BAD_HANDLE;
   if (p->width <= 0 || p->height <= 0 || p->spp <= 0 || p->max_depth < 0 || n->passes < 1 ||
-      n->terminate_depth < 0 || n->train_stride < 1 || n->record_cap < 16 || n->query_cap < 1024 || n->batch < 16)
+      n->terminate_depth < 0 || n->train_stride < 1 || n->record_cap < 16 || n->query_cap < 1024 || n->batch < 16 ||
+      n->first_pass_spp < 0 || n->first_train_steps < 0 || !(n->spread_c >= 0.f))
     return TPT_ERR_INVALID_ARGUMENT;
   TPT_CUDA(cudaSetDevice(c->device));
   const Slot &sl = c->slots[slot];
   const unsigned long long npix = (unsigned long long)p->width * p->height;
-  const int spp_pass = (p->spp + n->passes - 1) / n->passes;
-  const int spp_total = spp_pass * n->passes;
   tpt_status st;
   // a fresh cache for every render (reproducible online training), unless
   // warm_start continues from the context's cache
   const bool warm = n->warm_start != 0 && c->cache != nullptr;
+  // samples per pass: the uncached first pass may have its own size, the
+  // other passes share the rest (rounded up, so the frame has >= spp)
+  int spp_pass = (p->spp + n->passes - 1) / n->passes;
+  int spp_first = spp_pass;
+  if (!warm && n->first_pass_spp > 0 && n->passes > 1) {
+    spp_first = std::min(n->first_pass_spp, p->spp);
+    spp_pass = std::max(1, (p->spp - spp_first + n->passes - 2) / (n->passes - 1));
+  }
+  const int spp_total = spp_first + spp_pass * (n->passes - 1);
+  const float sqrt_c = std::sqrt(n->spread_c);
   if (!warm) {
     cache_destroy(c->cache);
     c->cache = nullptr;
@@ -2451,8 +2474,9 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
     const bool cached = pass > 0 || warm;  // a continued cache is queried from the first pass
     const int term = cached ? n->terminate_depth : (1 << 30);
     cudaMemsetAsync(counts, 0, sizeof(unsigned), c->stream);  // records of this pass
-    const unsigned long long pass_begin = (unsigned long long)pass * spp_pass * npix;
-    const unsigned long long pass_total = (unsigned long long)spp_pass * npix;
+    const unsigned long long pass_begin =
+        pass == 0 ? 0ull : ((unsigned long long)spp_first + (unsigned long long)(pass - 1) * spp_pass) * npix;
+    const unsigned long long pass_total = (unsigned long long)(pass == 0 ? spp_first : spp_pass) * npix;
     for (unsigned long long off = 0; off < pass_total && result == TPT_OK; off += chunk) {
       const unsigned long long cnt = std::min(chunk, pass_total - off);
       FrameDesc Fc = F;
@@ -2468,6 +2492,7 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
         W.rec_cap = (unsigned)n->record_cap;
         W.pend = (float4 *)c->learn_pend.p;
         W.term_depth = term;
+        W.spread_sqrt_c = cached ? sqrt_c : 0.f;
         W.queries = (float4 *)c->nrc_queries.p;
         W.q_count = counts + 1;
         W.q_cap = (unsigned)n->query_cap;
@@ -2481,7 +2506,8 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
         kern<<<grid, block, smem, c->stream>>>(S, cfg, Fc, c->counters, pass_begin + off, term,
                                               (uint32_t)n->train_stride, (float4 *)c->nrc_records.p, counts,
                                               (unsigned)n->record_cap, (float4 *)c->nrc_queries.p, counts + 1,
-                                              (unsigned)n->query_cap, (float4 *)c->learn_pend.p);
+                                              (unsigned)n->query_cap, (float4 *)c->learn_pend.p,
+                                              cached ? sqrt_c : 0.f);
       }
       cudaEventRecord(ev[1], c->stream);
       unsigned q = 0;
@@ -2531,7 +2557,8 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
     n_rec += nr;
     if (pass + 1 < n->passes && nr > 0) {
       cudaEventRecord(ev[4], c->stream);
-      result = cache_train(c->cache, (const float4 *)c->nrc_records.p, (int)nr, n->train_steps, n->batch, n->lr, lo,
+      const int steps = pass == 0 && n->first_train_steps > 0 ? n->first_train_steps : n->train_steps;
+      result = cache_train(c->cache, (const float4 *)c->nrc_records.p, (int)nr, steps, n->batch, n->lr, lo,
                            ext, (uint32_t)(n->seed * 2654435761ull + pass), c->stream);
       if (result != TPT_OK) break;
       cudaEventRecord(ev[5], c->stream);

@@ -90,7 +90,8 @@ class GuideStats(C.Structure):
 class NrcParams(C.Structure):
     _fields_ = [("passes", C.c_int32), ("train_steps", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float),
                 ("terminate_depth", C.c_int32), ("train_stride", C.c_int32), ("record_cap", C.c_int32),
-                ("query_cap", C.c_int32), ("seed", C.c_uint64), ("warm_start", C.c_int32)]
+                ("query_cap", C.c_int32), ("seed", C.c_uint64), ("warm_start", C.c_int32),
+                ("first_pass_spp", C.c_int32), ("first_train_steps", C.c_int32), ("spread_c", C.c_float)]
 
 
 class NrcStats(C.Structure):
