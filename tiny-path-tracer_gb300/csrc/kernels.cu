@@ -620,9 +620,12 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
 // claim new camera samples, and start their next walks.  The walk visits the
 // same nodes with the same tests, pruning and tie order as trace_closest's
 // stack walk (a node's children: boxes by the slab test, sphere leaves by the
-// reference's quadratic, inline in the node's record), so every sample's
-// radiance is the same; a scene that is not one top-level BVH item takes
-// trace_closest for its segments.
+// reference's quadratic, inline in the node's record), so every segment
+// finds the same closest hit; the shading arithmetic is the same source, but
+// the compiler contracts multiply-adds differently in each kernel, so a
+// sample's radiance can differ in the last bits (and, where such a bit flips
+// a scatter decision, the rest of that path).  A scene that is not one
+// top-level BVH item takes trace_closest for its segments.
 enum { STEP_NODES = 6 };
 enum { LANE_IDLE = 0, LANE_WALK = 1, LANE_READY = 2, LANE_DONE = 3 };
 
