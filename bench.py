@@ -17,8 +17,9 @@ cpu_baseline / --impl reference: the reference algorithm on the host cores
         (oracle/_ref linked from the reference sources when it was built here,
         else the CPU oracle port), on a bounded band of image rows.
 learned_equal_time: the second half of the metric - relMSE against an FP64
-        high-spp render of the learned renderers (path guiding on the small-
-        light Cornell box, the radiance cache on the next-week scene) next to
+        high-spp render of the learned renderers (path guiding and the
+        radiance cache on the small-light Cornell box, the radiance cache on
+        the next-week scene) next to
         the plain tracer: at equal spp, at equal wall time, and the wall time
         each needs to reach the plain tracer's relMSE (skip with
         --no-learned).
@@ -448,8 +449,13 @@ def learned_equal_time(ctx, which: str) -> dict:
             cached renderer at its default settings (an uncached 8-spp first
             pass, then paths end into the cache by the path-spread rule,
             c = 0.01, at the third bounce at the latest; 512 Adam steps after
-            each of the 4 passes) at the spp that takes the same time; FP64
-            reference 4096 spp.
+            each of the first 2 of 3 passes) at the spp that takes the same
+            time; FP64 reference 4096 spp.
+    nrc_cornell: the cached renderer on the guided configuration's Cornell
+            box (40x40 light, second box), 600x600, plain at 1024 spp; FP64
+            reference 16384 spp.
+    The cached renders run on the engine tpt_autotune_nrc picks for the
+    scene (timed before, like the plain tracer's autotune).
     Every point (plain, learned at equal spp, at equal time, and the points
     of the time-to-plain-relMSE search) is the mean over three seeds (each
     learned run trains its own network online; per-seed values are reported
@@ -465,12 +471,16 @@ def learned_equal_time(ctx, which: str) -> dict:
         sd, w, h, spp, ref_spp = scenes.cornell_guiding(), 600, 600, 1024, 16384
         run = lambda n, out, sd_: tpt.render_guided(ctx, slot, w, h, n, seed=sd_, out=out)
     else:
-        sd, w, h, spp, ref_spp = scenes.next_week(), 800, 800, 256, 4096
+        if which == "nrc_cornell":
+            sd, w, h, spp, ref_spp = scenes.cornell_guiding(), 600, 600, 1024, 16384
+        else:
+            sd, w, h, spp, ref_spp = scenes.next_week(), 800, 800, 256, 4096
         run = lambda n, out, sd_: tpt.render_nrc(ctx, slot, w, h, n, seed=sd_, out=out)
     slot = ctx.upload(tpt.Scene(sd.text()))
     # both sides use the engine the autotuner picks for this scene (physical
     # semantics): the plain baseline is the tracer's best configuration
     tuned = tpt.autotune(ctx, slot, w, h, 4, semantics=tpt.SEMANTICS_PHYSICAL)
+    cache_engine = tpt.autotune_nrc(ctx, slot, w, h) if which != "guided" else None
     dev = torch.empty((h, w, 3), dtype=torch.float32, device="cuda")
 
     def timed(fn):
@@ -564,10 +574,12 @@ def learned_equal_time(ctx, which: str) -> dict:
     plain_rec = {"spp": spp, "ms": t_plain, "relmse": e_plain, "seeds": list(seeds),
                  "ms_per_seed": t_p, "relmse_per_seed": e_p}
     ctx.release(slot)
-    name = "cornell_40x40_light_two_boxes" if which == "guided" else "next_week_final_seeded"
-    return {"scene": name, "width": w, "height": h, "ref_spp_fp64": ref_spp,
-            "engine": ["auto", "wavefront", "persistent"][tuned[0]],
-            "plain": plain_rec, which: eq, which + "_equal_time": et, **ratios, **extra}
+    name = "next_week_final_seeded" if which == "nrc" else "cornell_40x40_light_two_boxes"
+    engines = ["auto", "wavefront", "persistent"]
+    rec = {"scene": name, "width": w, "height": h, "ref_spp_fp64": ref_spp, "engine": engines[tuned[0]]}
+    if cache_engine is not None:
+        rec["cache_engine"] = engines[cache_engine]
+    return {**rec, "plain": plain_rec, which: eq, which + "_equal_time": et, **ratios, **extra}
 
 
 def main() -> None:
@@ -695,7 +707,7 @@ def main() -> None:
     learned = None
     if rank == 0 and not args.no_learned and args.spp == SPP:
         learned = {}
-        for which in ("guided", "nrc"):
+        for which in ("guided", "nrc", "nrc_cornell"):
             try:
                 learned[which] = learned_equal_time(ctx, which)
             except Exception as e:  # reported, never fatal to the throughput line

@@ -384,6 +384,15 @@ tpt_status tpt_guide_encode(const float *records, int64_t count, const float *lo
                             float *target, void *stream);
 tpt_status tpt_nrc_encode(const float *records, int64_t count, int32_t stride, const float *lo, const float *extent,
                           void *x_f16, void *stream);
+/* Radiance-cache network only: the cached renderer's query evaluation.
+ * queries: device, 6 float4 each - the four feature float4 of
+ * tpt_nrc_encode, then (throughput rgb, pixel index as int32 bits), then
+ * unused; accum: device, one float4 per pixel.  For every query, encodes
+ * its features (box [lo, lo + extent]), evaluates the network on the
+ * tensor cores and adds throughput x max(output rgb, 0) (NaN components as
+ * 0) to accum[pixel].xyz, in one kernel. */
+tpt_status tpt_mlp_cache_accumulate(tpt_mlp *m, const float *queries, int64_t count, const float *lo,
+                                    const float *extent, float *accum, void *stream);
 /* Adam step (lr, beta 0.9/0.999, eps 1e-8) on the accumulated gradient
  * multiplied by inv_loss_scale; clears the gradient. */
 tpt_status tpt_mlp_adam(tpt_mlp *m, float lr, float inv_loss_scale, void *stream);
@@ -448,7 +457,7 @@ tpt_status tpt_guide_records(tpt_context *ctx, float *out, int64_t cap, int64_t 
  * The estimator is biased by the cache's error; the plain tracer is its
  * fallback and the yardstick for that error.  Defaults in parentheses. */
 typedef struct {
-  int32_t passes;           /* >= 1 (4) */
+  int32_t passes;           /* >= 1 (3) */
   int32_t train_steps;      /* Adam steps after each pass (512) */
   int32_t batch;            /* training rows per step (16384) */
   float lr;                 /* Adam learning rate (3e-3) */
@@ -475,6 +484,15 @@ typedef struct {
   int64_t records, queries;
 } tpt_nrc_stats;
 void tpt_nrc_params_default(tpt_nrc_params *n);
+/* Chooses the engine of the slot's cached renders (TPT_ENGINE_AUTO): traces
+ * a short cached render of p's size and settings (probe_spp >= 2 samples per
+ * pixel, an untrained cache) on each engine and keeps the one with the
+ * shorter tracing time (*engine_out, may be NULL).  The cache's own
+ * training and inference cost the same on both engines.  The probes render
+ * with fresh caches, so the context's cache is replaced (load a checkpoint
+ * for a warm start afterwards). */
+tpt_status tpt_autotune_nrc(tpt_context *ctx, int32_t slot, const tpt_render_params *p, int32_t probe_spp,
+                            int32_t *engine_out);
 tpt_status tpt_render_nrc(tpt_context *ctx, int32_t slot, const tpt_render_params *p, const tpt_nrc_params *n,
                           float *out_rgb, int32_t mem, tpt_render_stats *stats, tpt_nrc_stats *nstats);
 

@@ -162,6 +162,43 @@ def test_nrc_encoder_matches_reference(built):
     assert d.max() <= 2.0 ** -11 and (d > 0).mean() < 1e-3, (d.max(), (d > 0).mean())
 
 
+def test_cache_query_accumulate_matches_reference(built):
+    """The cached renderer's query evaluation (one tcgen05 kernel: encode,
+    forward, throughput x max(cache, 0) added to the pixel's sum) against the
+    float64 reference of the same steps (mlp_ref.nrc_encode, mlp_ref.forward),
+    with queries colliding on pixels and some non-finite features; a count
+    that is not a multiple of the 128-row tile."""
+    import torch
+
+    net = tpt.Mlp(64, 5, 16, seed=7)
+    p16 = net.get_params().astype(np.float16).astype(np.float32)
+    n, npix = 50_001, 3_000
+    rec = _records(n, 4, 5)
+    rng = np.random.default_rng(9)
+    q = np.zeros((n, 6, 4), np.float32)
+    q[:, :4] = rec[:, :4]
+    q[:, 4, :3] = rng.uniform(0, 2, size=(n, 3))
+    pix = rng.integers(0, npix, size=n).astype(np.int32)
+    q[:, 4, 3] = pix.view(np.float32)
+    acc0 = rng.uniform(0, 1, size=(npix, 4)).astype(np.float32)
+    qd = torch.from_numpy(q.reshape(n, 24)).cuda()
+    ad = torch.from_numpy(acc0.copy()).cuda()
+    torch.cuda.synchronize()
+    net.cache_accumulate(qd.data_ptr(), n, LO, EXT, ad.data_ptr())
+    torch.cuda.synchronize()
+    acc = ad.cpu().numpy().astype(np.float64)
+    y, _ = mlp_ref.forward(p16, mlp_ref.nrc_encode(q, LO, EXT).astype(np.float64), 64, 5, 16)
+    L = q[:, 4, :3].astype(np.float64) * np.maximum(y[:, :3], 0.0)
+    L = np.where(np.isnan(L), 0.0, L)
+    ref = acc0.astype(np.float64)
+    np.add.at(ref[:, :3], pix, L)
+    assert np.array_equal(acc[:, 3], acc0[:, 3])  # w untouched
+    err = np.abs(acc[:, :3] - ref[:, :3])
+    scale = np.abs(ref[:, :3] - acc0[:, :3]).max()
+    print("cache accumulate", err.max() / scale)
+    assert err.max() < FWD_RTOL * scale, (err.max(), scale)
+
+
 def test_guide_encoder_matches_reference(built):
     """The guide's input encoding and loss targets (learn.cu
     guide_record_row) against mlp_ref.guide_encode: bit-identical, unusable

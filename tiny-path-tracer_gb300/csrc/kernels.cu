@@ -1007,17 +1007,6 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS)
   if (e) atomicExch(&C->err, e);
 }
 
-// accum[pixel] += de_nan(throughput * max(cache, 0)) for every query.
-__global__ void k_nrc_accumulate(const float4 *__restrict__ queries, const float *__restrict__ y, int count,
-                                 FrameDesc F) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-    const float4 tq = queries[6 * (size_t)i + 4];
-    const float *c = y + (size_t)i * 16;
-    const float3 L = de_nan(v3(tq.x * fmaxf(c[0], 0.f), tq.y * fmaxf(c[1], 0.f), tq.z * fmaxf(c[2], 0.f)));
-    accumulate(F, (uint32_t)__float_as_int(tq.w), L);
-  }
-}
-
 // mean = sum / spp, image order (row 0 = top).
 __global__ void k_resolve(FrameDesc F, float *__restrict__ out) {
   const long long npix = (long long)F.nx * F.ny;
@@ -1051,6 +1040,7 @@ struct Slot {
   bool live = false;
   bool tuned = false;        // tpt_autotune result for engine = AUTO
   tpt_render_params tp{};
+  int cache_engine = 0;      // tpt_autotune_nrc result for cached renders (0: none)
   float world_lo[3] = {0, 0, 0}, world_hi[3] = {0, 0, 0};
 };
 
@@ -2355,7 +2345,7 @@ extern "C" tpt_status tpt_guide_records(tpt_context *c, float *out, int64_t cap,
 
 extern "C" void tpt_nrc_params_default(tpt_nrc_params *n) {
   if (!n) return;
-  n->passes = 4;
+  n->passes = 3;
   n->train_steps = 512;
   n->batch = 16384;
   n->lr = 3e-3f;
@@ -2447,7 +2437,7 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
   S.flat_max = p->flat_nodes > 0 ? p->flat_nodes : c->flat_nodes;
   const RenderCfg cfg{p->max_depth, p->semantics, p->background, p->sky_scale,
                       make_uint2((uint32_t)p->seed, (uint32_t)(p->seed >> 32)), p->refill > 0 ? p->refill : 1};
-  const int engine = learned_engine(p, sl);
+  const int engine = p->engine == TPT_ENGINE_AUTO && sl.cache_engine ? sl.cache_engine : learned_engine(p, sl);
   const bool wf = engine == TPT_ENGINE_WAVEFRONT;
   const int wf_block =
       p->block > 0 ? p->block : (sl.tuned && sl.tp.engine == TPT_ENGINE_WAVEFRONT ? sl.tp.block : 128);
@@ -2534,11 +2524,8 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
       n_q += q;
       if (q > 0) {
         cudaEventRecord(ev[2], c->stream);
-        const float *y = nullptr;
-        result = cache_infer(c->cache, (const float4 *)c->nrc_queries.p, (int)q, lo, ext, &y, c->stream);
+        result = cache_infer(c->cache, (const float4 *)c->nrc_queries.p, (int)q, lo, ext, F.accum, c->stream);
         if (result != TPT_OK) break;
-        const int g2 = (int)std::min<unsigned>((q + 255) / 256, (unsigned)c->sm_count * 16);
-        k_nrc_accumulate<<<g2, 256, 0, c->stream>>>((const float4 *)c->nrc_queries.p, y, (int)q, F);
         cudaEventRecord(ev[3], c->stream);
         if ((ce = cudaStreamSynchronize(c->stream)) != cudaSuccess) {
           result = cuda_status(ce);
@@ -2575,6 +2562,7 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
     }
   }
   for (auto &x : ev) cudaEventDestroy(x);
+  if (result == TPT_OK) result = cache_check(c->cache, c->stream);
   if (result != TPT_OK) return result;
   FrameDesc R = F;
   R.spp = spp_total;
@@ -2604,6 +2592,47 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
     nstats->records = n_rec;
     nstats->queries = n_q;
   }
+  return TPT_OK;
+}
+
+// The engine of the slot's cached renders: each engine traces a short
+// cached render (an untrained cache: the paths' lengths and the queries do
+// not depend on the weights, and training and inference cost the same on
+// both engines), the faster by render time is kept for TPT_ENGINE_AUTO.
+extern "C" tpt_status tpt_autotune_nrc(tpt_context *c, int32_t slot, const tpt_render_params *p, int32_t probe_spp,
+                                       int32_t *engine_out) {
+  if (!c || !p || probe_spp < 2 || p->width <= 0 || p->height <= 0) return TPT_ERR_INVALID_ARGUMENT;
+  if (slot < 0 || slot >= (int32_t)c->slots.size() || !c->slots[slot].live) return TPT_ERR_BAD_HANDLE;
+  tpt_nrc_params n;
+  tpt_nrc_params_default(&n);
+  n.passes = 2;
+  n.first_pass_spp = 1;
+  n.train_steps = 0;
+  const size_t npix = (size_t)p->width * p->height;
+  tpt_status st;
+  if ((st = ensure(c->staging, npix * 3 * sizeof(float))) != TPT_OK) return st;
+  int best = TPT_ENGINE_WAVEFRONT;
+  double best_ms = 1e30;
+  for (int engine : {TPT_ENGINE_WAVEFRONT, TPT_ENGINE_PERSISTENT}) {
+    tpt_render_params q = *p;
+    q.engine = engine;
+    q.spp = probe_spp;
+    q.profile = 0;
+    q.accumulate_fp64 = 0;
+    double ms = 1e30;
+    for (int rep = 0; rep < 3; rep++) {  // the first run warms caches and allocations
+      tpt_nrc_stats ns;
+      if ((st = tpt_render_nrc(c, slot, &q, &n, (float *)c->staging.p, TPT_MEM_DEVICE, nullptr, &ns)) != TPT_OK)
+        return st;
+      if (rep > 0) ms = std::min(ms, ns.render_ms);
+    }
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = engine;
+    }
+  }
+  c->slots[slot].cache_engine = best;
+  if (engine_out) *engine_out = best;
   return TPT_OK;
 }
 

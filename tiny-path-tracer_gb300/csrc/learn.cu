@@ -8,8 +8,10 @@
 //                   weight-gradient sums to the f32 gradient);
 //   k_adam          Adam on f32 master weights, refreshing the f16 copy and
 //                   the training kernel's swizzled weight image.
-// Inference (k_mlp_forward) keeps register-resident mma.sync chains: 16 rows
-// per warp, no tensor-memory round trip between layers.
+//   k_mlp_infer_tc  the forward pass alone, on tcgen05, many tiles per CTA;
+//                   for the cache it encodes the queries itself and adds
+//                   throughput x radiance to the pixel sums (no input or
+//                   output matrix in memory).
 // Shapes are template parameters: <IN, NH, OUT> with hidden width 64.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -247,7 +249,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       fence_async_smem();
     }
     if (issuer && !weights) weights = ok = bar_wait(barL, 0, TC_WAIT_LIMIT);  // overlapped with the first tile's copies
-    if (!__syncthreads_and(ok)) break;
+    if (!(ok = __syncthreads_and(ok))) break;  // every thread leaves together
     // ---- forward (loops rolled: each CTA runs its body for a tile or two,
     // so a compact body keeps instruction fetch off the critical path)
 #pragma unroll 1
@@ -304,7 +306,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         fence_async_smem();
         fence_before();
       }
-      if (!__syncthreads_and(ok)) break;
+      if (!(ok = __syncthreads_and(ok))) break;  // every thread leaves together
     }
     if (!ok) break;
     // ---- backward, step l = NH .. 0: the issuer launches dH_l (critical
@@ -366,7 +368,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
       // step 0: dW_2's phase of barW[0] (if any) is consumed here
       if (l == 0 && NH >= 2 && rows_warp) wait_rows(barW0, phW0);
-      if (!__syncthreads_and(ok)) break;
+      if (!(ok = __syncthreads_and(ok))) break;  // every thread leaves together
     }
     if (!ok) break;
     // dW_1 and dW_0 (barA) read X, H_1 and two dZ tiles: complete before the
@@ -422,6 +424,145 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   __syncthreads();
   if (warp == 0) tmem_free(tm, T::TMEM_COLS);
 }
+
+// ------------------------------------------------- inference (tcgen05) ---
+// The forward pass alone, for many 128-row tiles per CTA: warps 0-3 own the
+// rows and tensor-memory lanes (thread t: row t of the tile), the first
+// thread of warp 4 issues the MMAs (M = 128, f32 accumulator in 64 tensor-
+// memory columns), the weights arrive by one bulk copy of the weight image.
+// Activations ping-pong between two tiles: X and H_2, H_4 .. in tile A,
+// H_1, H_3 .. in tile B; layer l reads one and its epilogue writes H_{l+1}
+// into the other, whose last reader (layer l - 1's MMAs) has completed.
+// Two CTAs share an SM, so one CTA's MMAs overlap the other's loads and
+// epilogues.  Io builds row t of the input tile (load, returning what
+// store needs) and takes row t's f32 outputs (store).
+template <int IN, int NH, int OUT>
+struct InferLayout {
+  using T = TrainLayout<IN, NH, OUT>;
+  static constexpr uint32_t A_OFF = T::W_BYTES;              // X (KB0 blocks), H_2, H_4 ...
+  static constexpr uint32_t B_OFF = A_OFF + T::KB0 * 16384;  // H_1, H_3 ...
+  static constexpr uint32_t BAR_OFF = B_OFF + 16384;
+  static constexpr uint32_t SMEM = BAR_OFF + 64 + 1024;      // + slack for the 1024-byte alignment
+  static constexpr uint32_t TMEM_COLS = 64;
+  static_assert(A_OFF % 1024 == 0, "operand tiles start on 1024-byte boundaries");
+  static_assert(2 * (SMEM + 1024) <= 228 * 1024, "two CTAs per SM");
+};
+
+template <int IN, int NH, int OUT, class Io>
+__global__ void __launch_bounds__(TC_THREADS, 2)
+    k_mlp_infer_tc(const uint8_t *__restrict__ wimg, int rows, Io io, int *err) {
+  using T = TrainLayout<IN, NH, OUT>;
+  using I = InferLayout<IN, NH, OUT>;
+  using namespace tc05;
+  extern __shared__ uint8_t tc_raw[];
+  uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~uintptr_t(1023));
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + I::BAR_OFF + 16);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const bool rows_warp = warp < 4;
+  const bool issuer = warp == 4 && lane == 0;
+  const uint32_t base = smem_addr(sm);
+  const uint32_t barA = base + I::BAR_OFF, barL = barA + 8;  // MMA completions; the weight image
+  uint32_t phA = 0;
+  bool ok = true;
+  if (issuer) {
+    bar_init(barA, 1);
+    bar_init(barL, 1);
+    bar_expect_bytes(barL, T::W_BYTES);
+    for (uint32_t o = 0; o < T::W_BYTES; o += 16384)
+      bulk_copy(base + o, wimg + o, T::W_BYTES - o < 16384 ? T::W_BYTES - o : 16384, barL);
+  }
+  if (warp == 0) tmem_alloc(tslot, I::TMEM_COLS);
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tm = *tslot;
+  const uint32_t lane_base = tm + ((uint32_t)((warp & 3) * 32) << 16);
+  bool weights = false;  // the issuer has seen the weight image arrive
+  const uint64_t dA = desc(base + I::A_OFF, 16, 1024), dB = desc(base + I::B_OFF, 16, 1024);
+  const uint64_t dW = desc(base, 16, 1024);
+  const int n_tiles = (rows + 127) / 128;
+  for (int tile = blockIdx.x; ok && tile < n_tiles; tile += gridDim.x) {
+    const int r0 = tile * 128;
+    typename Io::Pre pre{};
+    if (rows_warp) {
+      pre = io.load(r0 + t, r0 + t < rows, sm + I::A_OFF, t);
+      fence_async_smem();
+    }
+    if (issuer && !weights) weights = ok = bar_wait(barL, 0, TC_WAIT_LIMIT);  // overlapped with the first loads
+    if (!(ok = __syncthreads_and(ok))) break;  // every thread leaves together
+#pragma unroll 1
+    for (int l = 0; l <= NH; l++) {
+      if (issuer) {
+        fence_after();
+        const uint64_t a0 = (l & 1) ? dB : dA;
+        const uint64_t b0 = desc_add(dW, T::w_off(l));
+        const uint32_t id = idesc_f16(128, T::out_(l), false, false);
+        const uint32_t bstride = T::out_(l) * 128;  // between the weight tile's 64-input blocks
+#pragma unroll 1
+        for (int s = 0; s < T::in_(l) / 16; s++)
+          mma_f16(tm, desc_add(a0, (uint32_t)(s >> 2) * 16384 + (uint32_t)(s & 3) * 32),
+                  desc_add(b0, (uint32_t)(s >> 2) * bstride + (uint32_t)(s & 3) * 32), id, s > 0);
+        commit(barA);
+      }
+      if (rows_warp) {
+        const bool got = __all_sync(0xffffffffu, bar_wait(barA, phA, TC_WAIT_LIMIT));
+        phA ^= 1;
+        ok = ok && got;
+        if (got) {
+          fence_after();
+          float v[64];
+          tmem_ld64(lane_base, v);
+          if (l < NH) {  // ReLU, f16: row t of H_{l+1}
+            uint8_t *dst = sm + (((l + 1) & 1) ? I::B_OFF : I::A_OFF);
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+              uint4 q;
+              q.x = pack2(fmaxf(v[8 * c], 0.f), fmaxf(v[8 * c + 1], 0.f));
+              q.y = pack2(fmaxf(v[8 * c + 2], 0.f), fmaxf(v[8 * c + 3], 0.f));
+              q.z = pack2(fmaxf(v[8 * c + 4], 0.f), fmaxf(v[8 * c + 5], 0.f));
+              q.w = pack2(fmaxf(v[8 * c + 6], 0.f), fmaxf(v[8 * c + 7], 0.f));
+              *reinterpret_cast<uint4 *>(dst + sw128_chunk(t, c)) = q;
+            }
+            fence_async_smem();
+          } else {
+            io.store(r0 + t, r0 + t < rows, v, pre);
+          }
+          fence_before();
+        }
+      }
+      if (!(ok = __syncthreads_and(ok))) break;  // every thread leaves together
+    }
+  }
+  // a CTA that stopped early still lets the weight copy land before it exits
+  if (issuer && !weights) bar_wait(barL, 0, TC_WAIT_LIMIT);
+  if (!ok && t == 0) atomicExch(err, 1);
+  fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_free(tm, I::TMEM_COLS);
+}
+
+// Rows of an f16 input matrix X (rows x IN) in, f32 outputs Y (rows x OUT)
+// out: the plain forward pass.
+template <int IN, int OUT>
+struct MatrixIo {
+  const __half *X;
+  float *Y;
+  using Pre = int;
+  __device__ Pre load(int row, bool valid, uint8_t *xtile, int t) const {
+#pragma unroll
+    for (int k8 = 0; k8 < IN / 8; k8++)
+      tc05::cp_async16(xtile + (uint32_t)(k8 / 8) * 16384 + tc05::sw128_chunk(t, k8 % 8),
+                       X + (size_t)(valid ? row : 0) * IN + k8 * 8, valid ? 16 : 0);
+    tc05::cp_async_wait_all();
+    return 0;
+  }
+  __device__ void store(int row, bool valid, const float *v, Pre) const {
+    if (!valid) return;
+    float4 *y = reinterpret_cast<float4 *>(Y + (size_t)row * OUT);
+#pragma unroll
+    for (int o = 0; o < OUT / 4; o++) y[o] = make_float4(v[4 * o], v[4 * o + 1], v[4 * o + 2], v[4 * o + 3]);
+  }
+};
 
 // The weight image the training kernel copies: every f16 weight at its
 // swizzled position (after set_params / load_state; Adam keeps it current).
@@ -820,6 +961,38 @@ __global__ void k_nrc_encode_rows(const float4 *__restrict__ rec, int count, int
   }
 }
 
+// The cache's queries in (6 float4 each: the vertex features nrc_encode
+// reads, then throughput and pixel), throughput x max(cache, 0) out, added
+// to the pixel's f32 sum (NaN components as 0, like de_nan).
+struct CacheQueryIo {
+  const float4 *q;
+  float3 lo, inv_ext;
+  float4 *accum;
+  using Pre = float4;
+  __device__ Pre load(int row, bool valid, uint8_t *xtile, int t) const {
+    __align__(16) __half x[NRC_IN];
+    float4 tq = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid) {
+      nrc_encode(q + 6 * (size_t)row, lo, inv_ext, x);
+      tq = q[6 * (size_t)row + 4];
+    } else {
+#pragma unroll
+      for (int i = 0; i < NRC_IN; i++) x[i] = __float2half_rn(0.f);
+    }
+#pragma unroll
+    for (int c = 0; c < NRC_IN / 8; c++)
+      *reinterpret_cast<uint4 *>(xtile + tc05::sw128_chunk(t, c)) = reinterpret_cast<const uint4 *>(x)[c];
+    return tq;
+  }
+  __device__ void store(int, bool valid, const float *v, Pre tq) const {
+    if (!valid) return;
+    float L[3] = {tq.x * fmaxf(v[0], 0.f), tq.y * fmaxf(v[1], 0.f), tq.z * fmaxf(v[2], 0.f)};
+#pragma unroll
+    for (int c = 0; c < 3; c++) L[c] = isnan(L[c]) ? 0.f : L[c];
+    tc05::red_add_v4(reinterpret_cast<float *>(accum + __float_as_int(tq.w)), make_float4(L[0], L[1], L[2], 0.f));
+  }
+};
+
 __global__ void k_nrc_encode_queries(const float4 *__restrict__ q, int count, int rows, float3 lo, float3 inv_ext,
                                      __half *__restrict__ X) {
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
@@ -874,18 +1047,24 @@ bool supported(int in, int nh, int out) {
   return (in == 112 && nh == 3 && out == 48) || (in == 64 && nh == 5 && out == 16) || (in == 32 && nh == 2 && out == 16);
 }
 
+template <int IN, int NH, int OUT, class Io>
+tpt_status launch_infer(tpt_mlp *M, int rows, const Io &io, cudaStream_t s) {
+  using L = InferLayout<IN, NH, OUT>;
+  if ((int)L::T::W_BYTES != M->wimg_bytes) return TPT_ERR_INVALID_ARGUMENT;
+  if (rows <= 0) return TPT_OK;
+  int sms = 0;
+  MLP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, M->device));
+  MLP_CUDA(cudaFuncSetAttribute(k_mlp_infer_tc<IN, NH, OUT, Io>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)L::SMEM));
+  const int tiles = (rows + 127) / 128;
+  const int grid = tiles < 2 * sms ? tiles : 2 * sms;
+  k_mlp_infer_tc<IN, NH, OUT, Io><<<grid, TC_THREADS, L::SMEM, s>>>(M->wimg, rows, io, M->err);
+  return mlp_cuda(cudaGetLastError());
+}
+
 template <int IN, int NH, int OUT>
 tpt_status launch_forward(tpt_mlp *M, const __half *x, int rows, float *y, cudaStream_t s) {
-  const size_t smem = (size_t)smem_w_halves(M->net) * 2;
-  MLP_CUDA(cudaFuncSetAttribute(k_mlp_forward<IN, NH, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, M->device);
-  const int tiles = rows / 16;
-  int grid = (tiles + WARPS - 1) / WARPS;
-  if (grid > sms * 4) grid = sms * 4;
-  if (grid < 1) grid = 1;
-  k_mlp_forward<IN, NH, OUT><<<grid, WARPS * 32, smem, s>>>(M->net, x, rows, y);
-  return mlp_cuda(cudaGetLastError());
+  return launch_infer<IN, NH, OUT>(M, rows, MatrixIo<IN, OUT>{x, y}, s);
 }
 
 template <int IN, int NH, int OUT, class Loss>
@@ -912,7 +1091,7 @@ tpt_status check_train_err(tpt_mlp *M, cudaStream_t s) {
   MLP_CUDA(cudaStreamSynchronize(s));
   if (!e) return TPT_OK;
   MLP_CUDA(cudaMemsetAsync(M->err, 0, sizeof(int), s));
-  std::snprintf(g_mlp_err, sizeof(g_mlp_err), "tensor-core training kernel: an MMA completion wait timed out");
+  std::snprintf(g_mlp_err, sizeof(g_mlp_err), "tensor-core MLP kernel: an MMA completion wait timed out");
   return TPT_ERR_CUDA;
 }
 
@@ -1082,17 +1261,13 @@ tpt_status cache_train(CacheNet *G, const float4 *rec, int count, int steps, int
 // Evaluates the cache for `count` queries (6 float4 each: the 4 feature
 // float4 then (throughput, pixel bits), unused); writes RGB rows of
 // NRC_OUT floats to *y_out (workspace owned by the cache).
-tpt_status cache_infer(CacheNet *G, const float4 *queries, int count, float3 lo, float3 ext, const float **y_out,
+tpt_status cache_infer(CacheNet *G, const float4 *queries, int count, float3 lo, float3 ext, float4 *accum,
                        cudaStream_t s) {
-  const int rows = (count + 15) / 16 * 16;
-  tpt_status st = cache_ws(G, rows);
-  if (st != TPT_OK) return st;
   const float3 inv = make_float3(1.f / ext.x, 1.f / ext.y, 1.f / ext.z);
-  k_nrc_encode_queries<<<(rows + 255) / 256, 256, 0, s>>>(queries, count, rows, lo, inv, G->x);
-  st = launch_forward<NRC_IN, NRC_NH, NRC_OUT>(G->net, G->x, rows, G->y, s);
-  *y_out = G->y;
-  return st;
+  return launch_infer<NRC_IN, NRC_NH, NRC_OUT>(G->net, count, CacheQueryIo{queries, lo, inv, accum}, s);
 }
+
+tpt_status cache_check(CacheNet *G, cudaStream_t s) { return check_train_err(G->net, s); }
 
 float cache_last_loss(const CacheNet *G) { return G->last_loss; }
 tpt_mlp *cache_mlp(CacheNet *G) { return G->net; }
@@ -1228,6 +1403,20 @@ tpt_status tpt_mlp_forward(tpt_mlp *M, const void *x_f16, int64_t rows, float *y
   if (M->in_dim == 112) return launch_forward<112, 3, 48>(M, x, (int)rows, y, s);
   if (M->in_dim == 64) return launch_forward<64, 5, 16>(M, x, (int)rows, y, s);
   return launch_forward<32, 2, 16>(M, x, (int)rows, y, s);
+}
+
+tpt_status tpt_mlp_cache_accumulate(tpt_mlp *M, const float *queries, int64_t count, const float *lo,
+                                    const float *extent, float *accum, void *stream) {
+  if (!M || !queries || !lo || !extent || !accum || count <= 0 || count > (1 << 28) || M->in_dim != NRC_IN ||
+      M->n_hidden != NRC_NH || M->out_dim != NRC_OUT)
+    return TPT_ERR_INVALID_ARGUMENT;
+  MLP_CUDA(cudaSetDevice(M->device));
+  cudaStream_t s = (cudaStream_t)stream;
+  const float3 l = make_float3(lo[0], lo[1], lo[2]);
+  const float3 inv = make_float3(1.f / extent[0], 1.f / extent[1], 1.f / extent[2]);
+  const tpt_status st = launch_infer<NRC_IN, NRC_NH, NRC_OUT>(
+      M, (int)count, CacheQueryIo{(const float4 *)queries, l, inv, (float4 *)accum}, s);
+  return st != TPT_OK ? st : check_train_err(M, s);
 }
 
 tpt_status tpt_mlp_backward_given(tpt_mlp *M, const void *x_f16, const float *dy, int64_t rows, float scale,

@@ -20,8 +20,13 @@ tpt_status cache_create(int device, uint64_t seed, CacheNet **out);
 void cache_destroy(CacheNet *g);
 tpt_status cache_train(CacheNet *g, const float4 *records, int count, int steps, int batch, float lr, float3 lo,
                        float3 ext, uint32_t key, cudaStream_t s);
-tpt_status cache_infer(CacheNet *g, const float4 *queries, int count, float3 lo, float3 ext, const float **y_out,
+// Evaluates the cache at `count` queries (6 float4 each: vertex features,
+// then throughput and pixel) and adds throughput x max(cache, 0) to accum
+// (one float4 per pixel), in one tensor-core kernel.
+tpt_status cache_infer(CacheNet *g, const float4 *queries, int count, float3 lo, float3 ext, float4 *accum,
                        cudaStream_t s);
+// TPT_ERR_CUDA if an MMA completion wait of the cache's kernels timed out.
+tpt_status cache_check(CacheNet *g, cudaStream_t s);
 float cache_last_loss(const CacheNet *g);
 
 // Checkpoint of a network's training state: weights, Adam moments, step

@@ -164,6 +164,7 @@ _SIGS = {
                                        C.c_void_p]),
     "tpt_render_batch": (C.c_int32, [C.c_void_p, C.POINTER(BatchItem), C.c_int32, C.POINTER(RenderParams),
                                      C.c_int32, C.POINTER(RenderStats)]),
+    "tpt_autotune_nrc": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]),
     "tpt_autotune": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.c_int32,
                                  C.POINTER(C.c_double)]),
     "tpt_mlp_create": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_void_p]),
@@ -173,6 +174,8 @@ _SIGS = {
     "tpt_mlp_get_params": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "tpt_mlp_get_grad": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "tpt_mlp_forward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "tpt_mlp_cache_accumulate": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                             C.c_void_p, C.c_void_p]),
     "tpt_mlp_backward_given": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float,
                                            C.c_void_p]),
     "tpt_mlp_backward_vmf": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float, C.c_void_p,
@@ -563,6 +566,16 @@ def render_batch(ctx: "Context", jobs, max_depth=50, semantics=SEMANTICS_REFEREN
     return (imgs if host else None), st.as_dict()
 
 
+def autotune_nrc(ctx: "Context", slot: int, width: int, height: int, probe_spp: int = 16, **kw) -> int:
+    """Runs tpt_autotune_nrc; returns the engine the slot's cached renders
+    will use (ENGINE_WAVEFRONT or ENGINE_PERSISTENT)."""
+    kw.setdefault("semantics", SEMANTICS_PHYSICAL)
+    p = make_params(width, height, probe_spp, **kw)
+    e = C.c_int32()
+    check(lib().tpt_autotune_nrc(ctx._h, slot, C.byref(p), probe_spp, C.byref(e)), "autotune_nrc")
+    return e.value
+
+
 def autotune(ctx: "Context", slot: int, width: int, height: int, probe_spp: int = 4, **kw):
     """Runs tpt_autotune; returns (engine, block, wave, flat_nodes, Msamples/s)."""
     p = make_params(width, height, probe_spp, **kw)
@@ -630,6 +643,14 @@ class Mlp:
 
     def forward(self, x_f16_ptr: int, rows: int, y_ptr: int) -> None:
         check(lib().tpt_mlp_forward(self._h, C.c_void_p(x_f16_ptr), rows, C.c_void_p(y_ptr), None), "mlp_forward")
+
+    def cache_accumulate(self, q_ptr: int, count: int, lo, extent, accum_ptr: int) -> None:
+        """tpt_mlp_cache_accumulate: queries (device, count x 6 float4) ->
+        accum (device, float4 per pixel) += throughput x max(cache, 0)."""
+        lo_a = np.ascontiguousarray(lo, np.float32)
+        ext_a = np.ascontiguousarray(extent, np.float32)
+        check(lib().tpt_mlp_cache_accumulate(self._h, C.c_void_p(q_ptr), count, _ptr(lo_a), _ptr(ext_a),
+                                             C.c_void_p(accum_ptr), None), "mlp_cache_accumulate")
 
     def backward_given(self, x_f16_ptr: int, dy_ptr: int, rows: int, scale: float = 1.0) -> None:
         check(lib().tpt_mlp_backward_given(self._h, C.c_void_p(x_f16_ptr), C.c_void_p(dy_ptr), rows, scale, None),
