@@ -1983,7 +1983,7 @@ extern "C" tpt_status tpt_autotune_batch(tpt_context *c, const tpt_batch_item *i
   }
   if (spheres_only)  // the stepped walk, and how many lanes wait before they shade
     for (int var : {14, 15})
-      for (int refill : {16, 24}) cands.push_back({64, var, 16, refill});
+      for (int refill : {16, 20, 24}) cands.push_back({64, var, 16, refill});
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaError_t ce = cudaEventCreate(&e0);
   if (ce == cudaSuccess) ce = cudaEventCreate(&e1);

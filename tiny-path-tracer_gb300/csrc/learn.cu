@@ -49,41 +49,6 @@ struct LossGiven {  // dY supplied by the caller (tests)
   }
 };
 
-// ------------------------------------------------------------ kernels ---
-template <int IN, int NH, int OUT>
-__global__ void __launch_bounds__(WARPS * 32) k_mlp_forward(Net n, const __half *__restrict__ X, int rows,
-                                                            float *__restrict__ Y) {
-  extern __shared__ __half smem[];
-  load_weights(n, smem, nullptr);
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  for (int tile = blockIdx.x * WARPS + warp; tile * 16 < rows; tile += gridDim.x * WARPS) {
-    const int r0 = tile * 16;
-    uint32_t a0[IN / 16][4];
-    load_frag_rows<IN>(X + (size_t)r0 * IN, IN, a0);
-    float acc[HID / 8][4];
-    layer_mma<IN, HID>(a0, smem + smem_w_offset(n, 0), acc);
-    uint32_t h[HID / 16][4];
-    relu_to_frag<HID>(acc, h);
-#pragma unroll
-    for (int l = 1; l < NH; l++) {
-      layer_mma<HID, HID>(h, smem + smem_w_offset(n, l), acc);
-      relu_to_frag<HID>(acc, h);
-    }
-    float out[OUT / 8][4];
-    layer_mma<HID, OUT>(h, smem + smem_w_offset(n, NH), out);
-#pragma unroll
-    for (int j = 0; j < OUT / 8; j++) {
-      float *y0 = Y + (size_t)(r0 + g) * OUT + j * 8 + 2 * t;
-      float *y1 = y0 + 8 * OUT;
-      y0[0] = out[j][0];
-      y0[1] = out[j][1];
-      y1[0] = out[j][2];
-      y1[1] = out[j][3];
-    }
-  }
-}
-
 // ------------------------------------------- fused training (tcgen05) ---
 // One training step of a batch on the 5th-generation tensor cores: every CTA
 // (one warpgroup, 128 threads; thread t owns row t of the tile and tensor-
@@ -895,9 +860,9 @@ __device__ __forceinline__ int nrc_record_index(int row, int count, uint32_t key
 }
 
 // The cache's training loss with its input built inside the training kernel:
-// row r of the batch is record nrc_record_index(r) (the sampling of
-// k_nrc_encode_records), encoded by nrc_encode straight into row t of the
-// swizzled input tile; the target is the record's radiance (non-finite: 0).
+// row r of the batch is record nrc_record_index(r, ...), encoded by
+// nrc_encode straight into row t of the swizzled input tile; the target is
+// the record's radiance (non-finite: 0).
 struct LossRelL2Records {
   const float4 *rec;
   int count;
@@ -928,19 +893,6 @@ struct LossRelL2Records {
     return LossRelL2{nullptr, scale}.template grad<OUT>(row, y, dy, t);
   }
 };
-
-__global__ void k_nrc_encode_records(const float4 *__restrict__ rec, int count, int rows, uint32_t key,
-                                     uint32_t step, float3 lo, float3 inv_ext, __half *__restrict__ X,
-                                     float4 *__restrict__ target) {
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
-    const int idx = nrc_record_index(r, count, key, step);
-    __align__(16) __half row[NRC_IN];
-    nrc_encode(rec + 5 * (size_t)idx, lo, inv_ext, row);
-    store_row(row, X + (size_t)r * NRC_IN);
-    const float4 t = rec[5 * (size_t)idx + 4];
-    target[r] = finite4(t) ? t : make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-}
 
 // Record r -> row r, without sampling (the encoders as the C ABI exposes
 // them).  stride: float4 per record (guide 3; cache records 5, queries 6).
@@ -992,20 +944,6 @@ struct CacheQueryIo {
     tc05::red_add_v4(reinterpret_cast<float *>(accum + __float_as_int(tq.w)), make_float4(L[0], L[1], L[2], 0.f));
   }
 };
-
-__global__ void k_nrc_encode_queries(const float4 *__restrict__ q, int count, int rows, float3 lo, float3 inv_ext,
-                                     __half *__restrict__ X) {
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
-    __half *out = X + (size_t)r * NRC_IN;
-    if (r >= count) {
-      for (int i = 0; i < NRC_IN; i++) out[i] = __float2half_rn(0.f);
-      continue;
-    }
-    __align__(16) __half row[NRC_IN];
-    nrc_encode(q + 6 * (size_t)r, lo, inv_ext, row);
-    store_row(row, out);
-  }
-}
 
 }  // namespace mlp
 }  // namespace tpt
@@ -1192,29 +1130,12 @@ float guide_last_loss(const GuideNet *G) { return G->last_loss; }
 tpt_mlp *guide_mlp(GuideNet *G) { return G->net; }
 
 // Radiance-cache network state used by the renderer.
+// Radiance-cache state: the network only (its training rows are encoded and
+// its queries evaluated inside the tensor-core kernels, no workspaces).
 struct CacheNet {
   tpt_mlp *net = nullptr;
-  __half *x = nullptr;
-  float *y = nullptr;
-  float4 *target = nullptr;
-  int cap_rows = 0;
   float last_loss = 0.f;
 };
-
-static tpt_status cache_ws(CacheNet *G, int rows) {
-  if (rows <= G->cap_rows) return TPT_OK;
-  if (G->x) cudaFree(G->x);
-  if (G->y) cudaFree(G->y);
-  if (G->target) cudaFree(G->target);
-  G->x = nullptr;
-  G->y = nullptr;
-  G->target = nullptr;
-  MLP_CUDA(cudaMalloc(&G->x, (size_t)rows * NRC_IN * sizeof(__half)));
-  MLP_CUDA(cudaMalloc(&G->y, (size_t)rows * NRC_OUT * sizeof(float)));
-  MLP_CUDA(cudaMalloc(&G->target, (size_t)rows * sizeof(float4)));
-  G->cap_rows = rows;
-  return TPT_OK;
-}
 
 tpt_status cache_create(int device, uint64_t seed, CacheNet **out) {
   auto *G = new CacheNet();
@@ -1230,9 +1151,6 @@ tpt_status cache_create(int device, uint64_t seed, CacheNet **out) {
 void cache_destroy(CacheNet *G) {
   if (!G) return;
   tpt_mlp_destroy(G->net);
-  if (G->x) cudaFree(G->x);
-  if (G->y) cudaFree(G->y);
-  if (G->target) cudaFree(G->target);
   delete G;
 }
 
@@ -1240,8 +1158,7 @@ tpt_status cache_train(CacheNet *G, const float4 *rec, int count, int steps, int
                        float3 ext, uint32_t key, cudaStream_t s) {
   if (count <= 0 || steps <= 0) return TPT_OK;
   batch = (batch + 15) / 16 * 16;
-  tpt_status st = cache_ws(G, batch);
-  if (st != TPT_OK) return st;
+  tpt_status st = TPT_OK;
   const float3 inv = make_float3(1.f / ext.x, 1.f / ext.y, 1.f / ext.z);
   const float loss_scale = 1024.f;
   for (int k = 0; k < steps; k++) {
@@ -1259,8 +1176,8 @@ tpt_status cache_train(CacheNet *G, const float4 *rec, int count, int steps, int
 }
 
 // Evaluates the cache for `count` queries (6 float4 each: the 4 feature
-// float4 then (throughput, pixel bits), unused); writes RGB rows of
-// NRC_OUT floats to *y_out (workspace owned by the cache).
+// float4, then (throughput, pixel bits), then unused) and adds throughput x
+// max(radiance, 0) to the pixels' sums.
 tpt_status cache_infer(CacheNet *G, const float4 *queries, int count, float3 lo, float3 ext, float4 *accum,
                        cudaStream_t s) {
   const float3 inv = make_float3(1.f / ext.x, 1.f / ext.y, 1.f / ext.z);
