@@ -486,8 +486,9 @@ typedef struct {
 void tpt_nrc_params_default(tpt_nrc_params *n);
 /* Chooses the engine of the slot's cached renders (TPT_ENGINE_AUTO): traces
  * a short cached render of p's size and settings (probe_spp >= 2 samples per
- * pixel, an untrained cache) on each engine and keeps the one with the
- * shorter tracing time (*engine_out, may be NULL).  The cache's own
+ * pixel, an untrained cache) on the wavefront engine and on the persistent
+ * engine at 64 or 128 threads and 4 or 5 resident blocks per SM, and keeps
+ * the one with the shortest tracing time (*engine_out, may be NULL).  The cache's own
  * training and inference cost the same on both engines.  The probes render
  * with fresh caches, so the context's cache is replaced (load a checkpoint
  * for a warm start afterwards). */

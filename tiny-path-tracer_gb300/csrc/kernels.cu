@@ -1040,7 +1040,8 @@ struct Slot {
   bool live = false;
   bool tuned = false;        // tpt_autotune result for engine = AUTO
   tpt_render_params tp{};
-  int cache_engine = 0;      // tpt_autotune_nrc result for cached renders (0: none)
+  int cache_engine = 0;      // tpt_autotune_nrc result for cached renders (0: none),
+  int cache_block = 128, cache_variant = 4;  // and its persistent launch shape
   float world_lo[3] = {0, 0, 0}, world_hi[3] = {0, 0, 0};
 };
 
@@ -2442,8 +2443,13 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
   const int wf_block =
       p->block > 0 ? p->block : (sl.tuned && sl.tp.engine == TPT_ENGINE_WAVEFRONT ? sl.tp.block : 128);
   const size_t wave = wf_wave(p, sl);
-  const int block = 128, smem = stack_smem(block);
-  auto kern = k_persistent_nrc<4>;
+  // persistent: 64 or 128 threads, 4 or 5 resident blocks per SM (as asked,
+  // else the slot's tpt_autotune_nrc choice)
+  const bool tuned_c = p->engine == TPT_ENGINE_AUTO && sl.cache_engine == TPT_ENGINE_PERSISTENT;
+  const int block = p->block == 64 || p->block == 128 ? p->block : (tuned_c ? sl.cache_block : 128);
+  const int variant = p->wave == 4 || p->wave == 5 ? p->wave : (tuned_c ? sl.cache_variant : 4);
+  const int smem = stack_smem(block);
+  auto kern = variant == 5 ? k_persistent_nrc<5> : k_persistent_nrc<4>;
   TPT_CUDA(smem_optin(kern, smem));
   const int grid = grid_for(c, kern, block, smem);
   if ((st = ensure(c->learn_pend, (size_t)n->record_cap * 2 * sizeof(float4))) != TPT_OK) return st;
@@ -2595,10 +2601,12 @@ extern "C" tpt_status tpt_render_nrc(tpt_context *c, int32_t slot, const tpt_ren
   return TPT_OK;
 }
 
-// The engine of the slot's cached renders: each engine traces a short
-// cached render (an untrained cache: the paths' lengths and the queries do
-// not depend on the weights, and training and inference cost the same on
-// both engines), the faster by render time is kept for TPT_ENGINE_AUTO.
+// The engine of the slot's cached renders: the wavefront engine and the
+// persistent one at 64 or 128 threads and 4 or 5 resident blocks per SM
+// each trace a short cached render (an untrained cache: the paths' lengths
+// and the queries do not depend on the weights, and training and inference
+// cost the same on every engine); the fastest by render time is kept for
+// TPT_ENGINE_AUTO.
 extern "C" tpt_status tpt_autotune_nrc(tpt_context *c, int32_t slot, const tpt_render_params *p, int32_t probe_spp,
                                        int32_t *engine_out) {
   if (!c || !p || probe_spp < 2 || p->width <= 0 || p->height <= 0) return TPT_ERR_INVALID_ARGUMENT;
@@ -2611,11 +2619,18 @@ extern "C" tpt_status tpt_autotune_nrc(tpt_context *c, int32_t slot, const tpt_r
   const size_t npix = (size_t)p->width * p->height;
   tpt_status st;
   if ((st = ensure(c->staging, npix * 3 * sizeof(float))) != TPT_OK) return st;
-  int best = TPT_ENGINE_WAVEFRONT;
+  struct Cand {
+    int engine, block, variant;
+  };
+  const Cand cands[] = {{TPT_ENGINE_WAVEFRONT, 0, 0},  {TPT_ENGINE_PERSISTENT, 64, 4}, {TPT_ENGINE_PERSISTENT, 64, 5},
+                        {TPT_ENGINE_PERSISTENT, 128, 4}, {TPT_ENGINE_PERSISTENT, 128, 5}};
+  Cand best = cands[0];
   double best_ms = 1e30;
-  for (int engine : {TPT_ENGINE_WAVEFRONT, TPT_ENGINE_PERSISTENT}) {
+  for (const Cand &cd : cands) {
     tpt_render_params q = *p;
-    q.engine = engine;
+    q.engine = cd.engine;
+    q.block = cd.block;   // wavefront: 0 = the slot's tuned block and queue
+    q.wave = cd.variant;
     q.spp = probe_spp;
     q.profile = 0;
     q.accumulate_fp64 = 0;
@@ -2628,11 +2643,16 @@ extern "C" tpt_status tpt_autotune_nrc(tpt_context *c, int32_t slot, const tpt_r
     }
     if (ms < best_ms) {
       best_ms = ms;
-      best = engine;
+      best = cd;
     }
   }
-  c->slots[slot].cache_engine = best;
-  if (engine_out) *engine_out = best;
+  Slot &sl = c->slots[slot];
+  sl.cache_engine = best.engine;
+  if (best.engine == TPT_ENGINE_PERSISTENT) {
+    sl.cache_block = best.block;
+    sl.cache_variant = best.variant;
+  }
+  if (engine_out) *engine_out = best.engine;
   return TPT_OK;
 }
 
