@@ -101,6 +101,22 @@ def test_path_spread_rule_ends_paths_between_the_fixed_depths(ctx, engine):
     ctx.release(slot)
 
 
+def test_cache_engine_autotune(ctx):
+    """tpt_autotune_nrc picks an engine for the slot's cached renders, which
+    the next TPT_ENGINE_AUTO cached render uses (an explicit engine still
+    wins), and a zero probe is refused."""
+    import ctypes as C
+
+    slot = _slot(ctx)
+    e = tpt.autotune_nrc(ctx, slot, 48, 48, probe_spp=4)
+    assert e in (tpt.ENGINE_WAVEFRONT, tpt.ENGINE_PERSISTENT)
+    img, st, ns = tpt.render_nrc(ctx, slot, 48, 48, 16, passes=2, first_pass_spp=4, train_steps=4, batch=1024, seed=2)
+    assert np.isfinite(img).all() and ns["queries"] > 0
+    p = tpt.make_params(48, 48, 4, 50, tpt.SEMANTICS_PHYSICAL)
+    assert tpt.lib().tpt_autotune_nrc(ctx._h, slot, C.byref(p), 0, None) == 1
+    ctx.release(slot)
+
+
 def test_nrc_argument_errors(ctx):
     import ctypes as C
 

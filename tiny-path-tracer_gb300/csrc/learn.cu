@@ -21,6 +21,7 @@
 #include <cstdio>
 #include <cstring>
 #include <random>
+#include <utility>
 #include <vector>
 
 #include "../../include/tpt.h"
@@ -138,7 +139,7 @@ constexpr int TC_THREADS = 160;  // warps 0-3: rows / tensor-memory lanes; warp 
 template <int IN, int NH, int OUT, class Loss>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_mlp_train_tc(Net n, const uint8_t *__restrict__ wimg, const __half *__restrict__ X, int rows, Loss loss,
-                   float *loss_sum, int *err) {
+                   float *loss_sum, float *loss_next, int *err) {
   using T = TrainLayout<IN, NH, OUT>;
   using namespace tc05;
   static_assert(T::BAR_OFF - T::H_OFF >= (uint32_t)((IN * HID + (NH - 1) * HID * HID + HID * OUT) * 4),
@@ -160,11 +161,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   // the weight image: one bulk copy (in 16 KB pieces) completing on barL.
   // Padding columns of the tiles (past IN) are never read: the forward MMAs
   // stop at K = IN and the weight-gradient MMAs at N = IN.
+  // Launched as a chained step, this prologue and the first tile's rows run
+  // while the previous step's Adam kernel finishes: the weight image, the
+  // gradient and the loss sums are touched only after griddep_wait.
+  if (t == 0) griddep_launch();
   if (issuer) {
     bar_init(barA, 1);
     bar_init(barW0, 1);
     bar_init(barW0 + 8, 1);
     bar_init(barL, 1);
+    griddep_wait();
+    if (loss_next && blockIdx.x == 0) *loss_next = 0.f;  // the next step's loss sum
     bar_expect_bytes(barL, T::W_BYTES);
     for (uint32_t o = 0; o < T::W_BYTES; o += 16384)
       bulk_copy(base + o, wimg + o, T::W_BYTES - o < 16384 ? T::W_BYTES - o : 16384, barL);
@@ -212,6 +219,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         cp_async_wait_all();
       }
       fence_async_smem();
+      if (first) griddep_wait();  // before this thread's tensor memory, gradient and loss writes
     }
     if (issuer && !weights) weights = ok = bar_wait(barL, 0, TC_WAIT_LIMIT);  // overlapped with the first tile's copies
     if (!(ok = __syncthreads_and(ok))) break;  // every thread leaves together
@@ -542,6 +550,10 @@ __global__ void k_adam(int count, float *__restrict__ w32, __half *__restrict__ 
                        float *__restrict__ m, float *__restrict__ v, float lr, float b1, float b2, float eps,
                        float inv_scale, float bc1, float bc2, Net n, uint8_t *__restrict__ wimg) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    if (i == blockIdx.x * blockDim.x + threadIdx.x) {  // first iteration: chained launches (cache training)
+      tc05::griddep_launch();
+      tc05::griddep_wait();
+    }
     float gr = grad[i] * inv_scale;
     if (!isfinite(gr)) gr = 0.f;  // an overflowed element skips this step
     const float mi = b1 * m[i] + (1.f - b1) * gr;
@@ -1005,8 +1017,31 @@ tpt_status launch_forward(tpt_mlp *M, const __half *x, int rows, float *y, cudaS
   return launch_infer<IN, NH, OUT>(M, rows, MatrixIo<IN, OUT>{x, y}, s);
 }
 
+// A launch that may start while the previous kernel in the stream runs
+// (programmatic stream serialisation; the kernel orders itself with
+// griddep_wait).
+template <typename... K, typename... A>
+cudaError_t launch_chained(void (*kern)(K...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A &&...args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
+}
+
+// chain_step < 0: a standalone step (its loss sum in M->loss[0], zeroed
+// here).  chain_step = k >= 0: step k of a chain of steps each followed by
+// adam_step(.., chained): launched to overlap the previous Adam kernel, its
+// loss sum in M->loss[k & 1], and it zeroes M->loss[(k + 1) & 1] for the
+// next step (the caller zeroes both before step 0).
 template <int IN, int NH, int OUT, class Loss>
-tpt_status launch_train(tpt_mlp *M, const __half *x, int rows, const Loss &loss, cudaStream_t s) {
+tpt_status launch_train(tpt_mlp *M, const __half *x, int rows, const Loss &loss, cudaStream_t s, int chain_step = -1) {
   using L = TrainLayout<IN, NH, OUT>;
   static_assert(L::W_BYTES % 16 == 0, "bulk copies move 16-byte multiples");
   if ((int)L::W_BYTES != M->wimg_bytes) return TPT_ERR_INVALID_ARGUMENT;
@@ -1016,10 +1051,31 @@ tpt_status launch_train(tpt_mlp *M, const __half *x, int rows, const Loss &loss,
                                 (int)L::SMEM));
   const int tiles = (rows + 127) / 128;
   const int grid = tiles < sms ? tiles : sms;
-  MLP_CUDA(cudaMemsetAsync(M->loss, 0, sizeof(float), s));
-  k_mlp_train_tc<IN, NH, OUT, Loss><<<grid, TC_THREADS, L::SMEM, s>>>(M->net, M->wimg, x, rows, loss, M->loss,
-                                                                      M->err);
-  return mlp_cuda(cudaGetLastError());
+  if (chain_step < 0) {
+    MLP_CUDA(cudaMemsetAsync(M->loss, 0, sizeof(float), s));
+    k_mlp_train_tc<IN, NH, OUT, Loss><<<grid, TC_THREADS, L::SMEM, s>>>(M->net, M->wimg, x, rows, loss, M->loss,
+                                                                        nullptr, M->err);
+    return mlp_cuda(cudaGetLastError());
+  }
+  return mlp_cuda(launch_chained(k_mlp_train_tc<IN, NH, OUT, Loss>, dim3(grid), dim3(TC_THREADS), L::SMEM, s,
+                                 M->net, (const uint8_t *)M->wimg, x, rows, loss, M->loss + (chain_step & 1),
+                                 M->loss + ((chain_step + 1) & 1), M->err));
+}
+
+// Adam on the accumulated gradient (clears it); chained: launched to start
+// while the training kernel before it finishes (k_adam waits for it).
+tpt_status adam_step(tpt_mlp *M, float lr, float inv_loss_scale, cudaStream_t s, bool chained) {
+  M->steps++;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  const float bc1 = 1.f - std::pow(b1, (float)M->steps), bc2 = 1.f - std::pow(b2, (float)M->steps);
+  const int grid = (M->params + 255) / 256;
+  if (!chained) {
+    k_adam<<<grid, 256, 0, s>>>(M->params, M->w32, M->w16, M->grad, M->m, M->v, lr, b1, b2, eps, inv_loss_scale, bc1,
+                                bc2, M->net, M->wimg);
+    return mlp_cuda(cudaGetLastError());
+  }
+  return mlp_cuda(launch_chained(k_adam, dim3(grid), dim3(256), 0, s, M->params, M->w32, M->w16, M->grad, M->m, M->v,
+                                 lr, b1, b2, eps, inv_loss_scale, bc1, bc2, M->net, M->wimg));
 }
 
 // An MMA completion the training kernel waited for in vain: reported once.
@@ -1161,15 +1217,18 @@ tpt_status cache_train(CacheNet *G, const float4 *rec, int count, int steps, int
   tpt_status st = TPT_OK;
   const float3 inv = make_float3(1.f / ext.x, 1.f / ext.y, 1.f / ext.z);
   const float loss_scale = 1024.f;
+  // chained steps: each training kernel's prologue and row encoding overlap
+  // the previous step's Adam kernel
+  MLP_CUDA(cudaMemsetAsync(G->net->loss, 0, 2 * sizeof(float), s));
   for (int k = 0; k < steps; k++) {
     // the rows are sampled and encoded inside the training kernel
     LossRelL2Records L{rec, count, key, (uint32_t)(G->net->steps + 1), lo, inv, loss_scale / (float)batch};
-    st = launch_train<NRC_IN, NRC_NH, NRC_OUT>(G->net, nullptr, batch, L, s);
+    st = launch_train<NRC_IN, NRC_NH, NRC_OUT>(G->net, nullptr, batch, L, s, k);
     if (st != TPT_OK) return st;
-    if ((st = tpt_mlp_adam(G->net, lr, 1.f / loss_scale, s)) != TPT_OK) return st;
+    if ((st = adam_step(G->net, lr, 1.f / loss_scale, s, true)) != TPT_OK) return st;
   }
   float l = 0.f;
-  MLP_CUDA(cudaMemcpyAsync(&l, G->net->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+  MLP_CUDA(cudaMemcpyAsync(&l, G->net->loss + ((steps - 1) & 1), sizeof(float), cudaMemcpyDeviceToHost, s));
   MLP_CUDA(cudaStreamSynchronize(s));
   G->last_loss = l / (float)batch;
   return check_train_err(G->net, s);
@@ -1239,7 +1298,7 @@ tpt_status tpt_mlp_create(int32_t device, int32_t in_dim, int32_t n_hidden, int3
   if (e == cudaSuccess) e = cudaMalloc(&M->m, P * 4);
   if (e == cudaSuccess) e = cudaMalloc(&M->v, P * 4);
   if (e == cudaSuccess) e = cudaMalloc(&M->w16, P * 2);
-  if (e == cudaSuccess) e = cudaMalloc(&M->loss, 4);
+  if (e == cudaSuccess) e = cudaMalloc(&M->loss, 2 * sizeof(float));  // two slots for chained steps
   M->wimg_bytes = (int)wimg_bytes(M->net);
   if (e == cudaSuccess) e = cudaMalloc(&M->wimg, (size_t)M->wimg_bytes);
   if (e == cudaSuccess) e = cudaMemset(M->wimg, 0, (size_t)M->wimg_bytes);
@@ -1440,13 +1499,7 @@ tpt_status tpt_nrc_encode(const float *records, int64_t count, int32_t stride, c
 tpt_status tpt_mlp_adam(tpt_mlp *M, float lr, float inv_loss_scale, void *stream) {
   if (!M) return TPT_ERR_INVALID_ARGUMENT;
   MLP_CUDA(cudaSetDevice(M->device));
-  M->steps++;
-  const float b1 = 0.9f, b2 = 0.999f;
-  const float bc1 = 1.f - std::pow(b1, (float)M->steps), bc2 = 1.f - std::pow(b2, (float)M->steps);
-  k_adam<<<(M->params + 255) / 256, 256, 0, (cudaStream_t)stream>>>(M->params, M->w32, M->w16, M->grad, M->m, M->v,
-                                                                     lr, b1, b2, 1e-8f, inv_loss_scale, bc1, bc2,
-                                                                     M->net, M->wimg);
-  return mlp_cuda(cudaGetLastError());
+  return adam_step(M, lr, inv_loss_scale, (cudaStream_t)stream, false);
 }
 
 }  // extern "C"

@@ -119,6 +119,15 @@ __device__ __forceinline__ void bulk_copy(uint32_t dst_smem, const void *src, ui
 // a descriptor for the operand `bytes` further on (addresses stay below 256 KB)
 __device__ __forceinline__ uint64_t desc_add(uint64_t d, uint32_t bytes) { return d + (uint64_t)(bytes >> 4); }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialisation may start while its predecessor in the stream still runs;
+// griddep_wait blocks the calling thread until the predecessor grids have
+// completed and their memory is visible, griddep_launch lets this grid's
+// own dependents start (once every CTA has issued it or exited).  Without
+// the launch attribute both return at once.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // gradient[addr..addr+3] += v without a return value (16-byte aligned)
 __device__ __forceinline__ void red_add_v4(float *addr, float4 v) {
   asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
