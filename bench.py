@@ -457,7 +457,7 @@ def learned_equal_time(ctx, which: str) -> dict:
     The cached renders run on the engine tpt_autotune_nrc picks for the
     scene (timed before, like the plain tracer's autotune).
     Every point (plain, learned at equal spp, at equal time, and the points
-    of the time-to-plain-relMSE search) is the mean over three seeds (each
+    of the time-to-plain-relMSE search) is the mean over five seeds (each
     learned run trains its own network online; per-seed values are reported
     too).  time_to_plain_relmse_ratio = the learned renderer's wall time at
     the spp where its relMSE equals the plain tracer's, over the plain
@@ -492,7 +492,7 @@ def learned_equal_time(ctx, which: str) -> dict:
 
     ref, _ = ctx.render(slot, w, h, ref_spp, semantics=tpt.SEMANTICS_PHYSICAL, seed=999, fp64=True)
     passes = 8
-    seeds = (5, 6, 7)  # both sides: the mean over three seeds (each learned run trains its own network)
+    seeds = (5, 6, 7, 8, 9)  # both sides: the mean over five seeds (each learned run trains its own network)
     plain = lambda n, sd_: ctx.render(slot, w, h, n, semantics=tpt.SEMANTICS_PHYSICAL, seed=sd_,
                                       out=dev.data_ptr())
     plain(spp, seeds[0])  # warm-up
@@ -515,7 +515,7 @@ def learned_equal_time(ctx, which: str) -> dict:
     def time_to_plain(run, pts):
         """Wall time the learned renderer needs to reach the plain tracer's
         relMSE: secant steps on log(relMSE) against log(spp) from the points
-        measured so far (spp, ms, relMSE), three seeds per point, until a
+        measured so far (spp, ms, relMSE), five seeds per point, until a
         point lands within 5 % of the target; the time at the target spp
         is interpolated linearly between the two nearest points."""
         for _ in range(3):
