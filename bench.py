@@ -66,10 +66,25 @@ BYTES_PER_SEGMENT = 192
 TRAVERSE_BYTES_PER_SEGMENT = 64 + 16  # traverse reads the path record, writes the hit
 # k_persistent DRAM read+write bytes and warp instructions per ray segment,
 # from the ncu capture (--set full) of this script's 16 spp case in the tuned
-# launch (--spp 16 --engine 2 --block 64 --wave 5): 9.174 MB and 3.412 G warp
-# instructions over 30.42 M segments
-NCU_DRAM_BYTES_PER_SEGMENT = (8.19712e6 + 0.976896e6) / 30416883
-NCU_WARP_INST_PER_SEGMENT = 3411932611 / 30416883
+# launch (--spp 16 --engine 2 --block 64 --wave 5): 9.367 MB and 3.412 G warp
+# instructions over 30.42 M segments.  NCU_SOURCE is the fingerprint of the
+# kernel sources that capture ran (kernel_source_fingerprint()); the bench
+# line says whether the sources it runs still match it.
+NCU_DRAM_BYTES_PER_SEGMENT = (8.197632e6 + 1.169152e6) / 30416883
+NCU_WARP_INST_PER_SEGMENT = 3412038270 / 30416883
+NCU_SOURCE = "2dddc7c1aa56f67c"
+
+
+def kernel_source_fingerprint() -> str:
+    """First 16 hex digits of the SHA-256 of csrc/device.cuh + csrc/kernels.cu."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for f in ("device.cuh", "kernels.cu"):
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tiny-path-tracer_gb300", "csrc", f),
+                  "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
 # instruction issue peak: 152 SMs x 4 schedulers x 1 warp instruction per
 # cycle at the maximum SM clock (MEASURED_PEAKS.json sm_max_mhz)
 SMS, SCHEDULERS_PER_SM = 152, 4
@@ -759,9 +774,12 @@ def main() -> None:
             roof["issue_roofline"] = {
                 "bound": "issue", "achieved": ach_issue, "peak": peak_issue, "unit": "G warp-inst/s",
                 "frac": ach_issue / peak_issue, "warp_inst_per_segment": NCU_WARP_INST_PER_SEGMENT,
+                "counts_source": NCU_SOURCE, "counts_match_kernel_source": kernel_source_fingerprint() == NCU_SOURCE,
                 "note": ("instructions per segment from the ncu capture of the same kernel (16 spp case, "
                          "NCU_WARP_INST_PER_SEGMENT) x segments per second measured here; peak = 152 SMs x 4 "
-                         "schedulers x 1 instruction per cycle at the maximum SM clock")}
+                         "schedulers x 1 instruction per cycle at the maximum SM clock; "
+                         "counts_match_kernel_source: whether the kernel sources running now are the ones "
+                         "the capture ran")}
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
