@@ -387,12 +387,14 @@ tpt_status tpt_nrc_encode(const float *records, int64_t count, int32_t stride, c
 /* Radiance-cache network only: the cached renderer's query evaluation.
  * queries: device, 6 float4 each - the four feature float4 of
  * tpt_nrc_encode, then (throughput rgb, pixel index as int32 bits), then
- * unused; accum: device, one float4 per pixel.  For every query, encodes
- * its features (box [lo, lo + extent]), evaluates the network on the
- * tensor cores and adds throughput x max(output rgb, 0) (NaN components as
- * 0) to accum[pixel].xyz, in one kernel. */
+ * unused; accum: device, n_pixels float4.  For every query, encodes its
+ * features (box [lo, lo + extent]), evaluates the network on the tensor
+ * cores and adds throughput x max(output rgb, 0) (NaN components as 0) to
+ * accum[pixel].xyz, in one kernel.  Queries naming a pixel >= n_pixels are
+ * skipped and the call returns TPT_ERR_INVALID_ARGUMENT after the others
+ * were added.  Synchronises the stream. */
 tpt_status tpt_mlp_cache_accumulate(tpt_mlp *m, const float *queries, int64_t count, const float *lo,
-                                    const float *extent, float *accum, void *stream);
+                                    const float *extent, float *accum, int64_t n_pixels, void *stream);
 /* Adam step (lr, beta 0.9/0.999, eps 1e-8) on the accumulated gradient
  * multiplied by inv_loss_scale; clears the gradient. */
 tpt_status tpt_mlp_adam(tpt_mlp *m, float lr, float inv_loss_scale, void *stream);

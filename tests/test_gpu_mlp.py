@@ -184,7 +184,7 @@ def test_cache_query_accumulate_matches_reference(built):
     qd = torch.from_numpy(q.reshape(n, 24)).cuda()
     ad = torch.from_numpy(acc0.copy()).cuda()
     torch.cuda.synchronize()
-    net.cache_accumulate(qd.data_ptr(), n, LO, EXT, ad.data_ptr())
+    net.cache_accumulate(qd.data_ptr(), n, LO, EXT, ad.data_ptr(), npix)
     torch.cuda.synchronize()
     acc = ad.cpu().numpy().astype(np.float64)
     y, _ = mlp_ref.forward(p16, mlp_ref.nrc_encode(q, LO, EXT).astype(np.float64), 64, 5, 16)
@@ -197,6 +197,18 @@ def test_cache_query_accumulate_matches_reference(built):
     scale = np.abs(ref[:, :3] - acc0[:, :3]).max()
     print("cache accumulate", err.max() / scale)
     assert err.max() < FWD_RTOL * scale, (err.max(), scale)
+    # a query naming a pixel past the buffer is skipped and reported
+    q2 = q[:256].copy()
+    q2[7, 4, 3] = np.int32(npix).view(np.float32)
+    qd2 = torch.from_numpy(q2.reshape(256, 24)).cuda()
+    before = ad.clone()
+    with pytest.raises(tpt.TptError):
+        net.cache_accumulate(qd2.data_ptr(), 256, LO, EXT, ad.data_ptr(), npix)
+    got = (ad - before).cpu().numpy().astype(np.float64)[:, :3]
+    ok = np.arange(256) != 7
+    want = np.zeros((npix, 3))
+    np.add.at(want, pix[:256][ok], L[:256][ok])
+    assert np.abs(got - want).max() < FWD_RTOL * scale, np.abs(got - want).max()
 
 
 def test_guide_encoder_matches_reference(built):

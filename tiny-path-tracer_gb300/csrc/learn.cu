@@ -932,6 +932,8 @@ struct CacheQueryIo {
   const float4 *q;
   float3 lo, inv_ext;
   float4 *accum;
+  uint32_t n_pixels;  // accum's length: a query naming a pixel past it is skipped and flagged
+  int *bad;
   using Pre = float4;
   __device__ Pre load(int row, bool valid, uint8_t *xtile, int t) const {
     __align__(16) __half x[NRC_IN];
@@ -950,10 +952,15 @@ struct CacheQueryIo {
   }
   __device__ void store(int, bool valid, const float *v, Pre tq) const {
     if (!valid) return;
+    const uint32_t pixel = (uint32_t)__float_as_int(tq.w);
+    if (pixel >= n_pixels) {
+      atomicExch(bad, 1);
+      return;
+    }
     float L[3] = {tq.x * fmaxf(v[0], 0.f), tq.y * fmaxf(v[1], 0.f), tq.z * fmaxf(v[2], 0.f)};
 #pragma unroll
     for (int c = 0; c < 3; c++) L[c] = isnan(L[c]) ? 0.f : L[c];
-    tc05::red_add_v4(reinterpret_cast<float *>(accum + __float_as_int(tq.w)), make_float4(L[0], L[1], L[2], 0.f));
+    tc05::red_add_v4(reinterpret_cast<float *>(accum + pixel), make_float4(L[0], L[1], L[2], 0.f));
   }
 };
 
@@ -1240,7 +1247,9 @@ tpt_status cache_train(CacheNet *G, const float4 *rec, int count, int steps, int
 tpt_status cache_infer(CacheNet *G, const float4 *queries, int count, float3 lo, float3 ext, float4 *accum,
                        cudaStream_t s) {
   const float3 inv = make_float3(1.f / ext.x, 1.f / ext.y, 1.f / ext.z);
-  return launch_infer<NRC_IN, NRC_NH, NRC_OUT>(G->net, count, CacheQueryIo{queries, lo, inv, accum}, s);
+  // the renderer's own queries name pixels of its frame
+  return launch_infer<NRC_IN, NRC_NH, NRC_OUT>(G->net, count,
+                                               CacheQueryIo{queries, lo, inv, accum, 0xffffffffu, G->net->err}, s);
 }
 
 tpt_status cache_check(CacheNet *G, cudaStream_t s) { return check_train_err(G->net, s); }
@@ -1382,17 +1391,29 @@ tpt_status tpt_mlp_forward(tpt_mlp *M, const void *x_f16, int64_t rows, float *y
 }
 
 tpt_status tpt_mlp_cache_accumulate(tpt_mlp *M, const float *queries, int64_t count, const float *lo,
-                                    const float *extent, float *accum, void *stream) {
-  if (!M || !queries || !lo || !extent || !accum || count <= 0 || count > (1 << 28) || M->in_dim != NRC_IN ||
-      M->n_hidden != NRC_NH || M->out_dim != NRC_OUT)
+                                    const float *extent, float *accum, int64_t n_pixels, void *stream) {
+  if (!M || !queries || !lo || !extent || !accum || count <= 0 || count > (1 << 28) || n_pixels <= 0 ||
+      n_pixels > 0xffffffffll || M->in_dim != NRC_IN || M->n_hidden != NRC_NH || M->out_dim != NRC_OUT)
     return TPT_ERR_INVALID_ARGUMENT;
   MLP_CUDA(cudaSetDevice(M->device));
   cudaStream_t s = (cudaStream_t)stream;
   const float3 l = make_float3(lo[0], lo[1], lo[2]);
   const float3 inv = make_float3(1.f / extent[0], 1.f / extent[1], 1.f / extent[2]);
-  const tpt_status st = launch_infer<NRC_IN, NRC_NH, NRC_OUT>(
-      M, (int)count, CacheQueryIo{(const float4 *)queries, l, inv, (float4 *)accum}, s);
-  return st != TPT_OK ? st : check_train_err(M, s);
+  int *bad = nullptr;  // a query naming a pixel past accum
+  MLP_CUDA(cudaMallocAsync((void **)&bad, sizeof(int), s));
+  tpt_status st = mlp_cuda(cudaMemsetAsync(bad, 0, sizeof(int), s));
+  if (st == TPT_OK)
+    st = launch_infer<NRC_IN, NRC_NH, NRC_OUT>(
+        M, (int)count, CacheQueryIo{(const float4 *)queries, l, inv, (float4 *)accum, (uint32_t)n_pixels, bad}, s);
+  int b = 0;
+  if (st == TPT_OK) st = mlp_cuda(cudaMemcpyAsync(&b, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+  cudaFreeAsync(bad, s);
+  if (st == TPT_OK) st = check_train_err(M, s);  // synchronises the stream
+  if (st == TPT_OK && b) {
+    std::snprintf(g_mlp_err, sizeof(g_mlp_err), "cache queries name pixels past n_pixels (skipped)");
+    st = TPT_ERR_INVALID_ARGUMENT;
+  }
+  return st;
 }
 
 tpt_status tpt_mlp_backward_given(tpt_mlp *M, const void *x_f16, const float *dy, int64_t rows, float scale,

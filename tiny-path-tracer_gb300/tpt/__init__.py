@@ -175,7 +175,7 @@ _SIGS = {
     "tpt_mlp_get_grad": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "tpt_mlp_forward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "tpt_mlp_cache_accumulate": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
-                                             C.c_void_p, C.c_void_p]),
+                                             C.c_void_p, C.c_int64, C.c_void_p]),
     "tpt_mlp_backward_given": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float,
                                            C.c_void_p]),
     "tpt_mlp_backward_vmf": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float, C.c_void_p,
@@ -644,13 +644,13 @@ class Mlp:
     def forward(self, x_f16_ptr: int, rows: int, y_ptr: int) -> None:
         check(lib().tpt_mlp_forward(self._h, C.c_void_p(x_f16_ptr), rows, C.c_void_p(y_ptr), None), "mlp_forward")
 
-    def cache_accumulate(self, q_ptr: int, count: int, lo, extent, accum_ptr: int) -> None:
+    def cache_accumulate(self, q_ptr: int, count: int, lo, extent, accum_ptr: int, n_pixels: int) -> None:
         """tpt_mlp_cache_accumulate: queries (device, count x 6 float4) ->
-        accum (device, float4 per pixel) += throughput x max(cache, 0)."""
+        accum (device, n_pixels float4) += throughput x max(cache, 0)."""
         lo_a = np.ascontiguousarray(lo, np.float32)
         ext_a = np.ascontiguousarray(extent, np.float32)
         check(lib().tpt_mlp_cache_accumulate(self._h, C.c_void_p(q_ptr), count, _ptr(lo_a), _ptr(ext_a),
-                                             C.c_void_p(accum_ptr), None), "mlp_cache_accumulate")
+                                             C.c_void_p(accum_ptr), n_pixels, None), "mlp_cache_accumulate")
 
     def backward_given(self, x_f16_ptr: int, dy_ptr: int, rows: int, scale: float = 1.0) -> None:
         check(lib().tpt_mlp_backward_given(self._h, C.c_void_p(x_f16_ptr), C.c_void_p(dy_ptr), rows, scale, None),
