@@ -1395,6 +1395,8 @@ tpt_status tpt_mlp_cache_accumulate(tpt_mlp *M, const float *queries, int64_t co
   if (!M || !queries || !lo || !extent || !accum || count <= 0 || count > (1 << 28) || n_pixels <= 0 ||
       n_pixels > 0xffffffffll || M->in_dim != NRC_IN || M->n_hidden != NRC_NH || M->out_dim != NRC_OUT)
     return TPT_ERR_INVALID_ARGUMENT;
+  for (int a = 0; a < 3; a++)
+    if (!(extent[a] > 0.f) || !std::isfinite(lo[a]) || !std::isfinite(extent[a])) return TPT_ERR_INVALID_ARGUMENT;
   MLP_CUDA(cudaSetDevice(M->device));
   cudaStream_t s = (cudaStream_t)stream;
   const float3 l = make_float3(lo[0], lo[1], lo[2]);
