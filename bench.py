@@ -446,6 +446,25 @@ def _relmse(x, ref, eps=1e-2) -> float:
     return float(np.mean((x.astype(np.float64) - ref) ** 2 / (ref.astype(np.float64) ** 2 + eps)))
 
 
+def interpolate_to_target(pts, e_target):
+    """Points (spp, ms, relMSE) -> (spp, ms, reached) where the relMSE equals
+    e_target: log relMSE interpolated linearly in log spp between the
+    bracketing points (the last point above the target and the first at or
+    below it, by spp), the time linearly in spp; without a bracket, the
+    nearest end (reached False when no point is at or below the target)."""
+    pts = sorted(pts)
+    lo = [p for p in pts if p[2] > e_target]
+    hi = [p for p in pts if p[2] <= e_target]
+    a = max(lo) if lo else pts[0]
+    b = min(hi) if hi else pts[-1]
+    if a[0] == b[0]:
+        return float(a[0]), float(a[1]), bool(hi)
+    f = (np.log(e_target) - np.log(a[2])) / (np.log(b[2]) - np.log(a[2]))
+    n_star = float(np.exp(np.log(a[0]) + f * (np.log(b[0]) - np.log(a[0]))))
+    t_star = a[1] + (n_star - a[0]) / (b[0] - a[0]) * (b[1] - a[1])
+    return n_star, float(t_star), bool(hi)
+
+
 def learned_equal_time(ctx, which: str) -> dict:
     """Equal-time comparison of a learned renderer against the plain tracer,
     both scored by relMSE against an FP64-accumulated high-spp plain render
@@ -552,18 +571,8 @@ def learned_equal_time(ctx, which: str) -> dict:
             t, e, _, _ = at(run, n)
             pts.append((n, t, e))
         pts.sort()
-        # log-log interpolation of spp at the target between the bracketing points, time linear in spp
-        lo = [p for p in pts if p[2] > e_plain]
-        hi = [p for p in pts if p[2] <= e_plain]
-        a = max(lo) if lo else pts[0]
-        b = min(hi) if hi else pts[-1]
-        if a[0] == b[0]:
-            n_star, t_star = float(a[0]), a[1]
-        else:
-            f = (np.log(e_plain) - np.log(a[2])) / (np.log(b[2]) - np.log(a[2]))
-            n_star = float(np.exp(np.log(a[0]) + f * (np.log(b[0]) - np.log(a[0]))))
-            t_star = a[1] + (n_star - a[0]) / (b[0] - a[0]) * (b[1] - a[1])
-        return {"spp": n_star, "ms": t_star, "ratio": t_star / t_plain, "reached": bool(hi),
+        n_star, t_star, reached = interpolate_to_target(pts, e_plain)
+        return {"spp": n_star, "ms": t_star, "ratio": t_star / t_plain, "reached": reached,
                 "points": [{"spp": p[0], "ms": p[1], "relmse": p[2]} for p in pts]}
 
     def compare(run):
