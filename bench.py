@@ -446,23 +446,35 @@ def _relmse(x, ref, eps=1e-2) -> float:
     return float(np.mean((x.astype(np.float64) - ref) ** 2 / (ref.astype(np.float64) ** 2 + eps)))
 
 
-def interpolate_to_target(pts, e_target):
+def fit_to_target(pts, e_target, near=3):
     """Points (spp, ms, relMSE) -> (spp, ms, reached) where the relMSE equals
-    e_target: log relMSE interpolated linearly in log spp between the
-    bracketing points (the last point above the target and the first at or
-    below it, by spp), the time linearly in spp; without a bracket, the
-    nearest end (reached False when no point is at or below the target)."""
+    e_target.  log relMSE is fitted by least squares as a line in log spp
+    over the `near` points closest (in log spp) to a first fit's crossing,
+    its slope held in [-1.5, -0.2] (a Monte Carlo error falls as 1/spp, a
+    biased estimator's more slowly, never faster); one noisy point then
+    moves the answer less than a two-point bracket would.  The time is a
+    least-squares line in spp over the same points.  reached: some point is
+    at or below the target."""
     pts = sorted(pts)
-    lo = [p for p in pts if p[2] > e_target]
-    hi = [p for p in pts if p[2] <= e_target]
-    a = max(lo) if lo else pts[0]
-    b = min(hi) if hi else pts[-1]
-    if a[0] == b[0]:
-        return float(a[0]), float(a[1]), bool(hi)
-    f = (np.log(e_target) - np.log(a[2])) / (np.log(b[2]) - np.log(a[2]))
-    n_star = float(np.exp(np.log(a[0]) + f * (np.log(b[0]) - np.log(a[0]))))
-    t_star = a[1] + (n_star - a[0]) / (b[0] - a[0]) * (b[1] - a[1])
-    return n_star, float(t_star), bool(hi)
+
+    def fit(sel):
+        n = np.array([p[0] for p in sel], float)
+        t = np.array([p[1] for p in sel], float)
+        x, y = np.log(n), np.log(np.array([p[2] for p in sel], float))
+        slope = np.polyfit(x, y, 1)[0] if len(sel) >= 2 and np.ptp(x) > 0 else -1.0
+        slope = float(min(max(slope, -1.5), -0.2))
+        icpt = float(np.mean(y - slope * x))
+        n_star = float(np.exp((np.log(e_target) - icpt) / slope))
+        if len(sel) >= 2 and np.ptp(n) > 0:
+            b, a = np.polyfit(n, t, 1)
+        else:
+            b, a = t[0] / n[0], 0.0
+        return n_star, float(a + b * n_star)
+
+    n0, _ = fit(pts)
+    sel = sorted(pts, key=lambda p: abs(np.log(p[0] / n0)))[:max(2, near)]
+    n_star, t_star = fit(sel)
+    return n_star, t_star, any(p[2] <= e_target for p in pts)
 
 
 def learned_equal_time(ctx, which: str) -> dict:
@@ -548,30 +560,23 @@ def learned_equal_time(ctx, which: str) -> dict:
 
     def time_to_plain(run, pts):
         """Wall time the learned renderer needs to reach the plain tracer's
-        relMSE: secant steps on log(relMSE) against log(spp) from the points
-        measured so far (spp, ms, relMSE), five seeds per point, until a
-        point lands within 5 % of the target; the time at the target spp
-        is interpolated linearly between the two nearest points."""
+        relMSE (points (spp, ms, relMSE), five seeds each): fit_to_target
+        predicts the spp from the points measured so far, and a new point is
+        measured there while no measured point lies within 15 % of the
+        prediction (at most three); the answer is the fit over the final
+        points."""
         for _ in range(3):
-            pts.sort()
-            if any(abs(np.log(e / e_plain)) < 0.05 for _, _, e in pts):
+            n_pred, _, _ = fit_to_target(pts, e_plain)
+            if min(abs(p[0] - n_pred) for p in pts) <= 0.15 * n_pred:
                 break
-            below = [p for p in pts if p[2] <= e_plain]
-            above = [p for p in pts if p[2] > e_plain]
-            a = max(above) if above else None
-            b = min(below) if below else None
-            if a is None or b is None:  # extrapolate from the two outermost points
-                a, b = (pts[-2], pts[-1]) if above else (pts[0], pts[1])
-            slope = (np.log(b[2]) - np.log(a[2])) / (np.log(b[0]) - np.log(a[0])) if b[0] != a[0] else -1.0
-            slope = min(slope, -0.25)
-            n = int(round(np.exp(np.log(a[0]) + (np.log(e_plain) - np.log(a[2])) / slope) / passes)) * passes
+            n = int(round(n_pred / passes)) * passes
             n = int(min(max(n, passes), 8 * spp))
             if any(p[0] == n for p in pts):
                 break
             t, e, _, _ = at(run, n)
             pts.append((n, t, e))
         pts.sort()
-        n_star, t_star, reached = interpolate_to_target(pts, e_plain)
+        n_star, t_star, reached = fit_to_target(pts, e_plain)
         return {"spp": n_star, "ms": t_star, "ratio": t_star / t_plain, "reached": reached,
                 "points": [{"spp": p[0], "ms": p[1], "relmse": p[2]} for p in pts]}
 

@@ -1,5 +1,5 @@
 """The bench's measurement helpers on the CPU: the relMSE definition and the
-time-to-plain-relMSE interpolation (bench.interpolate_to_target), checked on
+time-to-plain-relMSE fit (bench.fit_to_target), checked on
 synthetic points of a known error model err(n) = V / n + B and time
 t(n) = a + b n, where the answer has a closed form."""
 import os
@@ -24,41 +24,40 @@ def _points(spps, V, B, a, b):
     return [(n, a + b * n, V / n + B) for n in spps]
 
 
-def test_interpolation_hits_a_point_exactly():
-    pts = _points([128, 256, 512], 1.0, 0.0, 10.0, 2.0)
-    n, t, reached = bench.interpolate_to_target(pts, 1.0 / 256)
-    assert reached and n == pytest.approx(256.0) and t == pytest.approx(10.0 + 2.0 * 256)
-
-
-def test_interpolation_is_exact_for_a_power_law():
-    # err = V / n is a straight line in log-log: the interpolated spp is exact
+def test_fit_is_exact_for_a_power_law():
+    # err = V / n is a line of slope -1 in log-log: the crossing is exact
     V, a, b = 3.0, 40.0, 0.9
-    pts = _points([100, 400], V, 0.0, a, b)
-    target = V / 250.0
-    n, t, reached = bench.interpolate_to_target(pts, target)
+    pts = _points([100, 400, 1600], V, 0.0, a, b)
+    n, t, reached = bench.fit_to_target(pts, V / 250.0)
     assert reached
     assert n == pytest.approx(250.0, rel=1e-9)
     assert t == pytest.approx(a + b * 250.0, rel=1e-9)
 
 
-def test_interpolation_with_a_bias_floor_stays_between_the_brackets():
+def test_fit_with_a_bias_floor_uses_the_points_near_the_crossing():
     V, B, a, b = 1.0, 2e-4, 20.0, 0.5
-    pts = _points([200, 500, 900, 1400], V, B, a, b)
-    target = V / 700.0 + B  # exact answer: 700 spp
-    n, t, reached = bench.interpolate_to_target(pts, target)
-    assert reached and 500 < n < 900
-    # log-log interpolation of a curve that flattens toward B is close, not exact
-    assert n == pytest.approx(700.0, rel=0.05)
-    assert t == pytest.approx(a + b * n, rel=1e-9)
+    pts = _points([100, 200, 500, 800, 1400, 4000], V, B, a, b)
+    n, t, reached = bench.fit_to_target(pts, V / 700.0 + B)  # exact answer: 700 spp
+    assert reached and n == pytest.approx(700.0, rel=0.05)
+    assert t == pytest.approx(a + b * n, rel=1e-6)
 
 
-def test_interpolation_points_unsorted_and_out_of_range():
-    pts = _points([800, 200, 400], 1.0, 0.0, 0.0, 1.0)
-    n, _, reached = bench.interpolate_to_target(pts, 1.0 / 300)
-    assert reached and n == pytest.approx(300.0, rel=1e-9)
-    # every point above the target: the largest spp, not reached
-    n, t, reached = bench.interpolate_to_target(pts, 1e-6)
-    assert not reached and n == 800.0 and t == 800.0
-    # every point below the target: the smallest spp, reached
-    n, t, reached = bench.interpolate_to_target(pts, 1.0)
-    assert reached and n == 200.0
+def test_fit_tolerates_one_noisy_point():
+    # three points on err = 1/n and one 25 % high: the answer moves little
+    pts = _points([300, 500, 700], 1.0, 0.0, 0.0, 1.0) + [(600, 600.0, 1.25 / 600)]
+    n, _, _ = bench.fit_to_target(pts, 1.0 / 550)
+    assert n == pytest.approx(550.0, rel=0.12)
+
+
+def test_fit_clamps_a_rising_slope():
+    # noise can make the error rise with spp between two points; the slope is
+    # then held at -0.2, so the crossing lies below both points
+    pts = [(1024, 367.0, 2.57e-4), (1344, 474.0, 3.09e-4)]
+    n, t, reached = bench.fit_to_target(pts, 3.23e-4)
+    assert reached and 200 < n < 1024 and 0 < t < 367.0
+
+
+def test_fit_all_points_above_the_target():
+    pts = _points([100, 200], 1.0, 0.0, 0.0, 1.0)
+    n, t, reached = bench.fit_to_target(pts, 1.0 / 800)
+    assert not reached and n == pytest.approx(800.0, rel=1e-9) and t == pytest.approx(800.0)
