@@ -76,3 +76,19 @@ def test_ctypes_mirror_matches_c(built, c_layout, struct):
     assert [getattr(py, n).offset for n in names] == offsets
     assert C.sizeof(py) == size
 
+
+
+def test_learned_parameter_names_are_checked():
+    """The learned renderers' keyword parameters go into the C structs by
+    name: a known name sets the field, an unknown one (a typo) raises rather
+    than being dropped silently."""
+    import tpt
+
+    n = tpt.NrcParams()
+    tpt._set_fields(n, {"train_steps": 7, "spread_c": 0.5}, "tpt_nrc_params")
+    assert n.train_steps == 7 and abs(n.spread_c - 0.5) < 1e-7
+    with pytest.raises(TypeError, match="train_step"):
+        tpt._set_fields(n, {"train_step": 7}, "tpt_nrc_params")
+    g = tpt.GuideParams()
+    with pytest.raises(TypeError, match="alpah"):
+        tpt._set_fields(g, {"alpah": 0.25}, "tpt_guide_params")

@@ -414,19 +414,31 @@ class Context:
         return None
 
 
+def _set_fields(struct, values: dict, name: str) -> None:
+    """Sets the named fields of a ctypes struct; a name that is not one of
+    its fields raises (setattr alone would add a Python attribute the C side
+    never sees)."""
+    known = {f for f, _ in type(struct)._fields_}
+    unknown = sorted(set(values) - known)
+    if unknown:
+        raise TypeError(f"{name} has no field(s) {', '.join(unknown)}; fields: {', '.join(sorted(known))}")
+    for k, v in values.items():
+        setattr(struct, k, v)
+
+
 def render_guided(ctx: "Context", slot: int, width: int, height: int, spp: int, max_depth: int = 50,
                   background: int = BACKGROUND_BLACK, seed: int = 1, out=None, refill: int = 0, engine: int = 0,
                   **guide):
     """Learned path guiding (physical semantics).  guide: fields of
     tpt_guide_params (passes, train_steps, batch, lr, grid_res, alpha,
-    record_cap, seed).  out: None (host image returned) or a device pointer.
+    record_cap, seed, light_share, warm_start; another name raises
+    TypeError).  out: None (host image returned) or a device pointer.
     Returns (image or None, render stats, guide stats)."""
     p = make_params(width, height, spp, max_depth, SEMANTICS_PHYSICAL, background, 1.0, seed, engine=engine,
                     refill=refill)
     g = GuideParams()
     lib().tpt_guide_params_default(C.byref(g))
-    for k, v in guide.items():
-        setattr(g, k, v)
+    _set_fields(g, guide, "tpt_guide_params")
     img = np.zeros((height, width, 3), np.float32) if out is None else None
     dst, mem = (_ptr(img), TPT_MEM_HOST) if out is None else (C.c_void_p(int(out)), TPT_MEM_DEVICE)
     st, gs = RenderStats(), GuideStats()
@@ -511,14 +523,14 @@ def guide_records(ctx: "Context", cap: int = 1 << 22) -> np.ndarray:
 def render_nrc(ctx: "Context", slot: int, width: int, height: int, spp: int, max_depth: int = 50,
                semantics: int = SEMANTICS_PHYSICAL, background: int = BACKGROUND_BLACK, seed: int = 1, out=None,
                refill: int = 0, engine: int = 0, **nrc):
-    """Neural radiance cache render.  nrc: fields of tpt_nrc_params.  out:
-    None (host image returned) or a device pointer.
+    """Neural radiance cache render.  nrc: fields of tpt_nrc_params (another
+    name raises TypeError).  out: None (host image returned) or a device
+    pointer.
     Returns (image or None, render stats, cache stats)."""
     p = make_params(width, height, spp, max_depth, semantics, background, 1.0, seed, engine=engine, refill=refill)
     n = NrcParams()
     lib().tpt_nrc_params_default(C.byref(n))
-    for k, v in nrc.items():
-        setattr(n, k, v)
+    _set_fields(n, nrc, "tpt_nrc_params")
     img = np.zeros((height, width, 3), np.float32) if out is None else None
     dst, mem = (_ptr(img), TPT_MEM_HOST) if out is None else (C.c_void_p(int(out)), TPT_MEM_DEVICE)
     st, ns = RenderStats(), NrcStats()
