@@ -325,8 +325,9 @@ tpt_status tpt_autotune_batch(tpt_context *ctx, const tpt_batch_item *items, int
                               int32_t spp_divisor, double *best_msps);
 
 /* ------------------------------------------------------------------------
- * Learned parts: fully fused FP16 MLPs on the tensor cores (FP32
- * accumulation), in -> [64, ReLU] x n_hidden -> out, no biases, weights
+ * Learned parts: fully fused FP16 MLPs on the 5th-generation tensor cores
+ * (tcgen05.mma, FP32 accumulators in tensor memory; training and inference
+ * alike), in -> [64, ReLU] x n_hidden -> out, no biases, weights
  * row-major [out][in] per layer, concatenated.  Supported shapes:
  * (112, 3, 48) path-guiding network, (64, 5, 16) radiance cache,
  * (32, 2, 16) test network.  Batches are device buffers of `rows` rows,
